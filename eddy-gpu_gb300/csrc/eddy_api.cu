@@ -1,0 +1,771 @@
+// eddy_api.cu -- the C ABI of libeddy_gpu (include/eddy_gpu.h): context,
+// gene sets, the permutation driver (main.cu:538-1502) and device buffers.
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdarg.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <algorithm>
+#include <string>
+#include <vector>
+
+#include "../../include/eddy_gpu.h"
+#include "eddy_host.h"
+#include "eddy_internal.h"
+#include "eddy_kernels.h"
+
+using namespace eddy;
+
+namespace {
+
+struct DevBuf {
+  void *p = nullptr;
+  size_t n = 0;
+  cudaError_t ensure(size_t bytes) {
+    if (bytes <= n) return cudaSuccess;
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+    cudaError_t e = cudaMalloc(&p, bytes);
+    if (e == cudaSuccess) n = bytes;
+    return e;
+  }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+  }
+  template <class T>
+  T *as() const {
+    return reinterpret_cast<T *>(p);
+  }
+};
+
+struct SetHost {
+  std::vector<int32_t> genes;
+  std::vector<uint8_t> prior;  // g*g or empty
+  std::vector<uint8_t> labels; // external labellings R x n
+  int R_ext = 0;
+  bool done = false;
+  std::vector<double> js;
+  std::vector<int32_t> U;
+  int iterations = 0, failed = 0, betafit_ok = 0;
+  double alpha = NAN, beta = NAN, pddn = NAN;
+  unsigned long long exact = 0, tables = 0;
+  // iteration-0 networks
+  int U0 = 0;
+  std::vector<int32_t> ids, nodes, epn, edges;
+  std::vector<double> lval;
+  std::vector<int32_t> el_nodes, el_epn, el_edges;
+};
+
+}  // namespace
+
+struct eddy_ctx {
+  eddy_opts o{};
+  std::string err = "";
+  int genes = 0, samples = 0, nA = 0, nB = 0, W = 0;
+  std::vector<int8_t> data;
+  std::vector<uint8_t> labels0;
+  std::vector<SetHost> sets;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+  GlibcRand rng{1};
+  std::vector<uint8_t> seen;
+  std::vector<int> order;
+  // device data
+  DevBuf d_lg, d_vals, d_planes, d_valid, d_ctot, d_prior, d_mask0;
+  DevBuf d_masks, d_dmask, d_scratch, d_js, d_U, d_status, d_keep, d_uset, d_uperm;
+  DevBuf d_oids, d_ocnt, d_opar, d_odist, d_olval, d_orows, d_stats;
+  int lg_shift = 0;
+  bool lg_ready = false;
+  // timing of the last run
+  double ms_total = 0, ms_pairs = 0, ms_units = 0;
+  long long launches = 0;
+  uint64_t salt = 0x5EED5EEDull;
+};
+
+static int fail(eddy_ctx *c, int code, const char *fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof buf, fmt, ap);
+  va_end(ap);
+  if (c) c->err = buf;
+  return code;
+}
+
+#define CK(call)                                                                            \
+  do {                                                                                      \
+    cudaError_t e_ = (call);                                                                \
+    if (e_ != cudaSuccess)                                                                  \
+      return fail(ctx, EDDY_ERR_CUDA, "%s: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, \
+                  __LINE__);                                                                \
+  } while (0)
+
+namespace {
+
+// Device state of the current set.
+struct SetRun {
+  SetDev sd{};
+  int set_id = -1;
+};
+
+int prepare_set(eddy_ctx *ctx, int set_id, SetRun &sr) {
+  SetHost &S = ctx->sets[set_id];
+  const int g = (int)S.genes.size(), n = ctx->samples, W = ctx->W;
+  const int c = g * (g - 1) / 2;
+  if (g > 512) return fail(ctx, EDDY_ERR_CAPACITY, "gene set %d has %d genes (> 512)", set_id, g);
+  CK(cudaSetDevice(ctx->o.device));
+  if (!ctx->lg_ready) {
+    std::vector<int64_t> lg;
+    int8_t dmap[82];
+    bdeu_table(n, lg, ctx->lg_shift, dmap);
+    CK(ctx->d_lg.ensure(lg.size() * sizeof(int64_t)));
+    CK(cudaMemcpy(ctx->d_lg.p, lg.data(), lg.size() * sizeof(int64_t), cudaMemcpyHostToDevice));
+    CK(set_divisor_map(dmap));
+    ctx->lg_ready = true;
+  }
+  std::vector<int8_t> vals((size_t)g * n);
+  bool all_valid = true;
+  for (int i = 0; i < g; i++) {
+    const int8_t *src = ctx->data.data() + (size_t)S.genes[i] * n;
+    memcpy(vals.data() + (size_t)i * n, src, n);
+    for (int s = 0; s < n; s++)
+      if (src[s] < -1 || src[s] > 1) all_valid = false;
+  }
+  std::vector<uint8_t> pbits(c > 0 ? c : 1, 0);
+  if (!S.prior.empty()) {
+    int p = 0;
+    for (int r = 1; r < g; r++)
+      for (int col = 0; col < r; col++, p++) pbits[p] = S.prior[(size_t)r * g + col] == 1 ? 1 : 0;
+  }
+  CK(ctx->d_vals.ensure(vals.size() + 16));
+  CK(ctx->d_planes.ensure(sizeof(uint64_t) * (size_t)g * 3 * W));
+  CK(ctx->d_valid.ensure(sizeof(uint64_t) * W));
+  CK(ctx->d_ctot.ensure(sizeof(uint16_t) * 9 * (size_t)(c > 0 ? c : 1)));
+  CK(ctx->d_prior.ensure(pbits.size()));
+  CK(cudaMemcpyAsync(ctx->d_vals.p, vals.data(), vals.size(), cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemcpyAsync(ctx->d_prior.p, pbits.data(), pbits.size(), cudaMemcpyHostToDevice, ctx->stream));
+  CK(launch_prep(ctx->d_vals.as<int8_t>(), g, n, W, c, ctx->d_planes.as<uint64_t>(),
+                 ctx->d_valid.as<uint64_t>(), ctx->d_ctot.as<uint16_t>(), ctx->stream));
+  ctx->launches += 1 + (c > 0);
+  SetDev &sd = sr.sd;
+  sd = SetDev{};
+  sd.g = g;
+  sd.n = n;
+  sd.W = W;
+  sd.c = c;
+  sd.nA = ctx->nA;
+  sd.nB = ctx->nB;
+  sd.S = n + 2;
+  sd.mp = ctx->o.max_parents;
+  sd.GW = (g + 31) / 32;
+  sd.bonf = ctx->o.bonferroni ? 1 : 0;
+  sd.alpha_edge = ctx->o.alpha_edge;
+  sd.alpha_edge_prior = ctx->o.alpha_edge_prior;
+  sd.exact_all = compute_thresholds(sd.alpha_edge, sd.alpha_edge_prior, g, sd.bonf, sd.thr) ? 1 : 0;
+  sd.all_valid = all_valid ? 1 : 0;
+  sd.planes = ctx->d_planes.as<uint64_t>();
+  sd.valid = ctx->d_valid.as<uint64_t>();
+  sd.vals = ctx->d_vals.as<int8_t>();
+  sd.ctot = ctx->d_ctot.as<uint16_t>();
+  sd.prior = ctx->d_prior.as<uint8_t>();
+  sd.lg = ctx->d_lg.as<int64_t>();
+  sd.lg_stride = n + 1;
+  sd.lg_shift = ctx->lg_shift;
+  sd.salt = ctx->salt;
+  sr.set_id = set_id;
+  return EDDY_OK;
+}
+
+void labels_to_mask(const uint8_t *labels, int n, int W, uint64_t *mask) {
+  for (int w = 0; w < W; w++) mask[w] = 0;
+  for (int s = 0; s < n; s++)
+    if (labels[s] == 0) mask[s >> 6] |= 1ull << (s & 63);
+}
+
+// Detailed outputs of one kept unit (host copies).
+struct KeepOut {
+  int U = 0;
+  std::vector<int32_t> ids, cnt, par;
+  std::vector<double> dist, lval;
+  std::vector<uint32_t> rows;
+  int mpk = 0;
+};
+
+// Runs units of one set.  masks_host: B x W host masks, or null to
+// generate counter-mode masks for perms[] on the device.
+int run_units(eddy_ctx *ctx, SetRun &sr, int nunits, const uint64_t *masks_host,
+              const int32_t *perms, double *js, int32_t *U, KeepOut *keep, int mpk_req) {
+  SetDev &sd = sr.sd;
+  const int W = sd.W, c = sd.c, S = sd.S, g = sd.g;
+  const bool keeping = keep != nullptr;
+  // batch size: bounded by memory (~3 GB for masks, decisions and scratch)
+  int kmax = 16;
+  size_t per_unit = unit_scratch_bytes(c, S, kmax) + sizeof(uint32_t) * (size_t)c + 8 * W + 64;
+  int Bmax = (int)std::max<size_t>(1, ((size_t)3 << 30) / std::max<size_t>(per_unit, 1));
+  Bmax = std::min(Bmax, 4096);
+  if (keeping) Bmax = 1;
+  std::vector<uint32_t> status;
+  std::vector<int32_t> uset, uperm;
+  const int mpk = std::max(1, mpk_req);
+  if (keeping) {
+    CK(ctx->d_oids.ensure(sizeof(int32_t) * S));
+    CK(ctx->d_ocnt.ensure(sizeof(int32_t) * (size_t)S * g));
+    CK(ctx->d_opar.ensure(sizeof(int32_t) * (size_t)S * g * mpk));
+    CK(ctx->d_odist.ensure(sizeof(double) * 2 * S));
+    CK(ctx->d_olval.ensure(sizeof(double) * 2 * S));
+    CK(ctx->d_orows.ensure(sizeof(uint32_t) * 2 * (size_t)g * sd.GW));
+    CK(cudaMemsetAsync(ctx->d_opar.p, 0xff, sizeof(int32_t) * (size_t)S * g * mpk, ctx->stream));
+  }
+  CK(ctx->d_stats.ensure(sizeof(unsigned long long) * 4));
+  CK(cudaMemsetAsync(ctx->d_stats.p, 0, sizeof(unsigned long long) * 4, ctx->stream));
+  float t_pairs = 0, t_units = 0;
+  for (int b0 = 0; b0 < nunits; b0 += Bmax) {
+    const int B = std::min(Bmax, nunits - b0);
+    int kmax_run = kmax;
+    std::vector<int> todo(B);
+    for (int i = 0; i < B; i++) todo[i] = i;
+    // the batch is run once; units whose status asks for it are re-run
+    for (int attempt = 0; attempt < 4 && !todo.empty(); attempt++) {
+      const int Bt = (int)todo.size();
+      const size_t ub = unit_scratch_bytes(c, S, kmax_run);
+      CK(ctx->d_masks.ensure(sizeof(uint64_t) * (size_t)Bt * W));
+      CK(ctx->d_dmask.ensure(sizeof(uint32_t) * (size_t)Bt * (c > 0 ? c : 1)));
+      CK(ctx->d_scratch.ensure(ub * Bt));
+      CK(ctx->d_js.ensure(sizeof(double) * Bt));
+      CK(ctx->d_U.ensure(sizeof(int32_t) * Bt));
+      CK(ctx->d_status.ensure(sizeof(uint32_t) * Bt));
+      CK(ctx->d_keep.ensure(sizeof(int32_t) * Bt));
+      if (masks_host) {
+        std::vector<uint64_t> mh((size_t)Bt * W);
+        for (int i = 0; i < Bt; i++)
+          memcpy(mh.data() + (size_t)i * W, masks_host + (size_t)(b0 + todo[i]) * W, 8 * W);
+        CK(cudaMemcpyAsync(ctx->d_masks.p, mh.data(), 8 * mh.size(), cudaMemcpyHostToDevice, ctx->stream));
+      } else {
+        uset.assign(Bt, sr.set_id);
+        uperm.resize(Bt);
+        for (int i = 0; i < Bt; i++) uperm[i] = perms[b0 + todo[i]];
+        CK(ctx->d_uset.ensure(sizeof(int32_t) * Bt));
+        CK(ctx->d_uperm.ensure(sizeof(int32_t) * Bt));
+        CK(cudaMemcpyAsync(ctx->d_uset.p, uset.data(), 4 * Bt, cudaMemcpyHostToDevice, ctx->stream));
+        CK(cudaMemcpyAsync(ctx->d_uperm.p, uperm.data(), 4 * Bt, cudaMemcpyHostToDevice, ctx->stream));
+        CK(launch_counter_masks(sd.n, sd.nA, W, ctx->o.seed, ctx->d_uset.as<int32_t>(),
+                                ctx->d_uperm.as<int32_t>(), ctx->d_mask0.as<uint64_t>(),
+                                ctx->d_masks.as<uint64_t>(), Bt, ctx->stream));
+        ctx->launches++;
+      }
+      std::vector<int32_t> ks(Bt, -1);
+      if (keeping) ks[0] = 0;
+      CK(cudaMemcpyAsync(ctx->d_keep.p, ks.data(), 4 * Bt, cudaMemcpyHostToDevice, ctx->stream));
+      BatchDev bd{};
+      bd.B = Bt;
+      bd.kmax = kmax_run;
+      bd.masks = ctx->d_masks.as<uint64_t>();
+      bd.dmask = ctx->d_dmask.as<uint32_t>();
+      bd.scratch = ctx->d_scratch.as<uint8_t>();
+      bd.unit_bytes = ub;
+      bd.js = ctx->d_js.as<double>();
+      bd.U = ctx->d_U.as<int32_t>();
+      bd.status = ctx->d_status.as<uint32_t>();
+      bd.keep_slot = ctx->d_keep.as<int32_t>();
+      bd.out_ids = ctx->d_oids.as<int32_t>();
+      bd.out_cnt = ctx->d_ocnt.as<int32_t>();
+      bd.out_par = ctx->d_opar.as<int32_t>();
+      bd.mpk = mpk;
+      bd.out_dist = ctx->d_odist.as<double>();
+      bd.out_lval = ctx->d_olval.as<double>();
+      bd.out_rows = ctx->d_orows.as<uint32_t>();
+      bd.stats = ctx->d_stats.as<unsigned long long>();
+      CK(cudaEventRecord(ctx->ev[0], ctx->stream));
+      CK(launch_pairs(sd, bd.masks, ctx->d_dmask.as<uint32_t>(), Bt, bd.stats, ctx->stream));
+      CK(cudaEventRecord(ctx->ev[1], ctx->stream));
+      CK(launch_units(sd, bd, ctx->stream));
+      CK(cudaEventRecord(ctx->ev[2], ctx->stream));
+      ctx->launches += 2;
+      std::vector<double> jsb(Bt);
+      std::vector<int32_t> Ub(Bt);
+      status.assign(Bt, 0);
+      CK(cudaMemcpyAsync(jsb.data(), ctx->d_js.p, 8 * Bt, cudaMemcpyDeviceToHost, ctx->stream));
+      CK(cudaMemcpyAsync(Ub.data(), ctx->d_U.p, 4 * Bt, cudaMemcpyDeviceToHost, ctx->stream));
+      CK(cudaMemcpyAsync(status.data(), ctx->d_status.p, 4 * Bt, cudaMemcpyDeviceToHost, ctx->stream));
+      CK(cudaStreamSynchronize(ctx->stream));
+      float a = 0, bms = 0;
+      cudaEventElapsedTime(&a, ctx->ev[0], ctx->ev[1]);
+      cudaEventElapsedTime(&bms, ctx->ev[1], ctx->ev[2]);
+      t_pairs += a;
+      t_units += bms;
+      std::vector<int> again;
+      bool overflow = false, collision = false;
+      for (int i = 0; i < Bt; i++) {
+        const int u = b0 + todo[i];
+        if (status[i] & kUnitKmaxOverflow) {
+          overflow = true;
+          again.push_back(todo[i]);
+        } else if (status[i] & kUnitHashCollision) {
+          collision = true;
+          again.push_back(todo[i]);
+        } else {
+          js[u] = jsb[i];
+          U[u] = Ub[i];
+        }
+      }
+      if (keeping && again.empty()) {
+        keep->mpk = mpk;
+        keep->U = Ub[0];
+        const int Uk = Ub[0];
+        keep->ids.resize(Uk);
+        keep->cnt.resize((size_t)Uk * g);
+        keep->par.resize((size_t)Uk * g * mpk);
+        keep->dist.resize(2 * (size_t)S);
+        keep->lval.resize(2 * (size_t)S);
+        keep->rows.resize(2 * (size_t)g * sd.GW);
+        CK(cudaMemcpy(keep->ids.data(), ctx->d_oids.p, 4 * Uk, cudaMemcpyDeviceToHost));
+        CK(cudaMemcpy(keep->cnt.data(), ctx->d_ocnt.p, 4 * (size_t)Uk * g, cudaMemcpyDeviceToHost));
+        CK(cudaMemcpy(keep->par.data(), ctx->d_opar.p, 4 * (size_t)Uk * g * mpk, cudaMemcpyDeviceToHost));
+        CK(cudaMemcpy(keep->dist.data(), ctx->d_odist.p, 16 * (size_t)S, cudaMemcpyDeviceToHost));
+        CK(cudaMemcpy(keep->lval.data(), ctx->d_olval.p, 16 * (size_t)S, cudaMemcpyDeviceToHost));
+        CK(cudaMemcpy(keep->rows.data(), ctx->d_orows.p, 4 * keep->rows.size(), cudaMemcpyDeviceToHost));
+      }
+      if (overflow) kmax_run = g + 1;
+      if (collision) {
+        ctx->salt = ctx->salt * 6364136223846793005ull + 1442695040888963407ull;
+        sd.salt = ctx->salt;
+      }
+      todo.swap(again);
+    }
+    if (!todo.empty())
+      return fail(ctx, EDDY_ERR_INTERNAL, "units of set %d did not converge (status %u)", sr.set_id,
+                  status.empty() ? 0u : status[0]);
+  }
+  ctx->ms_pairs += t_pairs;
+  ctx->ms_units += t_units;
+  ctx->ms_total += t_pairs + t_units;
+  return EDDY_OK;
+}
+
+// Capped or uncapped parent lists of a network given by its row bitsets.
+void rows_to_lists(const uint32_t *rows, int g, int GW, int cap, std::vector<int32_t> &nodes,
+                   std::vector<int32_t> &edges) {
+  int run = 0;
+  for (int t = 0; t < g; t++) {
+    nodes.push_back(run);
+    int cnt = 0;
+    for (int j = 0; j < t && cnt < cap; j++)
+      if ((rows[(size_t)t * GW + (j >> 5)] >> (j & 31)) & 1u) {
+        edges.push_back(j);
+        cnt++;
+      }
+    run += cnt;
+  }
+}
+
+int store_keep(eddy_ctx *ctx, SetHost &S, const KeepOut &K, int g) {
+  (void)ctx;
+  S.U0 = K.U;
+  S.ids.assign(K.ids.begin(), K.ids.end());
+  S.nodes.assign((size_t)K.U * g, 0);
+  S.epn.assign(K.U + 1, 0);
+  S.edges.clear();
+  for (int u = 0; u < K.U; u++) {
+    int run = 0;
+    for (int t = 0; t < g; t++) {
+      S.nodes[(size_t)u * g + t] = run;
+      const int cnt = K.cnt[(size_t)u * g + t];
+      for (int k = 0; k < cnt && k < K.mpk; k++) S.edges.push_back(K.par[((size_t)u * g + t) * K.mpk + k]);
+      run += cnt;
+    }
+    S.epn[u + 1] = S.epn[u] + run;
+  }
+  const int Sn = (int)K.dist.size() / 2;
+  S.lval.assign(2 * (size_t)K.U, 0.0);
+  for (int u = 0; u < K.U; u++) {
+    S.lval[u] = K.lval[u];
+    S.lval[K.U + u] = K.lval[Sn + u];
+  }
+  // uncapped lists of the two full networks (main.cu:1530-1617)
+  const int GW = (g + 31) / 32;
+  S.el_nodes.clear();
+  S.el_edges.clear();
+  std::vector<int32_t> e0, e1;
+  rows_to_lists(K.rows.data(), g, GW, 0x7fffffff, S.el_nodes, e0);
+  rows_to_lists(K.rows.data() + (size_t)g * GW, g, GW, 0x7fffffff, S.el_nodes, e1);
+  S.el_epn = {0, (int32_t)e0.size(), (int32_t)(e0.size() + e1.size())};
+  S.el_edges = e0;
+  S.el_edges.insert(S.el_edges.end(), e1.begin(), e1.end());
+  return EDDY_OK;
+}
+
+bool finite_js(double v) { return !isnan(v); }
+
+}  // namespace
+
+// ================================================================= C ABI
+extern "C" {
+
+int eddy_ctx_create(const eddy_opts *opts, eddy_ctx **out) {
+  if (!opts || !out) return EDDY_ERR_ARG;
+  *out = nullptr;
+  if (opts->max_parents < 1 || opts->permutations < 1) return EDDY_ERR_ARG;
+  if (opts->rng < EDDY_RNG_GLIBC || opts->rng > EDDY_RNG_EXTERNAL) return EDDY_ERR_ARG;
+  eddy_ctx *ctx = new eddy_ctx();
+  ctx->o = *opts;
+  int ndev = 0;
+  cudaError_t e = cudaGetDeviceCount(&ndev);
+  if (e != cudaSuccess || opts->device < 0 || opts->device >= ndev) {
+    delete ctx;
+    return EDDY_ERR_CUDA;
+  }
+  if (cudaSetDevice(opts->device) != cudaSuccess || cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess) {
+    delete ctx;
+    return EDDY_ERR_CUDA;
+  }
+  for (auto &ev : ctx->ev) cudaEventCreate(&ev);
+  *out = ctx;
+  return EDDY_OK;
+}
+
+int eddy_ctx_destroy(eddy_ctx *ctx) {
+  if (!ctx) return EDDY_ERR_ARG;
+  cudaSetDevice(ctx->o.device);
+  if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+  DevBuf *bufs[] = {&ctx->d_lg, &ctx->d_vals, &ctx->d_planes, &ctx->d_valid, &ctx->d_ctot,
+                    &ctx->d_prior, &ctx->d_mask0, &ctx->d_masks, &ctx->d_dmask, &ctx->d_scratch,
+                    &ctx->d_js, &ctx->d_U, &ctx->d_status, &ctx->d_keep, &ctx->d_uset,
+                    &ctx->d_uperm, &ctx->d_oids, &ctx->d_ocnt, &ctx->d_opar, &ctx->d_odist,
+                    &ctx->d_olval, &ctx->d_orows, &ctx->d_stats};
+  for (DevBuf *b : bufs) b->release();
+  for (auto &ev : ctx->ev)
+    if (ev) cudaEventDestroy(ev);
+  if (ctx->stream) cudaStreamDestroy(ctx->stream);
+  delete ctx;
+  return EDDY_OK;
+}
+
+const char *eddy_last_error(const eddy_ctx *ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+
+int eddy_load_matrix(eddy_ctx *ctx, const int8_t *data, int genes, int samples,
+                     const uint8_t *class_of_sample) {
+  if (!ctx) return EDDY_ERR_ARG;
+  if (!data || !class_of_sample || genes < 1 || samples < 2)
+    return fail(ctx, EDDY_ERR_ARG, "bad matrix shape %d x %d", genes, samples);
+  int nA = 0, nB = 0;
+  for (int s = 0; s < samples; s++) {
+    if (class_of_sample[s] == 0) nA++;
+    else if (class_of_sample[s] == 1) nB++;
+    else return fail(ctx, EDDY_ERR_ARG, "class label of sample %d is neither 0 nor 1", s);
+  }
+  if (nA == 0 || nB == 0) return fail(ctx, EDDY_ERR_ARG, "labels hold a single class");
+  ctx->genes = genes;
+  ctx->samples = samples;
+  ctx->nA = nA;
+  ctx->nB = nB;
+  ctx->W = (samples + 63) / 64;
+  ctx->data.assign(data, data + (size_t)genes * samples);
+  ctx->labels0.assign(class_of_sample, class_of_sample + samples);
+  ctx->lg_ready = false;
+  std::vector<uint64_t> m0(ctx->W);
+  labels_to_mask(ctx->labels0.data(), samples, ctx->W, m0.data());
+  CK(cudaSetDevice(ctx->o.device));
+  CK(ctx->d_mask0.ensure(8 * m0.size()));
+  CK(cudaMemcpy(ctx->d_mask0.p, m0.data(), 8 * m0.size(), cudaMemcpyHostToDevice));
+  return EDDY_OK;
+}
+
+int eddy_add_set(eddy_ctx *ctx, const int32_t *gene_idx, int g, const uint8_t *prior, int *set_id) {
+  if (!ctx) return EDDY_ERR_ARG;
+  if (ctx->samples == 0) return fail(ctx, EDDY_ERR_STATE, "load the matrix first");
+  if (!gene_idx || g < 0) return fail(ctx, EDDY_ERR_ARG, "bad gene set");
+  if (g > 512) return fail(ctx, EDDY_ERR_CAPACITY, "gene set of %d genes (> 512)", g);
+  SetHost S;
+  S.genes.assign(gene_idx, gene_idx + g);
+  for (int v : S.genes)
+    if (v < 0 || v >= ctx->genes) return fail(ctx, EDDY_ERR_ARG, "gene index %d out of range", v);
+  if (prior) S.prior.assign(prior, prior + (size_t)g * g);
+  ctx->sets.push_back(std::move(S));
+  if (set_id) *set_id = (int)ctx->sets.size() - 1;
+  return EDDY_OK;
+}
+
+int eddy_set_labellings(eddy_ctx *ctx, int set_id, const uint8_t *labels, int R) {
+  if (!ctx) return EDDY_ERR_ARG;
+  if (set_id < 0 || set_id >= (int)ctx->sets.size() || !labels || R < 1)
+    return fail(ctx, EDDY_ERR_ARG, "bad labellings");
+  for (long i = 0; i < (long)R * ctx->samples; i++)
+    if (labels[i] > 1) return fail(ctx, EDDY_ERR_ARG, "labels must be 0/1");
+  SetHost &S = ctx->sets[set_id];
+  S.labels.assign(labels, labels + (size_t)R * ctx->samples);
+  S.R_ext = R;
+  return EDDY_OK;
+}
+
+static int run_set(eddy_ctx *ctx, int set_id) {
+  SetHost &S = ctx->sets[set_id];
+  const int n = ctx->samples, W = ctx->W;
+  const int g = (int)S.genes.size();
+  int R = ctx->o.permutations;
+  if (ctx->o.rng == EDDY_RNG_EXTERNAL) {
+    if (S.R_ext < 1) return fail(ctx, EDDY_ERR_STATE, "set %d has no labellings", set_id);
+    R = S.R_ext;
+  }
+  S.js.assign(R, NAN);
+  S.U.assign(R, 0);
+  S.iterations = 0;
+  S.failed = 0;
+  S.betafit_ok = 0;
+  S.exact = S.tables = 0;
+  if (g < 2) {
+    // no pair: every network is empty, U = 1, JS is NaN (main.cu:1431)
+    S.js[0] = NAN;
+    S.U[0] = 1;
+    S.iterations = 1;
+    S.failed = 1;
+    S.U0 = 1;
+    if (ctx->o.rng == EDDY_RNG_GLIBC) {
+      std::vector<uint8_t> lab(ctx->labels0);
+      glibc_permutation(ctx->rng, n, ctx->nA, false, lab.data(), ctx->seen, ctx->order);
+    }
+    S.done = true;
+    return EDDY_OK;
+  }
+  SetRun sr;
+  int rc = prepare_set(ctx, set_id, sr);
+  if (rc) return rc;
+  // iteration 0 (kept: networks and likelihoods for the output files)
+  std::vector<uint64_t> masks((size_t)W);
+  std::vector<uint8_t> lab(ctx->labels0);
+  if (ctx->o.rng == EDDY_RNG_EXTERNAL) lab.assign(S.labels.begin(), S.labels.begin() + n);
+  if (ctx->o.rng == EDDY_RNG_GLIBC)
+    glibc_permutation(ctx->rng, n, ctx->nA, false, lab.data(), ctx->seen, ctx->order);
+  labels_to_mask(lab.data(), n, W, masks.data());
+  KeepOut K;
+  const int mpk = std::min(ctx->o.max_parents, std::max(g - 1, 1));
+  rc = run_units(ctx, sr, 1, masks.data(), nullptr, S.js.data(), S.U.data(),
+                 ctx->o.keep_networks ? &K : nullptr, mpk);
+  if (rc) return rc;
+  if (ctx->o.keep_networks) store_keep(ctx, S, K, g);
+  else S.U0 = S.U[0];
+  S.iterations = 1;
+  if (!finite_js(S.js[0])) {
+    S.failed = 1;
+    S.done = true;
+    return EDDY_OK;  // main.cu:1431-1435: break after iteration 0
+  }
+  if (R > 1) {
+    const int nu = R - 1;
+    std::vector<int32_t> perms(nu);
+    for (int i = 0; i < nu; i++) perms[i] = i + 1;
+    const bool device_counter = ctx->o.rng == EDDY_RNG_COUNTER && n <= 4096;
+    std::vector<uint64_t> mh;
+    if (!device_counter) {
+      mh.assign((size_t)nu * W, 0);
+      std::vector<uint8_t> cur(ctx->labels0);
+      for (int i = 0; i < nu; i++) {
+        if (ctx->o.rng == EDDY_RNG_GLIBC) {
+          glibc_permutation(ctx->rng, n, ctx->nA, true, cur.data(), ctx->seen, ctx->order);
+        } else if (ctx->o.rng == EDDY_RNG_COUNTER) {
+          counter_labels(ctx->o.seed, set_id, i + 1, n, ctx->nA, cur.data());
+        } else {
+          memcpy(cur.data(), S.labels.data() + (size_t)(i + 1) * n, n);
+          int a = 0;
+          for (int s = 0; s < n; s++) a += cur[s] == 0;
+          if (a != ctx->nA) return fail(ctx, EDDY_ERR_ARG, "labelling %d changes the class sizes", i + 1);
+        }
+        labels_to_mask(cur.data(), n, W, mh.data() + (size_t)i * W);
+      }
+    }
+    rc = run_units(ctx, sr, nu, device_counter ? nullptr : mh.data(), perms.data(), S.js.data() + 1,
+                   S.U.data() + 1, nullptr, 1);
+    if (rc) return rc;
+  }
+  S.iterations = R;
+  unsigned long long st[4];
+  CK(cudaMemcpy(st, ctx->d_stats.p, sizeof st, cudaMemcpyDeviceToHost));
+  S.exact += st[0];
+  S.tables += st[1];
+  for (int i = 0; i < R; i++)
+    if (!finite_js(S.js[i])) S.failed = 1;
+  if (!S.failed) S.betafit_ok = beta_pddn(S.js.data(), R, S.alpha, S.beta, S.pddn) ? 1 : 0;
+  S.done = true;
+  return EDDY_OK;
+}
+
+int eddy_run(eddy_ctx *ctx) {
+  if (!ctx) return EDDY_ERR_ARG;
+  if (ctx->samples == 0) return fail(ctx, EDDY_ERR_STATE, "no matrix loaded");
+  ctx->ms_total = ctx->ms_pairs = ctx->ms_units = 0;
+  ctx->launches = 0;
+  for (int s = 0; s < (int)ctx->sets.size(); s++) {
+    if (ctx->sets[s].done) continue;
+    int rc = run_set(ctx, s);
+    if (rc) return rc;
+  }
+  return EDDY_OK;
+}
+
+int eddy_get_set_summary(const eddy_ctx *ctx, int set_id, eddy_set_summary *out) {
+  if (!ctx || !out || set_id < 0 || set_id >= (int)ctx->sets.size()) return EDDY_ERR_ARG;
+  const SetHost &S = ctx->sets[set_id];
+  if (!S.done) return EDDY_ERR_STATE;
+  out->genes = (int)S.genes.size();
+  out->iterations = S.iterations;
+  out->failed = S.failed;
+  out->betafit_ok = S.betafit_ok;
+  out->unique0 = S.U0;
+  out->js0 = S.js.empty() ? NAN : S.js[0];
+  out->alpha = S.alpha;
+  out->beta = S.beta;
+  out->pddn = S.pddn;
+  out->exact_rechecks = S.exact;
+  out->tables = S.tables;
+  return EDDY_OK;
+}
+
+int eddy_get_js(const eddy_ctx *ctx, int set_id, double *js, int32_t *unique) {
+  if (!ctx || set_id < 0 || set_id >= (int)ctx->sets.size()) return EDDY_ERR_ARG;
+  const SetHost &S = ctx->sets[set_id];
+  if (!S.done) return EDDY_ERR_STATE;
+  for (int i = 0; i < S.iterations; i++) {
+    if (js) js[i] = S.js[i];
+    if (unique) unique[i] = S.U[i];
+  }
+  return EDDY_OK;
+}
+
+int eddy_get_networks(const eddy_ctx *ctx, int set_id, int *U, int *edges, int32_t *ids,
+                      int32_t *nodes, int32_t *epn, int32_t *edges_out, double *lval) {
+  if (!ctx || set_id < 0 || set_id >= (int)ctx->sets.size()) return EDDY_ERR_ARG;
+  const SetHost &S = ctx->sets[set_id];
+  if (!S.done || S.ids.empty()) return EDDY_ERR_STATE;
+  if (U) *U = S.U0;
+  if (edges) *edges = (int)S.edges.size();
+  if (ids) memcpy(ids, S.ids.data(), 4 * S.ids.size());
+  if (nodes) memcpy(nodes, S.nodes.data(), 4 * S.nodes.size());
+  if (epn) memcpy(epn, S.epn.data(), 4 * S.epn.size());
+  if (edges_out) memcpy(edges_out, S.edges.data(), 4 * S.edges.size());
+  if (lval) memcpy(lval, S.lval.data(), 8 * S.lval.size());
+  return EDDY_OK;
+}
+
+int eddy_get_edge_list(const eddy_ctx *ctx, int set_id, int *edges, int32_t *nodes, int32_t *epn,
+                       int32_t *edges_out) {
+  if (!ctx || set_id < 0 || set_id >= (int)ctx->sets.size()) return EDDY_ERR_ARG;
+  const SetHost &S = ctx->sets[set_id];
+  if (!S.done || S.el_nodes.empty()) return EDDY_ERR_STATE;
+  if (edges) *edges = (int)S.el_edges.size();
+  if (nodes) memcpy(nodes, S.el_nodes.data(), 4 * S.el_nodes.size());
+  if (epn) memcpy(epn, S.el_epn.data(), 4 * S.el_epn.size());
+  if (edges_out) memcpy(edges_out, S.el_edges.data(), 4 * S.el_edges.size());
+  return EDDY_OK;
+}
+
+int eddy_run_labellings(eddy_ctx *ctx, int set_id, const uint8_t *labels, int R, double *js,
+                        int32_t *unique) {
+  if (!ctx) return EDDY_ERR_ARG;
+  if (set_id < 0 || set_id >= (int)ctx->sets.size() || !labels || R < 1 || !js || !unique)
+    return fail(ctx, EDDY_ERR_ARG, "bad arguments");
+  const int n = ctx->samples, W = ctx->W;
+  for (int r = 0; r < R; r++) {
+    int a = 0;
+    for (int s = 0; s < n; s++) a += labels[(size_t)r * n + s] == 0;
+    if (a != ctx->nA) return fail(ctx, EDDY_ERR_ARG, "labelling %d has %d class-0 samples, expected %d", r, a, ctx->nA);
+  }
+  ctx->ms_total = ctx->ms_pairs = ctx->ms_units = 0;
+  ctx->launches = 0;
+  SetRun sr;
+  int rc = prepare_set(ctx, set_id, sr);
+  if (rc) return rc;
+  std::vector<uint64_t> mh((size_t)R * W);
+  for (int r = 0; r < R; r++) labels_to_mask(labels + (size_t)r * n, n, W, mh.data() + (size_t)r * W);
+  return run_units(ctx, sr, R, mh.data(), nullptr, js, unique, nullptr, 1);
+}
+
+int eddy_debug_edges(eddy_ctx *ctx, int set_id, const uint8_t *labels, uint8_t *edges) {
+  if (!ctx || !labels || !edges || set_id < 0 || set_id >= (int)ctx->sets.size()) return EDDY_ERR_ARG;
+  const int n = ctx->samples, W = ctx->W;
+  SetRun sr;
+  int rc = prepare_set(ctx, set_id, sr);
+  if (rc) return rc;
+  const SetDev &sd = sr.sd;
+  const int c = sd.c, S = sd.S;
+  std::vector<uint64_t> m(W);
+  labels_to_mask(labels, n, W, m.data());
+  CK(ctx->d_masks.ensure(8 * W));
+  CK(ctx->d_dmask.ensure(4 * (size_t)(c > 0 ? c : 1)));
+  CK(cudaMemcpyAsync(ctx->d_masks.p, m.data(), 8 * W, cudaMemcpyHostToDevice, ctx->stream));
+  CK(launch_pairs(sd, ctx->d_masks.as<uint64_t>(), ctx->d_dmask.as<uint32_t>(), 1, nullptr, ctx->stream));
+  std::vector<uint32_t> dm(c);
+  CK(cudaMemcpyAsync(dm.data(), ctx->d_dmask.p, 4 * (size_t)c, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  // expand the 10-bit masks to the S networks (kernel1.cu:85-88, 412-416)
+  std::vector<int> la, lb;
+  for (int s = 0; s < n; s++) (labels[s] == 0 ? la : lb).push_back(s);
+  const int g = sd.g;
+  auto st = [&](int gene, int smp) {
+    int8_t v = ctx->data[(size_t)ctx->sets[set_id].genes[gene] * n + smp];
+    return v == -1 ? 0 : v == 0 ? 1 : v == 1 ? 2 : 3;
+  };
+  for (int s = 0; s < S; s++) {
+    int k, sigma;
+    if (s == 0) { k = 0; sigma = -1; }
+    else if (s == S - 1) { k = 1; sigma = -1; }
+    else if (s <= sd.nA) { k = 0; sigma = la[s - 1]; }
+    else { k = 1; sigma = lb[s - sd.nA - 1]; }
+    int p = 0;
+    for (int r = 1; r < g; r++)
+      for (int col = 0; col < r; col++, p++) {
+        uint32_t mm = (dm[p] >> (16 * k)) & 0x3FFu;
+        int bit = mm & 1u;
+        if (sigma >= 0) {
+          int a = st(r, sigma), b = st(col, sigma);
+          if (a <= 2 && b <= 2) bit = (mm >> (1 + 3 * a + b)) & 1u;
+        }
+        edges[(size_t)s * c + p] = (uint8_t)bit;
+      }
+  }
+  return EDDY_OK;
+}
+
+int eddy_debug_unit(eddy_ctx *ctx, int set_id, const uint8_t *labels, int mpk, int *U, double *js,
+                    int32_t *ids, int32_t *counts, int32_t *parents, double *dist, double *lval) {
+  if (!ctx || !labels || set_id < 0 || set_id >= (int)ctx->sets.size() || mpk < 1) return EDDY_ERR_ARG;
+  const int n = ctx->samples, W = ctx->W;
+  SetRun sr;
+  int rc = prepare_set(ctx, set_id, sr);
+  if (rc) return rc;
+  std::vector<uint64_t> m(W);
+  labels_to_mask(labels, n, W, m.data());
+  KeepOut K;
+  double j = 0;
+  int32_t u = 0;
+  rc = run_units(ctx, sr, 1, m.data(), nullptr, &j, &u, &K, mpk);
+  if (rc) return rc;
+  const int g = sr.sd.g, S = sr.sd.S;
+  if (U) *U = K.U;
+  if (js) *js = j;
+  for (int i = 0; i < K.U; i++) {
+    if (ids) ids[i] = K.ids[i];
+    for (int t = 0; t < g; t++) {
+      if (counts) counts[(size_t)i * g + t] = K.cnt[(size_t)i * g + t];
+      if (parents)
+        for (int q = 0; q < mpk; q++) parents[((size_t)i * g + t) * mpk + q] = K.par[((size_t)i * g + t) * mpk + q];
+    }
+  }
+  if (dist) memcpy(dist, K.dist.data(), 16 * (size_t)S);
+  if (lval) memcpy(lval, K.lval.data(), 16 * (size_t)S);
+  return EDDY_OK;
+}
+
+int eddy_last_timing(const eddy_ctx *ctx, double *ms_kernels, double *ms_pairs, double *ms_units,
+                     long long *launches) {
+  if (!ctx) return EDDY_ERR_ARG;
+  if (ms_kernels) *ms_kernels = ctx->ms_total;
+  if (ms_pairs) *ms_pairs = ctx->ms_pairs;
+  if (ms_units) *ms_units = ctx->ms_units;
+  if (launches) *launches = ctx->launches;
+  return EDDY_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,356 @@
+// eddy_device.cuh -- device helpers of the EDDY hot path (sm_103a).
+//
+// Decision arithmetic (kernel1.cu:121-203, 419-431), the rigorous
+// leave-one-out filter, capped-parent-list generators (kernel3.cu:41-165),
+// network hashing, BDeu in fixed point (kernel5.cu:4-236).
+#pragma once
+#include <stdint.h>
+
+#include "eddy_internal.h"
+
+namespace eddy {
+
+__device__ __forceinline__ int st_of(int8_t v) { return v == -1 ? 0 : v == 0 ? 1 : v == 1 ? 2 : 3; }
+
+__device__ __forceinline__ uint64_t mix64(uint64_t z) {
+  // splitmix64 finaliser (Steele, Lea, Flood, OOPSLA'14)
+  z ^= z >> 30;
+  z *= 0xBF58476D1CE4E5B9ull;
+  z ^= z >> 27;
+  z *= 0x94D049BB133111EBull;
+  z ^= z >> 31;
+  return z;
+}
+__device__ __forceinline__ uint64_t node_hash_init(uint64_t salt, int t) {
+  return mix64(salt ^ ((uint64_t)(t + 1) * 0x9E3779B97F4A7C15ull));
+}
+__device__ __forceinline__ uint64_t node_hash_step(uint64_t h, int j) {
+  return mix64(h ^ ((uint64_t)(j + 1) * 0xC2B2AE3D27D4EB4Full));
+}
+
+__device__ __forceinline__ void pair_rc(int p, int &row, int &col) {
+  int r = (int)((1.f + sqrtf(1.f + 8.f * (float)p)) * 0.5f);
+  while ((long long)r * (r - 1) / 2 > p) r--;
+  while ((long long)(r + 1) * r / 2 <= p) r++;
+  row = r;
+  col = p - r * (r - 1) / 2;
+}
+
+// ------------------------------------------------------------ decisions
+// Exact FP64 evaluation of one table exactly as kernel1.cu:121-203 and
+// 419-431 compute it, without FMA contraction (explicit _rn intrinsics).
+__device__ __noinline__ int exact_decision(const int *t9, int prior,
+                                           const SetDev &sd) {
+  int ex[7] = {0, 0, 0, 0, 0, 0, 0};
+  for (int c = 0; c < 3; c++) {
+    for (int c1 = 0; c1 < 3; c1++) ex[c1] += t9[c * 3 + c1];
+    for (int b = 0; b < 3; b++) ex[3 + b] += t9[b * 3 + c];
+  }
+  ex[6] = ex[0] + ex[1] + ex[2];
+  const double divisor = (double)ex[6];
+  double e[9];
+  for (int c = 0; c < 3; c++)
+    for (int c1 = 0; c1 < 3; c1++)
+      e[c * 3 + c1] = __ddiv_rn(__dmul_rn((double)ex[c1], (double)ex[c + 3]), divisor);
+  double yates = 0.0;
+  bool flag = false;
+  for (int c = 0; c < 3 && !flag; c++)
+    for (int c1 = 0; c1 < 3; c1++)
+      if ((e[c * 3 + c1] < 5) && (ex[c1] && ex[c + 3])) {
+        yates = 0.5;
+        flag = true;
+        break;
+      }
+  double chi = 0.0;
+  int dofn = 0, dofm = 0;
+  for (int ii = 0; ii < 3; ii++) {
+    if (ex[ii] == 0) dofm++;
+    if (ex[ii + 3] == 0) dofn++;
+    for (int jj = 0; jj < 3; jj++)
+      if ((ex[jj] * ex[ii + 3]) != 0) {
+        double d = __dsub_rn(fabs(__dsub_rn((double)t9[ii * 3 + jj], e[ii * 3 + jj])), yates);
+        chi = __dadd_rn(chi, __ddiv_rn(__dmul_rn(d, d), e[ii * 3 + jj]));
+      }
+  }
+  const int dof = ((3 - dofm) - 1) * ((3 - dofn) - 1);
+  // AS 147 (kernel1.cu:10-74)
+  const double x = chi / 2.0, p = ((double)dof) / 2.0;
+  double G = 0.0;
+  if (x > 0.0 && p > 0.0) {
+    double arg = __dsub_rn(__dsub_rn(__dmul_rn(p, log(x)), lgamma(p + 1.0)), x);
+    if (!(arg < log(1.0e-37))) {
+      double f = exp(arg);
+      if (f != 0.0) {
+        double cc = 1.0, value = 1.0, a = p;
+        for (int it = 0; it < 100000; it++) {
+          a = __dadd_rn(a, 1.0);
+          cc = __ddiv_rn(__dmul_rn(cc, x), a);
+          value = __dadd_rn(value, cc);
+          if (cc <= __dmul_rn(1.0e-09, value)) break;
+        }
+        G = __dmul_rn(value, f);
+      }
+    }
+  }
+  double ev = 1.0 - G;
+  if (sd.bonf) {
+    double m = __dmul_rn(ev, (double)(((sd.g - 1) * sd.g) / 2));
+    ev = (1.0 < m) ? 1.0 : m;
+  }
+  return (ev < sd.alpha_edge || (prior == 1 && ev < sd.alpha_edge_prior)) ? 1 : 0;
+}
+
+struct TabInfo {
+  int R[3], C[3], N;
+  int dof;      // (2 - #zero cols)(2 - #zero rows)
+  int yates;    // 1 if the Yates correction applies
+  float chi;    // FP32 chi-square
+};
+
+__device__ __forceinline__ int dof_slot(int dof) { return dof == 1 ? 0 : dof == 2 ? 1 : dof == 4 ? 2 : -1; }
+
+// FP32 chi-square of a 3x3 table: (1/N) sum (|N o - R C| - yN)^2 / (R C),
+// numerators exact in integers.  Returns the marginals too.
+__device__ __forceinline__ void table_info(const int *t, TabInfo &ti) {
+  ti.R[0] = t[0] + t[1] + t[2];
+  ti.R[1] = t[3] + t[4] + t[5];
+  ti.R[2] = t[6] + t[7] + t[8];
+  ti.C[0] = t[0] + t[3] + t[6];
+  ti.C[1] = t[1] + t[4] + t[7];
+  ti.C[2] = t[2] + t[5] + t[8];
+  ti.N = ti.R[0] + ti.R[1] + ti.R[2];
+  int zr = (ti.R[0] == 0) + (ti.R[1] == 0) + (ti.R[2] == 0);
+  int zc = (ti.C[0] == 0) + (ti.C[1] == 0) + (ti.C[2] == 0);
+  ti.dof = (2 - zc) * (2 - zr);
+  int rm = 0x7fffffff, cm = 0x7fffffff;
+#pragma unroll
+  for (int a = 0; a < 3; a++) {
+    if (ti.R[a] > 0 && ti.R[a] < rm) rm = ti.R[a];
+    if (ti.C[a] > 0 && ti.C[a] < cm) cm = ti.C[a];
+  }
+  ti.yates = (ti.N > 0 && (long long)rm * cm < 5ll * ti.N) ? 1 : 0;
+  float chi = 0.f;
+  const int N = ti.N;
+#pragma unroll
+  for (int a = 0; a < 3; a++) {
+#pragma unroll
+    for (int b = 0; b < 3; b++) {
+      long long rc = (long long)ti.R[a] * ti.C[b];
+      if (rc != 0) {
+        long long d = (long long)N * t[a * 3 + b] - rc;
+        if (d < 0) d = -d;
+        long long num2 = ti.yates ? (2 * d - N) : (2 * d);  // 2(|d| - yN)
+        float nf = (float)num2;
+        chi += __fdividef(nf * nf, 4.f * (float)rc);
+      }
+    }
+  }
+  ti.chi = (N > 0) ? chi / (float)N : 0.f;
+}
+
+// 0/1 when certain from the FP32 value, 2 when the exact path must decide.
+__device__ __forceinline__ int fast_decision(const TabInfo &ti, int prior, const SetDev &sd) {
+  if (sd.exact_all || ti.N == 0) return 2;
+  int ds = dof_slot(ti.dof);
+  if (ds < 0) return 0;  // dof 0: p = 1, never below an alpha <= 1
+  const Thr &T = sd.thr[prior][ds];
+  const float x = ti.chi;
+  if (x < T.fA) return 0;
+  if (x > T.fB && x < T.fKlo) return 1;
+  if (x > T.fKhi) return 0;
+  return 2;
+}
+
+__device__ __forceinline__ int decide(const int *t, int prior, const SetDev &sd, TabInfo &ti,
+                                      unsigned &nexact) {
+  table_info(t, ti);
+  int d = fast_decision(ti, prior, sd);
+  if (d == 2) {
+    nexact++;
+    d = exact_decision(t, prior, sd);
+  }
+  return d;
+}
+
+// Rigorous leave-one-out filter.  True when every table t - e_ab (one
+// sample of any cell removed) is certain to get the same decision as t.
+// Bound: with u_rc = (|o-e|-y)/sqrt(e), chi = |u|^2 and Minkowski,
+// |sqrt(chi') - sqrt(chi)| <= A + B sqrt(chi), A^2 <= 15/e'min + 5/(N-1),
+// B = max_rc |sqrt(e/e') - 1|; requires unchanged support (marginals >= 2),
+// unchanged Yates flag and N >= 32.
+__device__ __forceinline__ bool loo_safe(const TabInfo &ti, int prior, const SetDev &sd) {
+  if (sd.exact_all || ti.N < 32) return false;
+  int ds = dof_slot(ti.dof);
+  if (ds < 0) {
+    // dof 0 stays 0 only when the support cannot grow: it never grows under
+    // removal; it can shrink only if a nonzero marginal is 1.
+  }
+  int rm = 0x7fffffff, cm = 0x7fffffff;
+#pragma unroll
+  for (int a = 0; a < 3; a++) {
+    if (ti.R[a] > 0 && ti.R[a] < rm) rm = ti.R[a];
+    if (ti.C[a] > 0 && ti.C[a] < cm) cm = ti.C[a];
+  }
+  if (rm < 2 || cm < 2) return false;
+  if (ds < 0) return true;  // support unchanged: dof stays 0, p = 1
+  const long long N = ti.N;
+  if (ti.yates) {
+    if (!((long long)rm * cm < 5ll * (N - 1))) return false;
+  } else {
+    if (!((long long)(rm - 1) * (cm - 1) >= 5ll * (N - 1))) return false;
+  }
+  const float emin = (float)((double)(rm - 1) * (double)(cm - 1) / (double)(N - 1));
+  const float A = sqrtf(15.f / emin + 5.f / (float)(N - 1));
+  const float ratio = ((float)rm / (float)(rm - 1)) * ((float)cm / (float)(cm - 1));
+  const float B = fmaxf(sqrtf(ratio) - 1.f, 1.f / (float)(N - 1)) * 1.001f;
+  const float rel = 2e-5f;
+  const float sup = sqrtf(ti.chi * (1.f + rel));
+  const float slo = sqrtf(fmaxf(ti.chi * (1.f - rel), 0.f));
+  const float D = (A + B * sup) * 1.01f + 1e-3f;
+  const float whi = (sup + D) * (sup + D) * 1.0001f;
+  const float wl = fmaxf(slo - D, 0.f);
+  const float wlo = wl * wl * 0.9999f;
+  const Thr &T = sd.thr[prior][ds];
+  if (whi < T.chiA) return true;
+  if (wlo > T.chiB && whi < T.kLo) return true;
+  if (wlo > T.kHi) return true;
+  return false;
+}
+
+// 10-bit decision mask of one (pair, class) table: bit 0 = full table,
+// bit 1+3a+b = table with one sample of cell (a,b) removed.
+__device__ __forceinline__ uint32_t pair_mask(int *t, int prior, const SetDev &sd,
+                                              unsigned &nexact, unsigned &nfilt) {
+  TabInfo ti;
+  const int bit0 = decide(t, prior, sd, ti, nexact);
+  if (loo_safe(ti, prior, sd)) {
+    nfilt++;
+    return bit0 ? 0x3FFu : 0u;
+  }
+  uint32_t m = (uint32_t)bit0;
+#pragma unroll 1
+  for (int cell = 0; cell < 9; cell++) {
+    int bit = bit0;
+    if (t[cell] > 0) {
+      t[cell]--;
+      TabInfo tj;
+      bit = decide(t, prior, sd, tj, nexact);
+      t[cell]++;
+    }
+    m |= (uint32_t)bit << (1 + cell);
+  }
+  return m;
+}
+
+// --------------------------------------------------- capped parent lists
+// Generates the parent list of node t (ascending gene index) of the network
+// "full network of class k with the pair tables of sample sigma removed":
+// row bits of the full network XOR the flips that sigma's cells trigger.
+struct ListGen {
+  const uint32_t *row;   // GW words, bit j = edge (t, j), j < t
+  const uint32_t *phi;   // flip entries (p << 9 | flipbits), sorted by p
+  const uint16_t *pcol;  // column of each flip entry
+  const int8_t *stsig;   // states (0..3) of all genes at sample sigma, or null
+  int fi, fe, w, GW, strow;
+  uint32_t word;
+
+  __device__ __forceinline__ uint32_t flipword(int ww) {
+    uint32_t m = 0;
+    if (stsig == nullptr || strow > 2) {
+      return 0;
+    }
+    const int hi = 32 * (ww + 1);
+    while (fi < fe) {
+      int col = pcol[fi];
+      if (col >= hi) break;
+      int sc = stsig[col];
+      if (sc <= 2) {
+        uint32_t bits = phi[fi] & 0x1FFu;
+        if ((bits >> (strow * 3 + sc)) & 1u) m |= 1u << (col - 32 * ww);
+      }
+      fi++;
+    }
+    return m;
+  }
+  __device__ __forceinline__ void init(const uint32_t *row_, int GW_, const uint32_t *phi_,
+                                       const uint16_t *pcol_, int fi_, int fe_,
+                                       const int8_t *stsig_, int strow_) {
+    row = row_;
+    GW = GW_;
+    phi = phi_;
+    pcol = pcol_;
+    fi = fi_;
+    fe = fe_;
+    stsig = stsig_;
+    strow = strow_;
+    w = 0;
+    word = (GW > 0) ? (row[0] ^ flipword(0)) : 0u;
+  }
+  __device__ __forceinline__ int next() {
+    while (true) {
+      if (word) {
+        int j = __ffs(word) - 1;
+        word &= word - 1;
+        return 32 * w + j;
+      }
+      if (++w >= GW) return -1;
+      word = row[w] ^ flipword(w);
+    }
+  }
+};
+
+// ------------------------------------------------------------------ BDeu
+__device__ __constant__ int8_t c_dmap[82];
+
+// BDeu score of node t with parent set ps[0..np) over the samples of one
+// class (mask m), fixed point.  kernel5.cu:30-218: q = product of the
+// parents' observed-state counts, r = node's; score = sum over parent
+// configurations j of [-LG(q)[N_ij] + sum_k LG(q r)[N_ijk]] with
+// LG(d)[m] = lgamma(m + 4/d) - lgamma(4/d).
+__device__ int64_t bdeu_score(const SetDev &sd, int t, int np, const int *ps,
+                              const uint64_t *m, const uint16_t *cnt3 /*[g][3] of this class*/) {
+  int nstate[4], st[4][3];
+  int idx[4] = {t, np > 0 ? ps[0] : 0, np > 1 ? ps[1] : 0, np > 2 ? ps[2] : 0};
+  for (int k = 0; k <= np; k++) {
+    int c = 0;
+    for (int a = 0; a < 3; a++)
+      if (cnt3[idx[k] * 3 + a] > 0) st[k][c++] = a;
+    nstate[k] = c;
+  }
+  const int r = nstate[0];
+  int q = 1;
+  for (int k = 1; k <= np; k++) q *= nstate[k];
+  if (q == 0) return 0;
+  const int64_t *LGq = sd.lg + (size_t)c_dmap[q] * sd.lg_stride;
+  const int64_t *LGqr = (r > 0) ? sd.lg + (size_t)c_dmap[q * r] * sd.lg_stride : nullptr;
+  const int W = sd.W;
+  const uint64_t *P = sd.planes;
+  int64_t score = 0;
+  for (int j = 0; j < q; j++) {
+    int rem = j;
+    const uint64_t *pp[3] = {nullptr, nullptr, nullptr};
+    for (int k = 1; k <= np; k++) {
+      int s = st[k][rem % nstate[k]];
+      rem /= nstate[k];
+      pp[k - 1] = P + ((size_t)idx[k] * 3 + s) * W;
+    }
+    int nij = 0;
+    for (int kk = 0; kk < r; kk++) {
+      const uint64_t *pt = P + ((size_t)t * 3 + st[0][kk]) * W;
+      int cnt = 0;
+      for (int w = 0; w < W; w++) {
+        uint64_t x = pt[w] & m[w];
+        if (np > 0) x &= pp[0][w];
+        if (np > 1) x &= pp[1][w];
+        if (np > 2) x &= pp[2][w];
+        cnt += __popcll(x);
+      }
+      nij += cnt;
+      score += LGqr[cnt];
+    }
+    score -= LGq[nij];
+  }
+  return score;
+}
+
+}  // namespace eddy

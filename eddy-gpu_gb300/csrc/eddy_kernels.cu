@@ -1,0 +1,1015 @@
+// eddy_kernels.cu -- sm_103a kernels of the EDDY hot path.
+//
+//   k_planes / k_ctot   set preparation: per-gene state bit-planes over the
+//                       samples and the permutation-invariant full-sample
+//                       3x3 table of every pair.
+//   k_counter_masks     counter-based labelling (Philox-4x32-10) -> class-1
+//                       sample masks, one block per unit.
+//   k_pairs             contingency counts of class 1 for every (unit, pair)
+//                       (class 2 = full table - class 1), and the 10-bit
+//                       leave-one-out decision mask per class: the reference's
+//                       run2/run2Scalable (kernel1.cu:389-477) over all S
+//                       networks collapsed to <= 10 distinct tables per class.
+//   k_units             one block per unit: full networks, flip lists,
+//                       per-network capped parent lists as deltas
+//                       (kernel2.cu:114-142, kernel3.cu:134-165), network
+//                       hashing and first-occurrence dedup with exact
+//                       verification (kernel4.cu:72-84, main.cu:1060-1121),
+//                       BDeu over the unique networks in fixed point
+//                       (kernel5.cu:237-257), normalisation and JS
+//                       (main.cu:1293-1428).
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <climits>
+
+#include "eddy_device.cuh"
+#include "eddy_kernels.h"
+
+namespace eddy {
+
+// ----------------------------------------------------------- set prep
+__global__ void k_planes(const int8_t *vals, int g, int n, int W, uint64_t *planes,
+                         uint64_t *valid) {
+  int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= g * W) return;
+  int i = idx / W, w = idx % W;
+  uint64_t b0 = 0, b1 = 0, b2 = 0, v = 0;
+  for (int k = 0; k < 64; k++) {
+    int s = w * 64 + k;
+    if (s >= n) break;
+    v |= 1ull << k;
+    int8_t x = vals[(size_t)i * n + s];
+    if (x == -1) b0 |= 1ull << k;
+    else if (x == 0) b1 |= 1ull << k;
+    else if (x == 1) b2 |= 1ull << k;
+  }
+  planes[((size_t)i * 3 + 0) * W + w] = b0;
+  planes[((size_t)i * 3 + 1) * W + w] = b1;
+  planes[((size_t)i * 3 + 2) * W + w] = b2;
+  if (i == 0) valid[w] = v;
+}
+
+__global__ void k_ctot(const uint64_t *planes, int g, int W, int c, uint16_t *ctot) {
+  int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= c) return;
+  int row, col;
+  pair_rc(p, row, col);
+  const uint64_t *Pr = planes + (size_t)row * 3 * W, *Pc = planes + (size_t)col * 3 * W;
+  int cnt[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+  for (int w = 0; w < W; w++) {
+    uint64_t r0 = Pr[w], r1 = Pr[W + w], r2 = Pr[2 * W + w];
+    uint64_t c0 = Pc[w], c1 = Pc[W + w], c2 = Pc[2 * W + w];
+    cnt[0] += __popcll(r0 & c0); cnt[1] += __popcll(r0 & c1); cnt[2] += __popcll(r0 & c2);
+    cnt[3] += __popcll(r1 & c0); cnt[4] += __popcll(r1 & c1); cnt[5] += __popcll(r1 & c2);
+    cnt[6] += __popcll(r2 & c0); cnt[7] += __popcll(r2 & c1); cnt[8] += __popcll(r2 & c2);
+  }
+  for (int k = 0; k < 9; k++) ctot[(size_t)p * 9 + k] = (uint16_t)cnt[k];
+}
+
+// ---------------------------------------------------- counter labelling
+__device__ __forceinline__ void philox10(uint32_t c[4], uint32_t k0, uint32_t k1) {
+  for (int r = 0; r < 10; r++) {
+    uint32_t hi0 = __umulhi(0xD2511F53u, c[0]), lo0 = 0xD2511F53u * c[0];
+    uint32_t hi1 = __umulhi(0xCD9E8D57u, c[2]), lo1 = 0xCD9E8D57u * c[2];
+    uint32_t n0 = hi1 ^ c[1] ^ k0, n2 = hi0 ^ c[3] ^ k1;
+    c[0] = n0; c[1] = lo1; c[2] = n2; c[3] = lo0;
+    k0 += 0x9E3779B9u;
+    k1 += 0xBB67AE85u;
+  }
+}
+
+// One block per unit.  key(s) = Philox(ctr = (s, perm, set, 0), key = seed)
+// word 0; the nA samples with the smallest (key, s) are class 1.
+// Bitonic sort of the padded (key << 32 | s) array in shared memory.
+__global__ void k_counter_masks(int n, int nA, int W, uint64_t seed, const int32_t *unit_set,
+                                const int32_t *unit_perm, const uint64_t *mask0,
+                                uint64_t *masks) {
+  extern __shared__ unsigned long long kv[];
+  const int u = blockIdx.x;
+  const int perm = unit_perm[u];
+  uint64_t *out = masks + (size_t)u * W;
+  if (perm == 0) {
+    for (int w = threadIdx.x; w < W; w += blockDim.x) out[w] = mask0[w];
+    return;
+  }
+  int P = 1;
+  while (P < n) P <<= 1;
+  const uint32_t k0 = (uint32_t)seed, k1 = (uint32_t)(seed >> 32);
+  for (int s = threadIdx.x; s < P; s += blockDim.x) {
+    if (s < n) {
+      uint32_t c[4] = {(uint32_t)s, (uint32_t)perm, (uint32_t)unit_set[u], 0u};
+      philox10(c, k0, k1);
+      kv[s] = ((unsigned long long)c[0] << 32) | (unsigned)s;
+    } else {
+      kv[s] = ~0ull;
+    }
+  }
+  __syncthreads();
+  for (int k = 2; k <= P; k <<= 1) {
+    for (int j = k >> 1; j > 0; j >>= 1) {
+      for (int i = threadIdx.x; i < P; i += blockDim.x) {
+        int ixj = i ^ j;
+        if (ixj > i) {
+          unsigned long long a = kv[i], b = kv[ixj];
+          bool up = (i & k) == 0;
+          if ((a > b) == up) {
+            kv[i] = b;
+            kv[ixj] = a;
+          }
+        }
+      }
+      __syncthreads();
+    }
+  }
+  for (int w = threadIdx.x; w < W; w += blockDim.x) out[w] = 0;
+  __syncthreads();
+  for (int i = threadIdx.x; i < nA; i += blockDim.x) {
+    int s = (int)(kv[i] & 0xffffffffu);
+    atomicOr((unsigned long long *)&out[s >> 6], 1ull << (s & 63));
+  }
+}
+
+// ------------------------------------------------------------ k_pairs
+__global__ void __launch_bounds__(128) k_pairs(SetDev sd, const uint64_t *masks, uint32_t *dmask,
+                                               unsigned long long *stats) {
+  extern __shared__ uint64_t smask[];
+  const int u = blockIdx.y;
+  const int W = sd.W;
+  for (int w = threadIdx.x; w < W; w += blockDim.x) smask[w] = masks[(size_t)u * W + w];
+  __syncthreads();
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  unsigned nexact = 0, nfilt = 0, ntab = 0;
+  if (p < sd.c) {
+    int row, col;
+    pair_rc(p, row, col);
+    const uint64_t *Pr = sd.planes + (size_t)row * 3 * W;
+    const uint64_t *Pc = sd.planes + (size_t)col * 3 * W;
+    int tA[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    for (int w = 0; w < W; w++) {
+      const uint64_t m = smask[w];
+      const uint64_t r0 = Pr[w] & m, r1 = Pr[W + w] & m, r2 = Pr[2 * W + w] & m;
+      const uint64_t c0 = Pc[w], c1 = Pc[W + w], c2 = Pc[2 * W + w];
+      tA[0] += __popcll(r0 & c0); tA[1] += __popcll(r0 & c1); tA[2] += __popcll(r0 & c2);
+      tA[3] += __popcll(r1 & c0); tA[4] += __popcll(r1 & c1); tA[5] += __popcll(r1 & c2);
+      tA[6] += __popcll(r2 & c0); tA[7] += __popcll(r2 & c1); tA[8] += __popcll(r2 & c2);
+    }
+    int tB[9];
+    const uint16_t *ct = sd.ctot + (size_t)p * 9;
+#pragma unroll
+    for (int k = 0; k < 9; k++) tB[k] = (int)ct[k] - tA[k];
+    const int prior = sd.prior[p] ? 1 : 0;
+    uint32_t mA = pair_mask(tA, prior, sd, nexact, nfilt);
+    uint32_t mB = pair_mask(tB, prior, sd, nexact, nfilt);
+    dmask[(size_t)u * sd.c + p] = mA | (mB << 16);
+    ntab = 2;
+  }
+  if (stats) {
+    // warp-aggregated counters
+    for (int o = 16; o > 0; o >>= 1) {
+      nexact += __shfl_down_sync(0xffffffffu, nexact, o);
+      nfilt += __shfl_down_sync(0xffffffffu, nfilt, o);
+      ntab += __shfl_down_sync(0xffffffffu, ntab, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+      if (nexact) atomicAdd(&stats[0], (unsigned long long)nexact);
+      if (ntab) atomicAdd(&stats[1], (unsigned long long)ntab);
+      if (nfilt) atomicAdd(&stats[2], (unsigned long long)nfilt);
+    }
+  }
+}
+
+// ------------------------------------------------------------ k_units
+struct UnitLayout {
+  size_t phi[2], pcol[2], rec, htk, htv, dist, uid, urep, total;
+  int HT, rec_words;  // rec_words: 64-bit words per network record
+};
+
+__host__ __device__ inline UnitLayout unit_layout(int c, int S, int kmax) {
+  UnitLayout L;
+  size_t o = 0;
+  auto al = [](size_t x) { return (x + 255) & ~(size_t)255; };
+  for (int k = 0; k < 2; k++) {
+    L.phi[k] = o;
+    o = al(o + sizeof(uint32_t) * (size_t)(c > 0 ? c : 1));
+    L.pcol[k] = o;
+    o = al(o + sizeof(uint16_t) * (size_t)(c > 0 ? c : 1));
+  }
+  L.rec_words = 2 + kmax;  // [H, nchg | flags, chg...]
+  L.rec = o;
+  o = al(o + sizeof(uint64_t) * (size_t)L.rec_words * S);
+  int HT = 1;
+  while (HT < 2 * S) HT <<= 1;
+  L.HT = HT;
+  L.htk = o;
+  o = al(o + sizeof(uint64_t) * (size_t)HT);
+  L.htv = o;
+  o = al(o + sizeof(int32_t) * (size_t)HT);
+  L.dist = o;
+  o = al(o + sizeof(int64_t) * 2 * (size_t)S);
+  L.uid = o;
+  o = al(o + sizeof(int32_t) * (size_t)S);
+  L.urep = o;
+  o = al(o + sizeof(int32_t) * (size_t)S);
+  L.total = o;
+  return L;
+}
+
+size_t unit_scratch_bytes(int c, int S, int kmax) { return unit_layout(c, S, kmax).total; }
+
+// Block-wide exclusive scan (blockDim multiple of 32, <= 1024).
+__device__ __forceinline__ int block_scan(int v, int &total, int *sbuf) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  int x = v;
+  for (int o = 1; o < 32; o <<= 1) {
+    int y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) sbuf[warp] = x;
+  __syncthreads();
+  if (warp == 0) {
+    int t = (lane < nw) ? sbuf[lane] : 0;
+    for (int o = 1; o < 32; o <<= 1) {
+      int y = __shfl_up_sync(0xffffffffu, t, o);
+      if (lane >= o) t += y;
+    }
+    sbuf[lane] = t;
+  }
+  __syncthreads();
+  int excl = x - v + (warp ? sbuf[warp - 1] : 0);
+  total = sbuf[nw - 1];
+  __syncthreads();
+  return excl;
+}
+
+// k-th (0-based) set bit of mask words (pc = exclusive popcount prefix).
+__device__ __forceinline__ int select_bit(const uint64_t *m, const int *pc, int W, int k) {
+  int lo = 0, hi = W - 1;
+  while (lo < hi) {  // last word with pc[w] <= k
+    int mid = (lo + hi + 1) >> 1;
+    if (pc[mid] <= k) lo = mid; else hi = mid - 1;
+  }
+  uint64_t x = m[lo];
+  int r = k - pc[lo];
+  for (int i = 0; i < r; i++) x &= x - 1;
+  return lo * 64 + (__ffsll((long long)x) - 1);
+}
+
+struct UnitSmem {
+  // fixed part; variable arrays follow in dynamic shared memory
+  unsigned long long HF[2];
+  long long base[2][2];  // [data class][full network of class]
+  int nphi[2];
+  int ndab;
+  int scan[32];
+  unsigned status;
+  int U;
+  double red_d[32];
+  long long red_l[32];
+};
+
+constexpr int kMemo = 512;
+
+struct UnitPtrs {
+  uint64_t *mA, *mB;      // [W]
+  int *pcA, *pcB;         // [W]
+  uint32_t *rows;         // [2][g][GW]
+  uint16_t *cnt3;         // [2][g][3] state counts per class
+  uint16_t *fcnt;         // [2][g] capped count of full networks
+  uint16_t *fps;          // [2][g][3] first three parents
+  unsigned long long *fh; // [2][g] node hash of full networks
+  int *phs, *phe;         // [2][g] flip-entry range per row
+  uint16_t *dab;          // [g] nodes whose full lists differ between classes
+  int8_t *stsig;          // [nwarps][g] states at sigma
+  unsigned long long *mkey;  // [kMemo]
+  long long *mval;           // [kMemo][2]
+  long long *fsc;            // [2 full][2 data][g] base node scores
+};
+
+__host__ __device__ inline size_t unit_smem_bytes(int g, int W, int GW, int nwarps) {
+  size_t o = sizeof(UnitSmem);
+  auto al = [](size_t x) { return (x + 15) & ~(size_t)15; };
+  o = al(o) + 2 * sizeof(uint64_t) * W;
+  o = al(o) + 2 * sizeof(int) * W;
+  o = al(o) + 2 * sizeof(uint32_t) * (size_t)g * GW;
+  o = al(o) + 2 * 3 * sizeof(uint16_t) * g;
+  o = al(o) + 2 * sizeof(uint16_t) * g;
+  o = al(o) + 2 * 3 * sizeof(uint16_t) * g;
+  o = al(o) + 2 * sizeof(unsigned long long) * g;
+  o = al(o) + 4 * sizeof(int) * g;
+  o = al(o) + sizeof(uint16_t) * g;
+  o = al(o) + (size_t)nwarps * g;
+  o = al(o) + sizeof(unsigned long long) * kMemo;
+  o = al(o) + 2 * sizeof(long long) * kMemo;
+  o = al(o) + 4 * sizeof(long long) * g;
+  return al(o);
+}
+
+size_t unit_smem_size(int g, int W, int nwarps) { return unit_smem_bytes(g, W, (g + 31) / 32, nwarps); }
+
+__device__ inline UnitPtrs carve(char *base, int g, int W, int GW, int nwarps) {
+  UnitPtrs P;
+  size_t o = sizeof(UnitSmem);
+  auto al = [](size_t x) { return (x + 15) & ~(size_t)15; };
+  o = al(o); P.mA = (uint64_t *)(base + o); P.mB = P.mA + W; o += 2 * sizeof(uint64_t) * W;
+  o = al(o); P.pcA = (int *)(base + o); P.pcB = P.pcA + W; o += 2 * sizeof(int) * W;
+  o = al(o); P.rows = (uint32_t *)(base + o); o += 2 * sizeof(uint32_t) * (size_t)g * GW;
+  o = al(o); P.cnt3 = (uint16_t *)(base + o); o += 2 * 3 * sizeof(uint16_t) * g;
+  o = al(o); P.fcnt = (uint16_t *)(base + o); o += 2 * sizeof(uint16_t) * g;
+  o = al(o); P.fps = (uint16_t *)(base + o); o += 2 * 3 * sizeof(uint16_t) * g;
+  o = al(o); P.fh = (unsigned long long *)(base + o); o += 2 * sizeof(unsigned long long) * g;
+  o = al(o); P.phs = (int *)(base + o); P.phe = P.phs + 2 * g; o += 4 * sizeof(int) * g;
+  o = al(o); P.dab = (uint16_t *)(base + o); o += sizeof(uint16_t) * g;
+  o = al(o); P.stsig = (int8_t *)(base + o); o += (size_t)nwarps * g;
+  o = al(o); P.mkey = (unsigned long long *)(base + o); o += sizeof(unsigned long long) * kMemo;
+  o = al(o); P.mval = (long long *)(base + o); o += 2 * sizeof(long long) * kMemo;
+  o = al(o); P.fsc = (long long *)(base + o);
+  return P;
+}
+
+// Network s of a unit: class k (0 = class 1, 1 = class 2) and left-out
+// sample sigma (-1 for the two full networks), kernel1.cu:85-88, 412-416.
+__device__ __forceinline__ void net_of(int s, const SetDev &sd, const UnitPtrs &P, int &k, int &sigma) {
+  if (s == 0) { k = 0; sigma = -1; return; }
+  if (s == sd.S - 1) { k = 1; sigma = -1; return; }
+  if (s <= sd.nA) { k = 0; sigma = select_bit(P.mA, P.pcA, sd.W, s - 1); return; }
+  k = 1;
+  sigma = select_bit(P.mB, P.pcB, sd.W, s - sd.nA - 1);
+}
+
+__device__ __forceinline__ void load_stsig(const SetDev &sd, int sigma, int8_t *dst, int lane) {
+  for (int i = lane; i < sd.g; i += 32)
+    dst[i] = (int8_t)(sigma >= 0 ? st_of(sd.vals[(size_t)i * sd.n + sigma]) : 3);
+  __syncwarp();
+}
+
+__device__ __forceinline__ void gen_for(ListGen &G, const SetDev &sd, const UnitPtrs &P,
+                                        const uint32_t *phi, const uint16_t *pcol, int k, int t,
+                                        const int8_t *st) {
+  const int GW = sd.GW;
+  const int strow = st ? st[t] : 3;
+  G.init(P.rows + ((size_t)k * sd.g + t) * GW, GW, phi, pcol, P.phs[k * sd.g + t],
+         P.phe[k * sd.g + t], st, strow);
+}
+
+// Exact comparison of the capped lists of node t in two networks.
+__device__ bool lists_equal(const SetDev &sd, const UnitPtrs &P, const uint32_t *const *phi,
+                            const uint16_t *const *pcol, int t, int k1, const int8_t *st1, int k2,
+                            const int8_t *st2) {
+  ListGen a, b;
+  gen_for(a, sd, P, phi[k1], pcol[k1], k1, t, st1);
+  gen_for(b, sd, P, phi[k2], pcol[k2], k2, t, st2);
+  for (int i = 0; i < sd.mp; i++) {
+    int x = a.next(), y = b.next();
+    if (x != y) return false;
+    if (x < 0) return true;
+  }
+  return true;
+}
+
+__device__ __forceinline__ unsigned long long memo_key(int t, int np, const int *ps) {
+  unsigned long long k = (unsigned long long)t | ((unsigned long long)np << 14);
+  for (int i = 0; i < 3; i++)
+    k |= (unsigned long long)(i < np ? (ps[i] & 0xFFFF) : 0xFFFF) << (16 + 16 * i);
+  return k;
+}
+
+// Scores of (t, parents) for both data classes, memoised per unit.
+__device__ void scores_of(const SetDev &sd, const UnitPtrs &P, int t, int np, const int *ps,
+                          long long out[2]) {
+  const unsigned long long key = memo_key(t, np, ps);
+  unsigned h = (unsigned)(mix64(key) & (kMemo - 1));
+  for (int probe = 0; probe < 8; probe++) {
+    unsigned slot = (h + probe) & (kMemo - 1);
+    unsigned long long kk = P.mkey[slot];
+    if (kk == key) {
+      __threadfence_block();
+      long long a = P.mval[2 * slot], b = P.mval[2 * slot + 1];
+      if (a != LLONG_MIN && b != LLONG_MIN) {
+        out[0] = a;
+        out[1] = b;
+        return;
+      }
+      break;
+    }
+    if (kk == ~0ull) break;
+  }
+  out[0] = bdeu_score(sd, t, np, ps, P.mA, P.cnt3);
+  out[1] = bdeu_score(sd, t, np, ps, P.mB, P.cnt3 + 3 * sd.g);
+  for (int probe = 0; probe < 8; probe++) {
+    unsigned slot = (h + probe) & (kMemo - 1);
+    unsigned long long prev = atomicCAS(&P.mkey[slot], ~0ull, key);
+    if (prev == ~0ull) {
+      P.mval[2 * slot] = out[0];
+      P.mval[2 * slot + 1] = out[1];
+      return;
+    }
+    if (prev == key) return;
+  }
+}
+
+__global__ void __launch_bounds__(256) k_units(SetDev sd, BatchDev bd) {
+  extern __shared__ __align__(16) char smraw[];
+  UnitSmem &SM = *reinterpret_cast<UnitSmem *>(smraw);
+  const int nw = blockDim.x >> 5, lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int g = sd.g, W = sd.W, GW = sd.GW, S = sd.S, c = sd.c;
+  UnitPtrs P = carve(smraw, g, W, GW, nw);
+  const int u = blockIdx.x;
+  const UnitLayout L = unit_layout(c, S, bd.kmax);
+  uint8_t *scr = bd.scratch + (size_t)u * bd.unit_bytes;
+  uint32_t *phi[2] = {(uint32_t *)(scr + L.phi[0]), (uint32_t *)(scr + L.phi[1])};
+  uint16_t *pcol[2] = {(uint16_t *)(scr + L.pcol[0]), (uint16_t *)(scr + L.pcol[1])};
+  unsigned long long *rec = (unsigned long long *)(scr + L.rec);
+  unsigned long long *htk = (unsigned long long *)(scr + L.htk);
+  int *htv = (int *)(scr + L.htv);
+  long long *dist = (long long *)(scr + L.dist);
+  int *uid = (int *)(scr + L.uid);
+  int *urep = (int *)(scr + L.urep);
+  const uint32_t *dm = bd.dmask + (size_t)u * c;
+  const int tid = threadIdx.x, nt = blockDim.x;
+
+  // ---- P0: masks, state counts, selection prefixes, init
+  if (tid == 0) {
+    SM.HF[0] = SM.HF[1] = 0;
+    SM.nphi[0] = SM.nphi[1] = 0;
+    SM.ndab = 0;
+    SM.status = 0;
+    for (int a = 0; a < 2; a++)
+      for (int b = 0; b < 2; b++) SM.base[a][b] = 0;
+  }
+  for (int w = tid; w < W; w += nt) {
+    uint64_t m = bd.masks[(size_t)u * W + w];
+    P.mA[w] = m;
+    P.mB[w] = sd.valid[w] & ~m;
+  }
+  for (int i = tid; i < 2 * g * GW; i += nt) P.rows[i] = 0;
+  for (int i = tid; i < 4 * g; i += nt) P.phs[i] = 0;  // phs and phe
+  for (int i = tid; i < kMemo; i += nt) {
+    P.mkey[i] = ~0ull;
+    P.mval[2 * i] = LLONG_MIN;
+    P.mval[2 * i + 1] = LLONG_MIN;
+  }
+  for (int i = tid; i < L.HT; i += nt) {
+    htk[i] = ~0ull;
+    htv[i] = 0x7fffffff;
+  }
+  __syncthreads();
+  for (int i = tid; i < g * 3; i += nt) {
+    const uint64_t *pl = sd.planes + (size_t)i * W;
+    int a = 0, b = 0;
+    for (int w = 0; w < W; w++) {
+      a += __popcll(pl[w] & P.mA[w]);
+      b += __popcll(pl[w] & P.mB[w]);
+    }
+    P.cnt3[i] = (uint16_t)a;
+    P.cnt3[3 * g + i] = (uint16_t)b;
+  }
+  if (warp == 0) {
+    for (int cls = 0; cls < 2; cls++) {
+      const uint64_t *m = cls ? P.mB : P.mA;
+      int *pc = cls ? P.pcB : P.pcA;
+      int run = 0;
+      for (int w0 = 0; w0 < W; w0 += 32) {
+        int w = w0 + lane;
+        int v = (w < W) ? __popcll(m[w]) : 0;
+        int x = v;
+        for (int o = 1; o < 32; o <<= 1) {
+          int y = __shfl_up_sync(0xffffffffu, x, o);
+          if (lane >= o) x += y;
+        }
+        if (w < W) pc[w] = run + x - v;
+        run += __shfl_sync(0xffffffffu, x, 31);
+      }
+    }
+  }
+
+  // ---- P1: full-network rows and ordered flip lists
+  for (int p0 = 0; p0 < c; p0 += nt) {
+    const int p = p0 + tid;
+    uint32_t m = (p < c) ? dm[p] : 0u;
+    int row = 0, col = 0;
+    if (p < c) {
+      pair_rc(p, row, col);
+      if (m & 1u) atomicOr(&P.rows[((size_t)0 * g + row) * GW + (col >> 5)], 1u << (col & 31));
+      if (m & (1u << 16)) atomicOr(&P.rows[((size_t)1 * g + row) * GW + (col >> 5)], 1u << (col & 31));
+    }
+    for (int cls = 0; cls < 2; cls++) {
+      uint32_t mm = (m >> (16 * cls)) & 0x3FFu;
+      uint32_t fb = (mm >> 1) ^ ((mm & 1u) ? 0x1FFu : 0u);
+      int flag = (p < c && fb != 0u) ? 1 : 0;
+      int total;
+      int off = block_scan(flag, total, SM.scan);
+      if (flag) {
+        int idx = SM.nphi[cls] + off;
+        phi[cls][idx] = ((uint32_t)p << 9) | fb;
+        pcol[cls][idx] = (uint16_t)col;
+      }
+      __syncthreads();
+      if (tid == 0) SM.nphi[cls] += total;
+      __syncthreads();
+    }
+  }
+  __syncthreads();
+  // flip ranges per row (entries sorted by p, rows contiguous)
+  for (int cls = 0; cls < 2; cls++) {
+    const int nphi = SM.nphi[cls];
+    for (int i = tid; i < nphi; i += nt) {
+      int r, cc;
+      pair_rc((int)(phi[cls][i] >> 9), r, cc);
+      int rp = -1;
+      if (i > 0) {
+        int r2, c2;
+        pair_rc((int)(phi[cls][i - 1] >> 9), r2, c2);
+        rp = r2;
+      }
+      if (rp != r) P.phs[cls * g + r] = i;
+      int rn = -1;
+      if (i + 1 < nphi) {
+        int r2, c2;
+        pair_rc((int)(phi[cls][i + 1] >> 9), r2, c2);
+        rn = r2;
+      }
+      if (rn != r) P.phe[cls * g + r] = i + 1;
+    }
+  }
+  __syncthreads();
+
+  // ---- P2: capped lists of the two full networks
+  for (int i = tid; i < 2 * g; i += nt) {
+    const int k = i / g, t = i % g;
+    ListGen G;
+    gen_for(G, sd, P, phi[k], pcol[k], k, t, nullptr);
+    uint64_t h = node_hash_init(sd.salt, t);
+    int cnt = 0;
+    int ps[3] = {0xFFFF, 0xFFFF, 0xFFFF};
+    while (cnt < sd.mp) {
+      int j = G.next();
+      if (j < 0) break;
+      if (cnt < 3) ps[cnt] = j;
+      h = node_hash_step(h, j);
+      cnt++;
+    }
+    P.fcnt[i] = (uint16_t)cnt;
+    for (int q = 0; q < 3; q++) P.fps[i * 3 + q] = (uint16_t)ps[q];
+    P.fh[i] = h;
+    atomicAdd(&SM.HF[k], (unsigned long long)h);
+  }
+  __syncthreads();
+  for (int t = tid; t < g; t += nt) {
+    if (!lists_equal(sd, P, phi, pcol, t, 0, nullptr, 1, nullptr)) {
+      int idx = atomicAdd(&SM.ndab, 1);
+      P.dab[idx] = (uint16_t)t;
+    }
+  }
+  __syncthreads();
+
+  // ---- P3: every network as a delta of its class's full network
+  int8_t *myst = P.stsig + (size_t)warp * g;
+  for (int s = warp; s < S; s += nw) {
+    int k, sigma;
+    net_of(s, sd, P, k, sigma);
+    unsigned long long *R = rec + (size_t)s * L.rec_words;
+    if (sigma < 0) {
+      if (lane == 0) {
+        R[0] = SM.HF[k];
+        R[1] = 0;
+      }
+      continue;
+    }
+    load_stsig(sd, sigma, myst, lane);
+    unsigned long long dh = 0;
+    int nchg = 0;
+    for (int t0 = 0; t0 < g; t0 += 32) {
+      const int t = t0 + lane;
+      bool changed = false;
+      unsigned long long hn = 0;
+      int ps[3] = {0xFFFF, 0xFFFF, 0xFFFF};
+      int cnt = 0;
+      if (t < g && P.phe[k * g + t] > P.phs[k * g + t] && myst[t] <= 2) {
+        ListGen Gn, Go;
+        gen_for(Gn, sd, P, phi[k], pcol[k], k, t, myst);
+        gen_for(Go, sd, P, phi[k], pcol[k], k, t, nullptr);
+        uint64_t h = node_hash_init(sd.salt, t);
+        bool diff = false;
+        for (int i = 0; i < sd.mp; i++) {
+          int x = Gn.next(), y = Go.next();
+          if (x != y) diff = true;
+          if (x < 0) break;
+          if (cnt < 3) ps[cnt] = x;
+          h = node_hash_step(h, x);
+          cnt++;
+        }
+        if (diff) {
+          changed = true;
+          hn = h;
+        }
+      }
+      unsigned bal = __ballot_sync(0xffffffffu, changed);
+      if (changed) {
+        int pos = nchg + __popc(bal & ((1u << lane) - 1u));
+        dh += hn - P.fh[k * g + t];
+        if (pos < bd.kmax) {
+          unsigned long long e = (unsigned long long)t | ((unsigned long long)(cnt < 3 ? cnt : 3) << 14) |
+                                 ((unsigned long long)(ps[0] & 0xFFFF) << 16) |
+                                 ((unsigned long long)(ps[1] & 0xFFFF) << 32) |
+                                 ((unsigned long long)(ps[2] & 0xFFFF) << 48);
+          R[2 + pos] = e;
+        }
+      }
+      nchg += __popc(bal);
+    }
+    for (int o = 16; o > 0; o >>= 1) dh += __shfl_down_sync(0xffffffffu, dh, o);
+    if (lane == 0) {
+      R[0] = SM.HF[k] + dh;
+      R[1] = (unsigned long long)nchg;
+      if (nchg > bd.kmax) atomicOr(&SM.status, kUnitKmaxOverflow);
+    }
+  }
+  __syncthreads();
+  if (SM.status & kUnitKmaxOverflow) {
+    if (tid == 0) {
+      bd.status[u] = SM.status;
+      bd.js[u] = __longlong_as_double(0x7ff8000000000000ll);
+      bd.U[u] = -1;
+    }
+    return;
+  }
+
+  // ---- P4: first-occurrence dedup by hash, exact verification
+  const int HT = L.HT;
+  for (int s = tid; s < S; s += nt) {
+    unsigned long long key = rec[(size_t)s * L.rec_words];
+    if (key == ~0ull) key ^= 1ull;
+    unsigned slot = (unsigned)(mix64(key) & (HT - 1));
+    while (true) {
+      unsigned long long prev = atomicCAS(&htk[slot], ~0ull, key);
+      if (prev == ~0ull || prev == key) {
+        atomicMin(&htv[slot], s);
+        break;
+      }
+      slot = (slot + 1) & (HT - 1);
+    }
+  }
+  __syncthreads();
+  int running = 0;
+  for (int s0 = 0; s0 < S; s0 += nt) {
+    const int s = s0 + tid;
+    int uq = 0;
+    int rep = -1;
+    if (s < S) {
+      unsigned long long key = rec[(size_t)s * L.rec_words];
+      if (key == ~0ull) key ^= 1ull;
+      unsigned slot = (unsigned)(mix64(key) & (HT - 1));
+      while (htk[slot] != key) slot = (slot + 1) & (HT - 1);
+      rep = htv[slot];
+      uq = (rep == s) ? 1 : 0;
+    }
+    int total;
+    int off = block_scan(uq, total, SM.scan);
+    if (s < S) {
+      if (uq) {
+        uid[s] = running + off;
+        urep[running + off] = s;
+      } else {
+        uid[s] = -1 - rep;  // encodes the representative
+      }
+    }
+    running += total;
+  }
+  if (tid == 0) SM.U = running;
+  __syncthreads();
+  const int U = SM.U;
+  // verify every duplicate against its representative (warp per network)
+  for (int s = warp; s < S; s += nw) {
+    int code = uid[s];
+    if (code >= 0) continue;
+    const int r = -1 - code;
+    int ks, ss, kr, sr;
+    net_of(s, sd, P, ks, ss);
+    net_of(r, sd, P, kr, sr);
+    const unsigned long long *Rs = rec + (size_t)s * L.rec_words;
+    const unsigned long long *Rr = rec + (size_t)r * L.rec_words;
+    const int ns = (int)Rs[1], nr = (int)Rr[1];
+    bool ok = true;
+    // states at both samples, shared by the warp
+    load_stsig(sd, ss, myst, lane);
+    int8_t str_local[1];
+    (void)str_local;
+    if (ks == kr) {
+      if (ns != nr) ok = false;
+      // every changed node of s must be changed in r with an equal list
+      for (int i = lane; ok && i < ns; i += 32) {
+        int t = (int)(Rs[2 + i] & 0x3FFF);
+        bool found = false;
+        for (int j = 0; j < nr; j++)
+          if ((int)(Rr[2 + j] & 0x3FFF) == t) { found = true; break; }
+        if (!found) ok = false;
+      }
+      ok = __all_sync(0xffffffffu, ok);
+    }
+    // list comparisons need sigma(r) states too: compare node by node,
+    // generating r's list with its own states loaded into a second buffer
+    // (the neighbouring warp's buffer is not free, so states of r are read
+    // directly from global memory inside a private generator buffer)
+    if (ok) {
+      // nodes to compare: changed of s, changed of r, and DAB when classes differ
+      const int nd = (ks != kr) ? SM.ndab : 0;
+      const int total = ns + nr + nd;
+      for (int i = lane; i < total; i += 32) {
+        int t;
+        if (i < ns) t = (int)(Rs[2 + i] & 0x3FFF);
+        else if (i < ns + nr) t = (int)(Rr[2 + (i - ns)] & 0x3FFF);
+        else t = P.dab[i - ns - nr];
+        // list of t in s
+        ListGen a, b;
+        gen_for(a, sd, P, phi[ks], pcol[ks], ks, t, ss >= 0 ? myst : nullptr);
+        // list of t in r: states of sigma(r) for row t and the columns read
+        // through a private lookup
+        const int GWl = sd.GW;
+        const int strow_r = (sr >= 0) ? st_of(sd.vals[(size_t)t * sd.n + sr]) : 3;
+        // b: manual generator with global-memory states
+        const uint32_t *rowr = P.rows + ((size_t)kr * g + t) * GWl;
+        int fi = P.phs[kr * g + t], fe = P.phe[kr * g + t];
+        int w = 0;
+        auto flipw = [&](int ww) -> uint32_t {
+          uint32_t mm = 0;
+          if (sr < 0 || strow_r > 2) return 0u;
+          const int hi = 32 * (ww + 1);
+          while (fi < fe) {
+            int col = pcol[kr][fi];
+            if (col >= hi) break;
+            int sc = st_of(sd.vals[(size_t)col * sd.n + sr]);
+            if (sc <= 2 && ((phi[kr][fi] & 0x1FFu) >> (strow_r * 3 + sc)) & 1u) mm |= 1u << (col - 32 * ww);
+            fi++;
+          }
+          return mm;
+        };
+        uint32_t word = GWl > 0 ? (rowr[0] ^ flipw(0)) : 0u;
+        auto nextb = [&]() -> int {
+          while (true) {
+            if (word) {
+              int j = __ffs(word) - 1;
+              word &= word - 1;
+              return 32 * w + j;
+            }
+            if (++w >= GWl) return -1;
+            word = rowr[w] ^ flipw(w);
+          }
+        };
+        (void)b;
+        for (int q = 0; q < sd.mp; q++) {
+          int x = a.next(), y = nextb();
+          if (x != y) { ok = false; break; }
+          if (x < 0) break;
+        }
+      }
+      ok = __all_sync(0xffffffffu, ok);
+    }
+    if (!ok && lane == 0) atomicOr(&SM.status, kUnitHashCollision);
+    __syncwarp();
+  }
+  __syncthreads();
+  if (bd.stats && tid == 0) atomicAdd(&bd.stats[3], (unsigned long long)(S - U));
+
+  // ---- P5: BDeu.  Base node scores of the two full networks.
+  for (int i = tid; i < 2 * g; i += nt) {
+    const int k = i / g, t = i % g;
+    int np = P.fcnt[i] < 3 ? P.fcnt[i] : 3;
+    int ps[3] = {P.fps[i * 3], P.fps[i * 3 + 1], P.fps[i * 3 + 2]};
+    long long sc[2];
+    scores_of(sd, P, t, np, ps, sc);
+    P.fsc[(k * 2 + 0) * g + t] = sc[0];
+    P.fsc[(k * 2 + 1) * g + t] = sc[1];
+  }
+  __syncthreads();
+  for (int i = tid; i < 4; i += nt) {
+    const int k = i / 2, cls = i % 2;
+    long long s = 0;
+    for (int t = 0; t < g; t++) s += P.fsc[(k * 2 + cls) * g + t];
+    SM.base[cls][k] = s;
+  }
+  __syncthreads();
+  // per unique network: base + deltas of its changed nodes
+  for (int uu = tid; uu < U; uu += nt) {
+    const int s = urep[uu];
+    int k, sigma;
+    net_of(s, sd, P, k, sigma);
+    const unsigned long long *R = rec + (size_t)s * L.rec_words;
+    const int nchg = (int)R[1];
+    long long d0 = SM.base[0][k], d1 = SM.base[1][k];
+    for (int i = 0; i < nchg; i++) {
+      unsigned long long e = R[2 + i];
+      const int t = (int)(e & 0x3FFF);
+      const int np = (int)((e >> 14) & 3);
+      int ps[3] = {(int)((e >> 16) & 0xFFFF), (int)((e >> 32) & 0xFFFF), (int)((e >> 48) & 0xFFFF)};
+      int fnp = P.fcnt[k * g + t] < 3 ? P.fcnt[k * g + t] : 3;
+      bool same = (np == fnp);
+      for (int q = 0; same && q < np; q++) same = (ps[q] == (int)P.fps[(k * g + t) * 3 + q]);
+      if (same) continue;
+      long long sc[2];
+      scores_of(sd, P, t, np, ps, sc);
+      d0 += sc[0] - P.fsc[(k * 2 + 0) * g + t];
+      d1 += sc[1] - P.fsc[(k * 2 + 1) * g + t];
+    }
+    dist[uu] = d0;
+    dist[S + uu] = d1;
+  }
+  __syncthreads();
+
+  // ---- P6: normalisation (main.cu:1302-1404) and JS (main.cu:1406-1428)
+  const int keep = bd.keep_slot ? bd.keep_slot[u] : -1;
+  double js = 0.0;
+  // per class: min, max, mean of (d - min)
+  long long mn[2], mx[2];
+  double mean[2], esum[2];
+  for (int cls = 0; cls < 2; cls++) {
+    long long lmn = LLONG_MAX, lmx = LLONG_MIN;
+    for (int uu = tid; uu < U; uu += nt) {
+      long long d = dist[cls * S + uu];
+      lmn = d < lmn ? d : lmn;
+      lmx = d > lmx ? d : lmx;
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      long long a = __shfl_down_sync(0xffffffffu, lmn, o), b = __shfl_down_sync(0xffffffffu, lmx, o);
+      lmn = a < lmn ? a : lmn;
+      lmx = b > lmx ? b : lmx;
+    }
+    if (lane == 0) { SM.red_l[warp] = lmn; SM.red_l[16 + warp] = lmx; }
+    __syncthreads();
+    if (tid == 0) {
+      long long a = SM.red_l[0], b = SM.red_l[16];
+      for (int w = 1; w < nw; w++) {
+        a = SM.red_l[w] < a ? SM.red_l[w] : a;
+        b = SM.red_l[16 + w] > b ? SM.red_l[16 + w] : b;
+      }
+      SM.red_l[0] = a;
+      SM.red_l[16] = b;
+    }
+    __syncthreads();
+    mn[cls] = SM.red_l[0];
+    mx[cls] = SM.red_l[16];
+    __syncthreads();
+    double ls = 0.0;
+    for (int uu = tid; uu < U; uu += nt) ls += (double)(dist[cls * S + uu] - mn[cls]);
+    for (int o = 16; o > 0; o >>= 1) ls += __shfl_down_sync(0xffffffffu, ls, o);
+    if (lane == 0) SM.red_d[warp] = ls;
+    __syncthreads();
+    if (tid == 0) {
+      double a = 0;
+      for (int w = 0; w < nw; w++) a += SM.red_d[w];
+      SM.red_d[0] = a;
+    }
+    __syncthreads();
+    mean[cls] = SM.red_d[0] / (double)U;
+    __syncthreads();
+  }
+  // exp of the adjusted scores and their sums
+  for (int cls = 0; cls < 2; cls++) {
+    const double scale = 10.0 / (double)(mx[cls] - mn[cls]);  // inf when all equal
+    double ls = 0.0;
+    for (int uu = tid; uu < U; uu += nt) {
+      double a = ((double)(dist[cls * S + uu] - mn[cls]) - mean[cls]) * scale;
+      float ah = (float)a;
+      float al = (float)(a - (double)ah);
+      double e = (double)expf(ah) * (1.0 + (double)al);
+      ls += e;
+    }
+    for (int o = 16; o > 0; o >>= 1) ls += __shfl_down_sync(0xffffffffu, ls, o);
+    if (lane == 0) SM.red_d[warp] = ls;
+    __syncthreads();
+    if (tid == 0) {
+      double a = 0;
+      for (int w = 0; w < nw; w++) a += SM.red_d[w];
+      SM.red_d[0] = a;
+    }
+    __syncthreads();
+    esum[cls] = SM.red_d[0];
+    __syncthreads();
+  }
+  {
+    const double sA = 10.0 / (double)(mx[0] - mn[0]), sB = 10.0 / (double)(mx[1] - mn[1]);
+    const double iA = 1.0 / esum[0], iB = 1.0 / esum[1];
+    double ls = 0.0;
+    for (int uu = tid; uu < U; uu += nt) {
+      double a = ((double)(dist[uu] - mn[0]) - mean[0]) * sA;
+      double b = ((double)(dist[S + uu] - mn[1]) - mean[1]) * sB;
+      float ah = (float)a, bh = (float)b;
+      double eA = (double)expf(ah) * (1.0 + (double)(float)(a - (double)ah));
+      double eB = (double)expf(bh) * (1.0 + (double)(float)(b - (double)bh));
+      double Pu = eA * iA, Qu = eB * iB;
+      double M = 0.5 * (Pu + Qu);
+      // 1/2 P log(P/M) + 1/2 Q log(Q/M) = 1/2 M phi(delta), delta = (P-Q)/(P+Q)
+      float dl = (float)((Pu - Qu) / (Pu + Qu));
+      float ad = fabsf(dl);
+      float phi;
+      if (ad < 0.25f) {
+        float d2 = dl * dl, term = d2, acc = 0.f;
+        for (int kk = 1; kk <= 12; kk++) {
+          acc += term / (float)(kk * (2 * kk - 1));
+          term *= d2;
+        }
+        phi = acc;
+      } else if (ad >= 1.f) {
+        phi = 2.f * 0.69314718055994531f;
+      } else {
+        phi = (1.f + dl) * log1pf(dl) + (1.f - dl) * log1pf(-dl);
+      }
+      ls += 0.5 * M * (double)phi;
+      if (keep >= 0) {
+        bd.out_lval[((size_t)keep * 2 + 0) * S + uu] = Pu;
+        bd.out_lval[((size_t)keep * 2 + 1) * S + uu] = Qu;
+      }
+    }
+    for (int o = 16; o > 0; o >>= 1) ls += __shfl_down_sync(0xffffffffu, ls, o);
+    if (lane == 0) SM.red_d[warp] = ls;
+    __syncthreads();
+    if (tid == 0) {
+      double a = 0;
+      for (int w = 0; w < nw; w++) a += SM.red_d[w];
+      js = a / 0.69314718055994530942;
+      bool degenerate = (mx[0] == mn[0]) || (mx[1] == mn[1]);
+      if (degenerate) js = __longlong_as_double(0x7ff8000000000000ll);
+      bd.js[u] = js;
+      bd.U[u] = U;
+      bd.status[u] = SM.status;
+    }
+  }
+
+  // ---- P7: detailed outputs of kept units
+  if (keep >= 0) {
+    const int mpk = bd.mpk;
+    const double fx = ldexp(1.0, -sd.lg_shift);
+    for (int uu = tid; uu < U; uu += nt) {
+      bd.out_ids[(size_t)keep * S + uu] = urep[uu];
+      bd.out_dist[((size_t)keep * 2 + 0) * S + uu] = (double)dist[uu] * fx;
+      bd.out_dist[((size_t)keep * 2 + 1) * S + uu] = (double)dist[S + uu] * fx;
+    }
+    for (int i = tid; i < 2 * g * GW; i += nt)
+      bd.out_rows[(size_t)keep * 2 * g * GW + i] = P.rows[i];
+    // full capped lists of every unique network: warp per network
+    for (int uu = warp; uu < U; uu += nw) {
+      const int s = urep[uu];
+      int k, sigma;
+      net_of(s, sd, P, k, sigma);
+      load_stsig(sd, sigma, myst, lane);
+      for (int t = lane; t < g; t += 32) {
+        ListGen G;
+        gen_for(G, sd, P, phi[k], pcol[k], k, t, sigma >= 0 ? myst : nullptr);
+        int cnt = 0;
+        while (cnt < sd.mp) {
+          int j = G.next();
+          if (j < 0) break;
+          if (cnt < mpk) bd.out_par[(((size_t)keep * S + uu) * g + t) * mpk + cnt] = j;
+          cnt++;
+        }
+        bd.out_cnt[((size_t)keep * S + uu) * g + t] = cnt;
+      }
+      __syncwarp();
+    }
+  }
+}
+
+// ------------------------------------------------------------ launchers
+cudaError_t launch_prep(const int8_t *vals, int g, int n, int W, int c, uint64_t *planes,
+                        uint64_t *valid, uint16_t *ctot, cudaStream_t st) {
+  int tot = g * W;
+  k_planes<<<(tot + 127) / 128, 128, 0, st>>>(vals, g, n, W, planes, valid);
+  if (c > 0) k_ctot<<<(c + 127) / 128, 128, 0, st>>>(planes, g, W, c, ctot);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_counter_masks(int n, int nA, int W, uint64_t seed, const int32_t *unit_set,
+                                 const int32_t *unit_perm, const uint64_t *mask0, uint64_t *masks,
+                                 int B, cudaStream_t st) {
+  int P = 1;
+  while (P < n) P <<= 1;
+  size_t smem = sizeof(unsigned long long) * P;
+  if (smem > 96 * 1024) {
+    cudaFuncSetAttribute(k_counter_masks, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  }
+  k_counter_masks<<<B, 512, smem, st>>>(n, nA, W, seed, unit_set, unit_perm, mask0, masks);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_pairs(const SetDev &sd, const uint64_t *masks, uint32_t *dmask, int B,
+                         unsigned long long *stats, cudaStream_t st) {
+  if (sd.c == 0) return cudaSuccess;
+  dim3 grid((sd.c + 127) / 128, B);
+  k_pairs<<<grid, 128, sizeof(uint64_t) * sd.W, st>>>(sd, masks, dmask, stats);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_units(const SetDev &sd, const BatchDev &bd, cudaStream_t st) {
+  const int threads = 256;
+  size_t smem = unit_smem_bytes(sd.g, sd.W, sd.GW, threads / 32);
+  cudaError_t e = cudaFuncSetAttribute(k_units, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  k_units<<<bd.B, threads, smem, st>>>(sd, bd);
+  return cudaGetLastError();
+}
+
+cudaError_t set_divisor_map(const int8_t *map82) {
+  return cudaMemcpyToSymbol(c_dmap, map82, 82);
+}
+
+}  // namespace eddy

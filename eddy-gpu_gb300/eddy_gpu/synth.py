@@ -1,0 +1,155 @@
+"""Seeded synthetic inputs with the shapes of the five benchmark workloads.
+
+The reference reads an already-discretised ternary matrix (main.cu:297) and
+has no discretisation rule of its own; this generator defines one: per-gene
+equal-frequency tertiles of the continuous values, ties to the lower bin,
+-> {-1, 0, 1}.  Planted dependencies act on class-1 samples only.
+
+Workloads (genes x samples, class sizes, sets, flags):
+  1  20 x 200 (100/100), 6 planted genes (0.8 x sum of 3 others + N(0, .5^2)),
+     one set of 20, -mp 3 -r 100 -pw 0
+  2  40 x 400 (150/250), 10 planted dependencies (1-3 parents, w ~ U(.5, 1),
+     noise .5), one set of 40 with 30 prior pairs, -pw .5 -mp 3 -r 200
+  3  5000 x 600 (300/300), 2% planted, 500 sets of U{10..150} genes, 20% of
+     sets with 5-20 prior pairs, -pw .5 -mp 3 -r 1000
+  4  200 x 1000 (400/600), 40 planted dependencies of strength near the
+     Bonferroni edge threshold, one set of 200, -mp 4 -r 10000
+  5  20000 x 1000 (500/500), log-normal then log, 2000 sets of log-normal
+     sizes clipped to 5-300 (median 40), 0-30 prior pairs, -pw .5 -mp 3 -r 1000
+"""
+from __future__ import annotations
+
+import os
+
+import numpy as np
+
+
+def tertiles(x: np.ndarray) -> np.ndarray:
+    """Per-row equal-frequency tertiles -> int8 {-1, 0, 1}, ties low."""
+    n = x.shape[1]
+    s = np.sort(x, axis=1)
+    t1 = s[:, int(np.ceil(n / 3)) - 1][:, None]
+    t2 = s[:, int(np.ceil(2 * n / 3)) - 1][:, None]
+    return np.where(x <= t1, -1, np.where(x <= t2, 0, 1)).astype(np.int8)
+
+
+def _plant(rng, x, nA, targets, parents, weights, noise):
+    for t, ps, ws in zip(targets, parents, weights):
+        x[t, :nA] = sum(w * x[p, :nA] for p, w in zip(ps, ws)) + noise * rng.standard_normal(nA)
+
+
+def _random_priors(rng, g, k):
+    pairs = set()
+    while len(pairs) < min(k, g * (g - 1) // 2):
+        i, j = rng.choice(g, 2, replace=False)
+        pairs.add((min(i, j), max(i, j)))
+    pr = np.zeros((g, g), np.uint8)
+    for i, j in pairs:
+        pr[i, j] = pr[j, i] = 1
+    return pr
+
+
+class Workload:
+    """data (G x n int8), labels (n, 0 = class 1), sets [(name, gene idx,
+    prior g x g or None)], flags dict."""
+
+    def __init__(self, name, data, labels, sets, flags):
+        self.name, self.data, self.labels, self.sets, self.flags = name, data, labels, sets, flags
+
+
+def make(cfg: int, seed: int = 0, n_sets: int | None = None, scale: float = 1.0) -> Workload:
+    rng = np.random.default_rng(seed)
+    if cfg == 1:
+        G, nA, nB = 20, 100, 100
+        x = rng.standard_normal((G, nA + nB))
+        others = list(range(6, G))
+        parents = [list(rng.choice(others, 3, replace=False)) for _ in range(6)]
+        _plant(rng, x, nA, range(6), parents, [[0.8] * 3] * 6, 0.5)
+        sets = [("SET1", np.arange(G), None)]
+        flags = dict(mp=3, r=100, pw=0.0)
+    elif cfg == 2:
+        G, nA, nB = 40, 150, 250
+        x = rng.standard_normal((G, nA + nB))
+        targets = rng.choice(G, 10, replace=False)
+        rest = [i for i in range(G) if i not in set(targets)]
+        parents = [list(rng.choice(rest, rng.integers(1, 4), replace=False)) for _ in targets]
+        weights = [list(rng.uniform(0.5, 1.0, len(p))) for p in parents]
+        _plant(rng, x, nA, targets, parents, weights, 0.5)
+        sets = [("SET2", np.arange(G), _random_priors(rng, G, 30))]
+        flags = dict(mp=3, r=200, pw=0.5)
+    elif cfg == 3:
+        G, nA, nB = 5000, 300, 300
+        x = rng.standard_normal((G, nA + nB))
+        k = int(0.02 * G)
+        targets = rng.choice(G, k, replace=False)
+        rest = np.setdiff1d(np.arange(G), targets)
+        parents = [list(rng.choice(rest, rng.integers(1, 4), replace=False)) for _ in targets]
+        weights = [list(rng.uniform(0.5, 1.0, len(p))) for p in parents]
+        _plant(rng, x, nA, targets, parents, weights, 0.5)
+        ns = n_sets or 500
+        sets = []
+        for s in range(ns):
+            g = int(rng.integers(10, 151))
+            genes = np.sort(rng.choice(G, g, replace=False))
+            pr = _random_priors(rng, g, int(rng.integers(5, 21))) if rng.random() < 0.2 else None
+            sets.append((f"SET3_{s:04d}", genes, pr))
+        flags = dict(mp=3, r=1000, pw=0.5)
+    elif cfg == 4:
+        G, nA, nB = 200, 400, 600
+        x = rng.standard_normal((G, nA + nB))
+        targets = rng.choice(G, 40, replace=False)
+        rest = [i for i in range(G) if i not in set(targets)]
+        parents = [[int(rng.choice(rest))] for _ in targets]
+        # strengths around the Bonferroni threshold of 19900 pair tests
+        weights = [[float(rng.uniform(0.22, 0.34))] for _ in targets]
+        _plant(rng, x, nA, targets, parents, weights, 1.0)
+        sets = [("SET4", np.arange(G), None)]
+        flags = dict(mp=4, r=10000, pw=0.5)
+    elif cfg == 5:
+        G, nA, nB = 20000, 500, 500
+        x = np.log(np.exp(rng.standard_normal((G, nA + nB))))
+        ns = n_sets or 2000
+        sizes = np.clip(np.round(np.exp(rng.normal(np.log(40), 0.8, ns))), 5, 300).astype(int)
+        sets = []
+        for s in range(ns):
+            genes = np.sort(rng.choice(G, sizes[s], replace=False))
+            k = int(rng.integers(0, 31))
+            sets.append((f"SET5_{s:04d}", genes, _random_priors(rng, sizes[s], k) if k else None))
+        flags = dict(mp=3, r=1000, pw=0.5)
+    else:
+        raise ValueError(cfg)
+    data = tertiles(x)
+    labels = np.concatenate([np.zeros(nA, np.uint8), np.ones(nB, np.uint8)])
+    return Workload(f"config{cfg}", data, labels, sets, flags)
+
+
+def write_files(w: Workload, outdir: str, class_names=("CLASS_A", "CLASS_B")) -> dict:
+    """Writes -d / -c / -g files and PRIORS/<set>.prior in the reference's
+    formats (main.cu:255-352, 359-503), with the trailing blank line the
+    reference's row counter expects (main.cu:276-283)."""
+    os.makedirs(outdir, exist_ok=True)
+    G, n = w.data.shape
+    gnames = [f"G{i:05d}" for i in range(G)]
+    snames = [f"S{s:05d}" for s in range(n)]
+    d = os.path.join(outdir, f"{w.name}_expr.txt")
+    with open(d, "w") as f:
+        f.write("gene_id\t" + "\t".join(snames) + "\n")
+        for i in range(G):
+            f.write(gnames[i] + "\t" + "\t".join(map(str, w.data[i].tolist())) + "\n")
+        f.write("\n")
+    c = os.path.join(outdir, f"{w.name}_class.txt")
+    with open(c, "w") as f:
+        f.write("\t".join(class_names[int(v)] for v in w.labels) + "\n")
+    gm = os.path.join(outdir, f"{w.name}.gmt")
+    os.makedirs(os.path.join(outdir, "PRIORS"), exist_ok=True)
+    with open(gm, "w") as f:
+        for name, genes, pr in w.sets:
+            f.write(name + "\thttp://none\t" + "\t".join(gnames[i] for i in genes) + "\n")
+            if pr is not None:
+                with open(os.path.join(outdir, "PRIORS", name + ".prior"), "w") as fp:
+                    g = len(genes)
+                    for a in range(g):
+                        for b in range(a + 1, g):
+                            if pr[a, b]:
+                                fp.write(f"{gnames[genes[a]]}\tpp\t{gnames[genes[b]]}\n")
+    return dict(d=d, c=c, g=gm, genes=gnames, samples=snames)

@@ -1,0 +1,154 @@
+/*
+ * eddy_gpu.h -- C ABI of libeddy_gpu, the GB300 (sm_103a) implementation of
+ * EDDY's per-class dependency-network inference and class-label
+ * permutation test (the hot path of skimlab/eddy-gpu's ./eddy).
+ *
+ * The reference has no library boundary: its interface is the process
+ * (main.cu:27-1711).  Each entry point below replaces one block of that
+ * process; the citation names it.  Conventions:
+ *   - every function returns an int status (EDDY_OK = 0) and never exits;
+ *   - the library copies all caller input buffers; result buffers are
+ *     caller-allocated (sizes are queried first) and filled by copy;
+ *   - one context = one CUDA device and one stream, single-threaded use;
+ *   - arrays are plain C pointers and sizes, no framework types.
+ * Vocabulary: genes x samples expression matrix (ternary -1/0/1, any other
+ * value is "not counted" like the reference's sscanf("%d") values outside
+ * {-1,0,1}, kernel1.cu:91-118); class 0 = the reference's class1 (first
+ * label of the class file), class 1 = class2; a gene set of g genes; a
+ * unit = one gene set under one labelling (permutation); S = n + 2
+ * leave-one-out networks per unit.
+ */
+#ifndef EDDY_GPU_H
+#define EDDY_GPU_H
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define EDDY_OK 0
+#define EDDY_ERR_ARG 1        /* invalid argument or size */
+#define EDDY_ERR_CUDA 2       /* CUDA runtime error (message via eddy_last_error) */
+#define EDDY_ERR_STATE 3      /* call out of order (e.g. results before eddy_run) */
+#define EDDY_ERR_CAPACITY 4   /* set too large for the GPU path (g > 512) */
+#define EDDY_ERR_BETAFIT 5    /* beta fit has alpha/beta <= 0 or non-finite */
+#define EDDY_ERR_INTERNAL 6   /* an internal consistency check failed */
+
+/* Label-permutation streams.  GLIBC reproduces main.cu:538-573 exactly
+ * (glibc rand(), never reseeded, one stream across all gene sets);
+ * COUNTER uses Philox-4x32-10 keyed by (seed, set, permutation, sample);
+ * EXTERNAL takes caller-supplied labellings (eddy_set_labellings). */
+#define EDDY_RNG_GLIBC 0
+#define EDDY_RNG_COUNTER 1
+#define EDDY_RNG_EXTERNAL 2
+
+/* Run options: the reference's command-line values after its defaults and
+ * clamps (main.cu:118-202). */
+typedef struct {
+  int max_parents;          /* -mp (main.cu:129-130, 171-175) */
+  double alpha_edge;        /* -pE, or 1-theta^(1/lambda) with -t (main.cu:188-192) */
+  double alpha_edge_prior;  /* 1-(1-alpha_edge)*pw^(1/lambda) (main.cu:195) */
+  int bonferroni;           /* 0 with -rawp (main.cu:141-142) */
+  int permutations;         /* -r, iterations incl. the unpermuted one (main.cu:538) */
+  int rng;                  /* EDDY_RNG_* */
+  uint64_t seed;            /* COUNTER stream key */
+  int device;               /* CUDA device ordinal */
+  int keep_networks;        /* 1: keep iteration-0 networks for the output files */
+} eddy_opts;
+
+typedef struct eddy_ctx eddy_ctx;
+
+/* Creates a context (replaces main.cu's globals and device choice). */
+int eddy_ctx_create(const eddy_opts *opts, eddy_ctx **out);
+/* Releases everything the context holds. */
+int eddy_ctx_destroy(eddy_ctx *ctx);
+/* Text of the last error of this context (never NULL). */
+const char *eddy_last_error(const eddy_ctx *ctx);
+
+/* Expression matrix and class labels (replaces main.cu:255-352: the
+ * parsed `data` matrix, gene-major, and classIDs).  data: genes x samples,
+ * class_of_sample: samples entries, 0 or 1. */
+int eddy_load_matrix(eddy_ctx *ctx, const int8_t *data, int genes, int samples,
+                     const uint8_t *class_of_sample);
+
+/* Adds a gene set (replaces main.cu:375-503: genesetIndexIntoData and the
+ * prior matrix).  gene_idx: g row indices into the matrix (duplicates
+ * allowed, kept in order); prior: g x g 0/1 (NULL = no prior file).
+ * *set_id receives the set's index (0, 1, ... in call order). */
+int eddy_add_set(eddy_ctx *ctx, const int32_t *gene_idx, int g, const uint8_t *prior,
+                 int *set_id);
+
+/* Caller-supplied labellings for EDDY_RNG_EXTERNAL (replaces the
+ * permutation loop's classIDs, main.cu:561-570).  labels: R x samples,
+ * row 0 is the unpermuted labelling. */
+int eddy_set_labellings(eddy_ctx *ctx, int set_id, const uint8_t *labels, int R);
+
+/* Runs every set: all permutations of the hot path (main.cu:538-1460) and
+ * the beta fit (main.cu:1465-1502). */
+int eddy_run(eddy_ctx *ctx);
+
+typedef struct {
+  int genes;            /* g */
+  int iterations;       /* JS values computed (R, or 1 after a NaN JS0 break) */
+  int failed;           /* 1 = NaN JS (main.cu:1431-1435, 1465-1479) */
+  int betafit_ok;       /* 0 when alpha/beta are not positive finite */
+  int unique0;          /* unique networks of iteration 0 (main.cu:1123-1125) */
+  double js0;           /* JS of iteration 0 (main.cu:1482) */
+  double alpha, beta;   /* beta fit (main.cu:1491-1495) */
+  double pddn;          /* ibetac(alpha, beta, js0) (main.cu:1497) */
+  uint64_t exact_rechecks;  /* tables re-evaluated in FP64 */
+  uint64_t tables;          /* tables decided */
+} eddy_set_summary;
+
+/* Per-set results (replaces the printed lines and results.txt row). */
+int eddy_get_set_summary(const eddy_ctx *ctx, int set_id, eddy_set_summary *out);
+/* JS value and unique-network count of every iteration (jsVals,
+ * main.cu:1427; unisum, main.cu:1088-1103).  Arrays of `iterations`. */
+int eddy_get_js(const eddy_ctx *ctx, int set_id, double *js, int32_t *unique);
+
+/* Iteration-0 unique networks for the _Networks and _BDEU_SCORES files
+ * (first_uniNodes/first_uniEdges/first_uniEpn/uniqueNetIds/first_lval1,
+ * main.cu:1087-1187, 1406-1409).  Query with NULL arrays to get *U and
+ * *edges; then ids[U], nodes[U*g] (exclusive prefix of capped parent
+ * counts, pNodes layout), epn[U+1], edges_out[edges], lval[2*U]
+ * (class-0 likelihoods then class-1). */
+int eddy_get_networks(const eddy_ctx *ctx, int set_id, int *U, int *edges, int32_t *ids,
+                      int32_t *nodes, int32_t *epn, int32_t *edges_out, double *lval);
+
+/* Uncapped parent lists of the two full-data networks of iteration 0 for
+ * the _EdgeList file (main.cu:1530-1617): nodes[2*g], epn[3], edges_out.
+ * Query with NULL arrays for *edges. */
+int eddy_get_edge_list(const eddy_ctx *ctx, int set_id, int *edges, int32_t *nodes,
+                       int32_t *epn, int32_t *edges_out);
+
+/* ------------------------------------------------ stage-level entry points
+ * Direct access to the hot path for one gene set and explicit labellings,
+ * without the permutation driver: the GPU counterparts of the reference's
+ * per-permutation kernel sequence (run2 .. run4 + normalisation + JS).
+ * labels: R x samples.  js[R], unique[R]. */
+int eddy_run_labellings(eddy_ctx *ctx, int set_id, const uint8_t *labels, int R, double *js,
+                        int32_t *unique);
+
+/* Edge decisions of all S networks of one labelling, S x c bytes (the
+ * reference's out23 array after run2/run2Scalable, kernel1.cu:426-431). */
+int eddy_debug_edges(eddy_ctx *ctx, int set_id, const uint8_t *labels, uint8_t *edges);
+
+/* Details of one labelling: unique network ids [S], capped parent counts
+ * [S*g] and lists [S*g*mpk] (-1 padded), node-summed BDeu [2*S] and
+ * normalised likelihoods [2*S] of the unique networks (class 0 block then
+ * class 1, each S long); *U receives the unique count, *js the JS. */
+int eddy_debug_unit(eddy_ctx *ctx, int set_id, const uint8_t *labels, int mpk, int *U,
+                    double *js, int32_t *ids, int32_t *counts, int32_t *parents, double *dist,
+                    double *lval);
+
+/* Timing of the last eddy_run / eddy_run_labellings, device side (CUDA
+ * events around the kernels) in milliseconds, and the number of kernel
+ * launches it made. */
+int eddy_last_timing(const eddy_ctx *ctx, double *ms_kernels, double *ms_pairs, double *ms_units,
+                     long long *launches);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

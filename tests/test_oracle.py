@@ -1,0 +1,206 @@
+"""The oracle pinned against the reference: golden vectors produced by the
+reference's own kernel and host-routine sources (tests/golden), and
+known-answer tests from independent implementations (scipy)."""
+import json
+import os
+
+import numpy as np
+import pytest
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+GOLD = os.path.join(HERE, "golden")
+
+
+def _load():
+    z = np.load(os.path.join(GOLD, "units.npz"))
+    return z, [str(k) for k in z["cases"]]
+
+
+Z, CASES = _load()
+
+
+def _params(O, key):
+    mp, ae, ap, bonf = Z[key + "_params"]
+    return O.Params(int(mp), float(ae), float(ap), int(bonf))
+
+
+@pytest.mark.parametrize("key", CASES)
+def test_oracle_matches_reference_golden(key, oracle_lib):
+    O = oracle_lib
+    data, lab, pr = Z[key + "_data"], Z[key + "_labels"], Z[key + "_prior"]
+    prm = _params(O, key)
+    r = O.unit(data, lab, pr, prm)
+    shape = tuple(Z[key + "_edges_shape"])
+    edges = np.unpackbits(Z[key + "_edges"])[:int(np.prod(shape))].reshape(shape)
+    assert np.array_equal(r["edges"], edges)
+    U, E, S = (int(v) for v in Z[key + "_scal"])
+    assert (r["U"], r["total_edges"], r["S"]) == (U, E, S)
+    assert np.array_equal(r["unique_ids"], Z[key + "_unique_ids"])
+    assert np.array_equal(r["uni_nodes"].ravel(), Z[key + "_uni_nodes"].ravel())
+    assert np.array_equal(r["uni_edges"], Z[key + "_uni_edges"])
+    assert np.array_equal(r["uni_epn"], Z[key + "_uni_epn"])
+    # same libm family on both sides (glibc): identical up to a few ulps
+    np.testing.assert_allclose(r["out5"].ravel(), Z[key + "_out5"].ravel(), rtol=1e-13, atol=1e-12)
+    np.testing.assert_allclose(r["lval"].ravel(), Z[key + "_lval"].ravel(), rtol=1e-11, atol=1e-15)
+    js, jg = r["js"], float(Z[key + "_js"][0])
+    assert (np.isnan(js) and np.isnan(jg)) or abs(js - jg) <= 1e-12 * max(1.0, abs(jg))
+
+
+@pytest.mark.parametrize("key", CASES)
+def test_oracle_stages_match_golden(key, oracle_lib):
+    """K2/K3 parent lists and K1 state counts against the reference's arrays."""
+    O = oracle_lib
+    shape = tuple(Z[key + "_edges_shape"])
+    edges = np.unpackbits(Z[key + "_edges"])[:int(np.prod(shape))].reshape(shape)
+    g = Z[key + "_data"].shape[0]
+    mp = int(Z[key + "_params"][0])
+    pn, epn, pe = O.parents(edges, g, mp)
+    assert np.array_equal(pn.ravel(), Z[key + "_pnodes"].ravel())
+    assert np.array_equal(epn, Z[key + "_edges_pn"])
+    assert np.array_equal(pe, Z[key + "_pedges"])
+    lab = Z[key + "_labels"]
+    data = Z[key + "_data"]
+    _, ppn, stf = O.k1_edges(data[:, lab == 0], data[:, lab == 1], Z[key + "_prior"],
+                             _params(O, key))
+    assert np.array_equal(ppn, Z[key + "_ppn"])
+    assert np.array_equal(stf, Z[key + "_stf"])
+
+
+def test_gammds_golden_and_scipy(oracle_lib):
+    """AS 147 (kernel1.cu:10-74) vs the reference's host twin and scipy."""
+    from scipy.special import gammainc
+    g = np.load(os.path.join(GOLD, "gammds.npz"))
+    for i, x in enumerate(g["x"]):
+        for j, p in enumerate(g["p"]):
+            v = oracle_lib.gammds(x, p)
+            assert v == g["value"][i, j] or abs(v - g["value"][i, j]) <= 1e-15
+            if x > 0 and p > 0 and v > 0:
+                # the series truncates at a relative term of 1e-9
+                assert abs(v - gammainc(p, x)) <= 5e-9 * gammainc(p, x) + 1e-300
+    # underflow cliff: AS 147 returns 0 when the first term underflows 1e-37
+    assert oracle_lib.gammds(100.0, 2.0) == 0.0
+    assert oracle_lib.gammds(0.0, 2.0) == 0.0 and oracle_lib.gammds(3.0, 0.0) == 0.0
+
+
+def test_chisq_known_tables(oracle_lib):
+    O = oracle_lib
+    # balanced independent table: chi = 0, dof 4, no Yates (e = 10)
+    chi, dof = O.chisq([10, 10, 10, 10, 10, 10, 10, 10, 10])
+    assert dof == 4 and chi == 0.0
+    # rows (20, 10), cols (15, 15): e = (10, 10, 5, 5); e == 5 is not < 5, no Yates
+    chi, dof = O.chisq([12, 8, 0, 3, 7, 0, 0, 0, 0])
+    assert dof == 1 and abs(chi - (0.4 + 0.4 + 0.8 + 0.8)) < 1e-12
+    # rows (20, 8), cols (15, 13): smallest expected 8*13/28 < 5 -> Yates 0.5
+    t = np.array([[12, 8], [3, 5]], float)
+    chi, dof = O.chisq([12, 8, 0, 3, 5, 0, 0, 0, 0])
+    e = np.outer(t.sum(1), t.sum(0)) / t.sum()
+    ref = (((np.abs(t - e) - 0.5) ** 2) / e).sum()
+    assert dof == 1 and abs(chi - ref) < 1e-12
+    # a single populated row: dof = (3-1-1)*(3-2-1) = 0
+    chi, dof = O.chisq([5, 6, 7, 0, 0, 0, 0, 0, 0])
+    assert dof == 0
+    # empty table: dof (3-3-1)*(3-3-1) = 1 and chi = 0 -> p = 1
+    chi, dof = O.chisq([0] * 9)
+    assert dof == 1 and chi == 0.0
+    prm = O.params(mp=3, bonferroni=False)
+    assert O.lib().or_edge_decision(0.0, 1, 5, 0, prm) == 0
+
+
+def test_ibetac_against_scipy(oracle_lib):
+    from scipy.special import betaincc
+    rng = np.random.default_rng(0)
+    for _ in range(200):
+        a, b = rng.uniform(0.2, 400, 2)
+        x = rng.uniform(0, 1)
+        v, r = oracle_lib.ibetac(a, b, x), betaincc(a, b, x)
+        assert abs(v - r) <= 1e-10 * max(r, 1e-300) + 1e-14, (a, b, x, v, r)
+    assert np.isnan(oracle_lib.ibetac(-1, 2, 0.5))
+
+
+def test_pddn_fit_and_errors(oracle_lib):
+    from scipy.special import betaincc
+    rng = np.random.default_rng(1)
+    js = rng.beta(20, 5, 300)
+    rc, a, b, p = oracle_lib.pddn(js)
+    mu, var = js.mean(), js.var()
+    ea = ((1 - mu) / var - 1 / mu) * mu * mu
+    assert rc == 0 and abs(a - ea) < 1e-9 * ea
+    assert abs(p - betaincc(a, b, js[0])) < 1e-10
+    rc, a, b, p = oracle_lib.pddn(np.full(10, 0.5))  # var = 0 -> alpha inf
+    assert rc == -1 and np.isnan(p)
+
+
+def test_js_identical_and_disjoint(oracle_lib):
+    O = oracle_lib
+    p = np.array([0.2, 0.3, 0.5])
+    assert abs(O.lib().or_js(3, p, p.copy())) < 1e-15
+    a = np.array([1.0, 0.0])
+    b = np.array([0.0, 1.0])
+    assert abs(O.lib().or_js(2, a, b) - 1.0) < 1e-15
+
+
+def test_normalise_single_network_is_nan(oracle_lib):
+    out = np.zeros(1)
+    oracle_lib.lib().or_normalise(1, np.array([-123.0]), out)
+    assert np.isnan(out[0])
+
+
+def test_glibc_stream_restatement(oracle_lib):
+    """glibc rand() ≡ the additive-feedback restatement, and the reference's
+    sampler (main.cu:541-570) consumes n + (draws until n distinct)."""
+    import ctypes
+    libc = ctypes.CDLL(None)
+    libc.srand(1)
+    first = [libc.rand() for _ in range(5)]
+    # restatement: TYPE_3, degree 31, separation 3, 310 discarded outputs
+    r = [0] * 34
+    r[0] = 1
+    for i in range(1, 31):
+        hi, lo = divmod(r[i - 1], 127773)
+        w = 16807 * lo - 2836 * hi
+        r[i] = w + 2147483647 if w < 0 else w
+    for i in range(31, 34):
+        r[i] = r[i - 31]
+    seq = r[:]
+    out = []
+    while len(out) < 344 + 5:
+        k = len(seq)
+        seq.append((seq[k - 31] + seq[k - 3]) & 0xFFFFFFFF)
+        out.append(seq[-1] >> 1)
+    assert first == out[344 - 34:344 - 34 + 5]
+    lab0 = np.array([0] * 7 + [1] * 5, np.uint8)
+    a = oracle_lib.glibc_labels(12, 7, lab0, 4, reset=True)
+    assert np.array_equal(a[0], lab0)
+    assert all((row == 0).sum() == 7 for row in a)
+
+
+def test_writer_golden_is_consistent():
+    w = json.load(open(os.path.join(GOLD, "writers.json")))
+    assert w["networks"].startswith("\t\tUnique Networks\n\ninput : expr.txt\n")
+    assert "BDEU SCORES" in w["bdeu"]
+
+
+def test_reference_emulator_matches_oracle_random(oracle_lib):
+    """Where the reference sources were compiled (oracle/_ref), random cases
+    beyond the committed fixtures."""
+    O = oracle_lib
+    if not O.ref_available():
+        pytest.skip("reference CPU build not present (no reference sources here)")
+    rng = np.random.default_rng(7)
+    for t in range(6):
+        g = int(rng.integers(3, 30))
+        n = int(rng.integers(6, 60))
+        nA = int(rng.integers(2, n - 2))
+        x = rng.standard_normal((g, n))
+        x[-1, :nA] = x[0, :nA] + 0.5 * rng.standard_normal(nA)
+        s = np.sort(x, axis=1)
+        d = np.where(x <= s[:, [n // 3]], -1, np.where(x <= s[:, [2 * n // 3]], 0, 1)).astype(np.int8)
+        lab = np.ones(n, np.uint8)
+        lab[rng.choice(n, nA, replace=False)] = 0
+        prm = O.params(mp=int(rng.integers(1, 5)), bonferroni=bool(t % 2),
+                       alpha_edge=float(rng.uniform(0.01, 0.4)))
+        a, b = O.unit(d, lab, None, prm), O.ref_unit(d, lab, None, prm)
+        assert np.array_equal(a["edges"], b["edges"])
+        assert a["U"] == b["U"] and np.array_equal(a["unique_ids"], b["unique_ids"])
+        assert np.allclose(a["out5"], b["out5"], rtol=1e-13, atol=1e-12)
+        assert (np.isnan(a["js"]) and np.isnan(b["js"])) or abs(a["js"] - b["js"]) < 1e-12
