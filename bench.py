@@ -1,0 +1,335 @@
+"""Benchmark of the EDDY permutation test on GB300: gene-set x permutation
+units per second, exact edges.
+
+Workload (one gene set, the largest single-GPU configuration the metric is
+quoted on): 200 genes x 1000 samples (classes 400/600), -mp 4, a stretch of
+the -r 10000 permutation test; synthetic seeded data with the shapes of the
+"precision stress" workload (eddy_gpu/synth.py config 4).  One step = one
+batch of `--units` permutations (default 2048) of that set.
+
+  value  device time of the hot path with the set resident in HBM (CUDA
+         events on the library's launching stream around K steps; labellings
+         generated on the device from the counter stream).
+  e2e    the same units through the public C ABI per step: the matrix and
+         labels copied from pinned host memory, the set added, eddy_run
+         (iteration 0 with its networks, the permutations, the beta fit) and
+         the JS values read back.
+  cpu_baseline  the oracle (CPU restatement of the reference kernels, FP64,
+         OpenMP over units) on a bounded sample of the same units.
+
+`--impl reference` runs the reference's algorithm on the host cores (the
+oracle port: the reference's own hot path exists only as CUDA kernels; its
+CPU build here runs under a thread emulator and is not a performance arm)
+on the same workload, each step a bounded sample of units.
+Multi-GPU: every rank processes its own permutation indices (weak scaling,
+no collective on the data path); timing is the max over ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+for _p in (os.path.join(ROOT, "eddy-gpu_gb300"), os.path.join(ROOT, "oracle")):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+import numpy as np  # noqa: E402
+
+METRIC = "gene-set x permutations/sec, batched FP32 vs plain FP64 on one GB300, exact edges"
+UNIT = "units/s"
+WORKLOAD = "config 4: one 200-gene set x 1000 samples (400/600), -mp 4, permutations of -r 10000"
+
+
+def load_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return d.get("hbm_gbs", 6800.0), d.get("bf16_tflops", 1900.0), "measured"
+    return 6800.0, 1900.0, "fallback"
+
+
+def algorithmic_bytes(g, n, mp):
+    """Per-unit algorithmic bytes of the two kernels (each stage reads its
+    inputs and writes its outputs once through HBM):
+    contingency+decision kernel: 2 classes x c pairs x 10 distinct tables x
+    36 B read, S x c edge bits written; network+BDeu+JS kernel: S x c edge
+    bits read, S x g x mp 2-byte parents and S 8-byte hashes written, 2 x g x
+    n bytes of class data read, 2 x S 4-byte scores written."""
+    c = g * (g - 1) // 2
+    S = n + 2
+    pairs = 2 * c * 10 * 36 + S * c / 8
+    units = S * c / 8 + S * g * mp * 2 + S * 8 + 2 * g * n + 2 * S * 4
+    return pairs, units
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+
+    def __init__(self, index=0):
+        self.index = index
+        self.rows = []
+        self.proc = None
+
+    def __enter__(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={q}", "--format=csv,noheader,nounits", "-lms", "200",
+                 "-i", str(self.index)], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 9:
+                self.rows.append(parts)
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in self.rows for i in range(4)
+                          if r[5 + i].lower().startswith("active")})
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons,
+                "samples": len(self.rows)}
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def cpu_sample(w, genes, seed, first, count, threads):
+    """Oracle (FP64, the reference's algorithm) on `count` units; returns
+    (units/s, seconds)."""
+    import oracle
+    lab = oracle.counter_labels(seed, 0, w.labels, first + count)[first:first + count]
+    prm = oracle.params(mp=w.flags["mp"], pw=w.flags["pw"])
+    t0 = time.perf_counter()
+    oracle.units(w.data[genes], lab, None, prm, threads=threads)
+    dt = time.perf_counter() - t0
+    return count / dt, dt
+
+
+def run_reference(args, rank, world):
+    """Reference arm: the reference's hot path on the host cores (oracle
+    port), same workload and metric; rank 0 only."""
+    if rank != 0:
+        return
+    from eddy_gpu import synth
+    import oracle
+    oracle.build(ref=False)
+    w = synth.make(4, seed=0)
+    genes = w.sets[0][1]
+    threads = os.cpu_count() or 1
+    per_step = args.cpu_units
+    for i in range(args.warmup):
+        cpu_sample(w, genes, 4242, 1 + i * per_step, per_step, threads)
+    t0 = time.perf_counter()
+    done = 0
+    for i in range(args.steps):
+        cpu_sample(w, genes, 4242, 1 + (args.warmup + i) * per_step, per_step, threads)
+        done += per_step
+    dt = time.perf_counter() - t0
+    v = done / dt
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT,
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1e3 * dt / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": WORKLOAD + f"; a bounded sample of {per_step} "
+                       "permutations per step", "units_per_step": per_step},
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": f"{per_step} permutations per step x {args.steps} steps"},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args, rank, world, local):
+    import torch
+    import torch.distributed as dist
+
+    torch.cuda.set_device(local)
+    if world > 1 and not dist.is_initialized():
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    import build as _build
+    _build.build()
+    import eddy_gpu
+    from eddy_gpu import synth
+
+    w = synth.make(4, seed=0)
+    genes = w.sets[0][1]
+    g, n = len(genes), w.data.shape[1]
+    mp, pw = w.flags["mp"], w.flags["pw"]
+    B = args.units
+    seed = 4242
+    ctx = eddy_gpu.Context(max_parents=mp, prior_weight=pw, permutations=B,
+                           rng=eddy_gpu.RNG_COUNTER, seed=seed, device=local, keep_networks=False)
+    stream = torch.cuda.current_stream()
+    ctx.set_stream(stream.cuda_stream)
+    ctx.load_matrix(w.data, w.labels)
+    sid = ctx.add_set(genes)
+    # each rank its own permutation indices
+    base = 1 + rank * (args.warmup + args.steps + 1) * B
+
+    def step(i):
+        js, U = ctx.run_permutations(sid, base + i * B, B)
+        t = ctx.timing()
+        return t
+
+    for i in range(args.warmup):
+        step(i)
+    # timed region: barrier + synchronize on both sides, events on the stream
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    acc = {"ms_pairs": 0.0, "ms_units": 0.0, "launches": 0}
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        e0.record(stream)
+        for i in range(args.steps):
+            t = step(args.warmup + i)
+            acc["ms_pairs"] += t["ms_pairs"]
+            acc["ms_units"] += t["ms_units"]
+            acc["launches"] += t["launches"]
+        e1.record(stream)
+        torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    if world > 1:
+        dist.barrier()
+        tt = torch.tensor([ms], device="cuda")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        ms = float(tt.item())
+    total_units = B * args.steps * world
+    value = total_units / (ms / 1e3)
+
+    # end to end through the public API with host buffers
+    data_pinned = torch.from_numpy(w.data).pin_memory().numpy()
+    labels_pinned = torch.from_numpy(w.labels).pin_memory().numpy()
+    ectx = eddy_gpu.Context(max_parents=mp, prior_weight=pw, permutations=B,
+                            rng=eddy_gpu.RNG_COUNTER, seed=seed + 1 + rank, device=local,
+                            keep_networks=True)
+
+    def e2e_step():
+        ectx.clear_sets()
+        ectx.load_matrix(data_pinned, labels_pinned)
+        s = ectx.add_set(genes)
+        ectx.run()
+        js, U = ectx.js(s)
+        return ectx.summary(s)
+
+    for _ in range(max(1, args.warmup)):
+        e2e_step()
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    launches_e2e = 0
+    for _ in range(args.steps):
+        e2e_step()
+        launches_e2e += ectx.timing()["launches"]
+    torch.cuda.synchronize()
+    e2e_s = time.perf_counter() - t0
+    if world > 1:
+        tt = torch.tensor([e2e_s], device="cuda")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        e2e_s = float(tt.item())
+    e2e_value = B * args.steps * world / e2e_s
+    W = (n + 63) // 64
+    h2d = w.data.size + n + 8 * B
+    d2h = 16 * B
+
+    if rank != 0:
+        return
+    hbm, bf16, peak_kind = load_peaks()
+    bp, bu = algorithmic_bytes(g, n, mp)
+    launches_per_kernel = args.steps  # one launch of each kernel per step (B units)
+    if acc["ms_pairs"] >= acc["ms_units"]:
+        kname, kms, kbytes = "k_pairs", acc["ms_pairs"], bp * B
+    else:
+        kname, kms, kbytes = "k_units", acc["ms_units"], bu * B
+    avg_ms = kms / launches_per_kernel
+    achieved = kbytes / (avg_ms / 1e3) / 1e9
+    traffic = None
+    tf = os.path.join(ROOT, "profiles", f"{kname}_traffic.json")
+    if os.path.exists(tf):
+        with open(tf) as f:
+            tr = json.load(f)
+        traffic = tr.get("bytes_per_unit", 0) * B if tr.get("bytes_per_unit") else None
+    cpu = None
+    if world == 1 and not args.no_cpu:
+        try:
+            cu, cs = cpu_sample(w, genes, seed, 1, args.cpu_units, os.cpu_count() or 1)
+            cpu = {"value": cu, "unit": UNIT, "cores": os.cpu_count() or 1, "kind": "port",
+                   "sample": f"{args.cpu_units} permutations of the same set ({cs:.1f} s)"}
+        except Exception as e:  # pragma: no cover - reported, not hidden
+            cpu = {"value": None, "unit": UNIT, "cores": 0, "kind": "port", "sample": f"failed: {e}"}
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "u8/i32 counts, f32 decisions + f64 rechecks",
+            "data": "synthetic (seeded, shapes of the precision-stress workload)",
+            "config": {"workload": WORKLOAD, "units_per_step": B, "genes": g, "samples": n,
+                       "max_parents": mp, "rng": "counter (Philox-4x32-10, on device)",
+                       "l2": "per-step working set (decision masks + per-unit scratch) "
+                             f"~{(B * (19900 * 4 + 420e3)) / 1e9:.2f} GB > L2"},
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h},
+            "gpu_launches": acc["launches"],
+            "stage_ms": {"k_pairs": acc["ms_pairs"], "k_units": acc["ms_units"]},
+            "roofline": {"kernel": kname, "bound": "hbm", "achieved": achieved, "peak": hbm,
+                         "unit": "GB/s", "frac": achieved / hbm, "traffic": traffic,
+                         "peak_source": f"MEASURED_PEAKS.json hbm_gbs ({peak_kind})",
+                         "algorithmic_bytes_per_launch": kbytes},
+            "clocks": clk.summary(),
+            "cpu_baseline": cpu}
+    print(json.dumps(line), flush=True)
+    ctx.close()
+    ectx.close()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--units", type=int, default=2048, help="permutations per step")
+    ap.add_argument("--cpu-units", type=int, default=16, help="permutations in the CPU sample")
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    rank, world, local = dist_env()
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+    else:
+        run_ours(args, rank, world, local)
+
+
+if __name__ == "__main__":
+    main()

@@ -84,6 +84,9 @@ struct eddy_ctx {
   double ms_total = 0, ms_pairs = 0, ms_units = 0;
   long long launches = 0;
   uint64_t salt = 0x5EED5EEDull;
+  cudaStream_t own_stream = nullptr;
+  int prepared_set = -1;  // set whose data is resident in d_vals/d_planes/d_ctot
+  bool set_all_valid = true;
 };
 
 static int fail(eddy_ctx *c, int code, const char *fmt, ...) {
@@ -127,30 +130,36 @@ int prepare_set(eddy_ctx *ctx, int set_id, SetRun &sr) {
     CK(set_divisor_map(dmap));
     ctx->lg_ready = true;
   }
-  std::vector<int8_t> vals((size_t)g * n);
+  const bool resident = (ctx->prepared_set == set_id);
+  std::vector<int8_t> vals(resident ? 0 : (size_t)g * n);
   bool all_valid = true;
-  for (int i = 0; i < g; i++) {
+  for (int i = 0; i < g && !resident; i++) {
     const int8_t *src = ctx->data.data() + (size_t)S.genes[i] * n;
     memcpy(vals.data() + (size_t)i * n, src, n);
     for (int s = 0; s < n; s++)
       if (src[s] < -1 || src[s] > 1) all_valid = false;
   }
   std::vector<uint8_t> pbits(c > 0 ? c : 1, 0);
-  if (!S.prior.empty()) {
+  if (!S.prior.empty() && !resident) {
     int p = 0;
     for (int r = 1; r < g; r++)
       for (int col = 0; col < r; col++, p++) pbits[p] = S.prior[(size_t)r * g + col] == 1 ? 1 : 0;
   }
-  CK(ctx->d_vals.ensure(vals.size() + 16));
-  CK(ctx->d_planes.ensure(sizeof(uint64_t) * (size_t)g * 3 * W));
-  CK(ctx->d_valid.ensure(sizeof(uint64_t) * W));
-  CK(ctx->d_ctot.ensure(sizeof(uint16_t) * 9 * (size_t)(c > 0 ? c : 1)));
-  CK(ctx->d_prior.ensure(pbits.size()));
-  CK(cudaMemcpyAsync(ctx->d_vals.p, vals.data(), vals.size(), cudaMemcpyHostToDevice, ctx->stream));
-  CK(cudaMemcpyAsync(ctx->d_prior.p, pbits.data(), pbits.size(), cudaMemcpyHostToDevice, ctx->stream));
-  CK(launch_prep(ctx->d_vals.as<int8_t>(), g, n, W, c, ctx->d_planes.as<uint64_t>(),
-                 ctx->d_valid.as<uint64_t>(), ctx->d_ctot.as<uint16_t>(), ctx->stream));
-  ctx->launches += 1 + (c > 0);
+  if (!resident) {
+    ctx->prepared_set = -1;
+    CK(ctx->d_vals.ensure(vals.size() + 16));
+    CK(ctx->d_planes.ensure(sizeof(uint64_t) * (size_t)g * 3 * W));
+    CK(ctx->d_valid.ensure(sizeof(uint64_t) * W));
+    CK(ctx->d_ctot.ensure(sizeof(uint16_t) * 9 * (size_t)(c > 0 ? c : 1)));
+    CK(ctx->d_prior.ensure(pbits.size()));
+    CK(cudaMemcpyAsync(ctx->d_vals.p, vals.data(), vals.size(), cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(ctx->d_prior.p, pbits.data(), pbits.size(), cudaMemcpyHostToDevice, ctx->stream));
+    CK(launch_prep(ctx->d_vals.as<int8_t>(), g, n, W, c, ctx->d_planes.as<uint64_t>(),
+                   ctx->d_valid.as<uint64_t>(), ctx->d_ctot.as<uint16_t>(), ctx->stream));
+    ctx->launches += 1 + (c > 0);
+    ctx->set_all_valid = all_valid;
+    ctx->prepared_set = set_id;
+  }
   SetDev &sd = sr.sd;
   sd = SetDev{};
   sd.g = g;
@@ -166,7 +175,7 @@ int prepare_set(eddy_ctx *ctx, int set_id, SetRun &sr) {
   sd.alpha_edge = ctx->o.alpha_edge;
   sd.alpha_edge_prior = ctx->o.alpha_edge_prior;
   sd.exact_all = compute_thresholds(sd.alpha_edge, sd.alpha_edge_prior, g, sd.bonf, sd.thr) ? 1 : 0;
-  sd.all_valid = all_valid ? 1 : 0;
+  sd.all_valid = ctx->set_all_valid ? 1 : 0;
   sd.planes = ctx->d_planes.as<uint64_t>();
   sd.valid = ctx->d_valid.as<uint64_t>();
   sd.vals = ctx->d_vals.as<int8_t>();
@@ -418,10 +427,12 @@ int eddy_ctx_create(const eddy_opts *opts, eddy_ctx **out) {
     delete ctx;
     return EDDY_ERR_CUDA;
   }
-  if (cudaSetDevice(opts->device) != cudaSuccess || cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess) {
+  if (cudaSetDevice(opts->device) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&ctx->own_stream, cudaStreamNonBlocking) != cudaSuccess) {
     delete ctx;
     return EDDY_ERR_CUDA;
   }
+  ctx->stream = ctx->own_stream;
   for (auto &ev : ctx->ev) cudaEventCreate(&ev);
   *out = ctx;
   return EDDY_OK;
@@ -439,7 +450,7 @@ int eddy_ctx_destroy(eddy_ctx *ctx) {
   for (DevBuf *b : bufs) b->release();
   for (auto &ev : ctx->ev)
     if (ev) cudaEventDestroy(ev);
-  if (ctx->stream) cudaStreamDestroy(ctx->stream);
+  if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
   delete ctx;
   return EDDY_OK;
 }
@@ -466,6 +477,7 @@ int eddy_load_matrix(eddy_ctx *ctx, const int8_t *data, int genes, int samples,
   ctx->data.assign(data, data + (size_t)genes * samples);
   ctx->labels0.assign(class_of_sample, class_of_sample + samples);
   ctx->lg_ready = false;
+  ctx->prepared_set = -1;
   std::vector<uint64_t> m0(ctx->W);
   labels_to_mask(ctx->labels0.data(), samples, ctx->W, m0.data());
   CK(cudaSetDevice(ctx->o.device));
@@ -755,6 +767,76 @@ int eddy_debug_unit(eddy_ctx *ctx, int set_id, const uint8_t *labels, int mpk, i
   }
   if (dist) memcpy(dist, K.dist.data(), 16 * (size_t)S);
   if (lval) memcpy(lval, K.lval.data(), 16 * (size_t)S);
+  return EDDY_OK;
+}
+
+int eddy_run_permutations(eddy_ctx *ctx, int set_id, int first, int count, double *js,
+                          int32_t *unique) {
+  if (!ctx) return EDDY_ERR_ARG;
+  if (set_id < 0 || set_id >= (int)ctx->sets.size() || first < 0 || count < 1 || !js || !unique)
+    return fail(ctx, EDDY_ERR_ARG, "bad arguments");
+  if (ctx->o.rng == EDDY_RNG_GLIBC)
+    return fail(ctx, EDDY_ERR_STATE, "the GLIBC stream is sequential: use eddy_run");
+  SetHost &S = ctx->sets[set_id];
+  const int n = ctx->samples, W = ctx->W;
+  ctx->ms_total = ctx->ms_pairs = ctx->ms_units = 0;
+  ctx->launches = 0;
+  if (S.genes.size() < 2) {
+    for (int i = 0; i < count; i++) {
+      js[i] = NAN;
+      unique[i] = 1;
+    }
+    return EDDY_OK;
+  }
+  SetRun sr;
+  int rc = prepare_set(ctx, set_id, sr);
+  if (rc) return rc;
+  std::vector<int32_t> perms(count);
+  for (int i = 0; i < count; i++) perms[i] = first + i;
+  if (ctx->o.rng == EDDY_RNG_COUNTER && n <= 4096)
+    return run_units(ctx, sr, count, nullptr, perms.data(), js, unique, nullptr, 1);
+  std::vector<uint64_t> mh((size_t)count * W);
+  std::vector<uint8_t> cur(n);
+  for (int i = 0; i < count; i++) {
+    const int it = first + i;
+    if (ctx->o.rng == EDDY_RNG_COUNTER) {
+      if (it == 0) memcpy(cur.data(), ctx->labels0.data(), n);
+      else counter_labels(ctx->o.seed, set_id, it, n, ctx->nA, cur.data());
+    } else {
+      if (it >= S.R_ext) return fail(ctx, EDDY_ERR_ARG, "iteration %d has no labelling", it);
+      memcpy(cur.data(), S.labels.data() + (size_t)it * n, n);
+    }
+    labels_to_mask(cur.data(), n, W, mh.data() + (size_t)i * W);
+  }
+  return run_units(ctx, sr, count, mh.data(), nullptr, js, unique, nullptr, 1);
+}
+
+int eddy_set_stream(eddy_ctx *ctx, void *stream) {
+  if (!ctx) return EDDY_ERR_ARG;
+  cudaStream_t st = stream ? (cudaStream_t)stream : ctx->own_stream;
+  if (st != ctx->stream) CK(cudaStreamSynchronize(ctx->stream));
+  ctx->stream = st;
+  return EDDY_OK;
+}
+
+int eddy_clear_sets(eddy_ctx *ctx) {
+  if (!ctx) return EDDY_ERR_ARG;
+  ctx->sets.clear();
+  ctx->prepared_set = -1;
+  return EDDY_OK;
+}
+
+int eddy_device_info(int device, char *name, int name_len, int *sms, int *cc_major,
+                     int *cc_minor) {
+  cudaDeviceProp p;
+  if (cudaGetDeviceProperties(&p, device) != cudaSuccess) return EDDY_ERR_CUDA;
+  if (name && name_len > 0) {
+    strncpy(name, p.name, name_len - 1);
+    name[name_len - 1] = 0;
+  }
+  if (sms) *sms = p.multiProcessorCount;
+  if (cc_major) *cc_major = p.major;
+  if (cc_minor) *cc_minor = p.minor;
   return EDDY_OK;
 }
 

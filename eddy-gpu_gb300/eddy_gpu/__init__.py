@@ -26,7 +26,9 @@ ERRORS = {1: "EDDY_ERR_ARG", 2: "EDDY_ERR_CUDA", 3: "EDDY_ERR_STATE",
 EXPORTS = ["eddy_ctx_create", "eddy_ctx_destroy", "eddy_last_error", "eddy_load_matrix",
            "eddy_add_set", "eddy_set_labellings", "eddy_run", "eddy_get_set_summary",
            "eddy_get_js", "eddy_get_networks", "eddy_get_edge_list", "eddy_run_labellings",
-           "eddy_debug_edges", "eddy_debug_unit", "eddy_last_timing"]
+           "eddy_debug_edges", "eddy_debug_unit", "eddy_run_permutations",
+           "eddy_set_stream", "eddy_clear_sets", "eddy_write_networks", "eddy_write_bdeu",
+           "eddy_write_edge_list", "eddy_device_info", "eddy_last_timing"]
 
 
 class Opts(C.Structure):
@@ -77,10 +79,59 @@ def library(path: str | None = None):
     L.eddy_debug_edges.argtypes = [vp, C.c_int, vp, vp]
     L.eddy_debug_unit.argtypes = [vp, C.c_int, vp, C.c_int, C.POINTER(C.c_int),
                                   C.POINTER(C.c_double), vp, vp, vp, vp, vp]
+    L.eddy_run_permutations.argtypes = [vp, C.c_int, C.c_int, C.c_int, vp, vp]
+    L.eddy_set_stream.argtypes = [vp, vp]
+    L.eddy_clear_sets.argtypes = [vp]
+    cp = C.c_char_p
+    L.eddy_write_networks.argtypes = [cp, cp, cp, cp, C.c_int, vp, vp, C.c_int, vp, vp, C.c_int,
+                                      vp]
+    L.eddy_write_bdeu.argtypes = [cp, cp, cp, cp, cp, cp, C.c_int, vp]
+    L.eddy_write_edge_list.argtypes = [cp, vp, C.c_int, vp, vp, vp, vp, cp, cp]
     L.eddy_last_timing.argtypes = [vp, C.POINTER(C.c_double), C.POINTER(C.c_double),
                                    C.POINTER(C.c_double), C.POINTER(C.c_longlong)]
     _lib = L
     return L
+
+
+def write_networks(path, input_name, class_name, set_name, net: dict, genes):
+    """<set>_Networks.txt from eddy_get_networks() output (routines.cu:240-306)."""
+    L = library()
+    g = len(genes)
+    names = (C.c_char_p * g)(*[s.encode() for s in genes])
+    epn = np.ascontiguousarray(net["epn"], np.int32)
+    nodes = np.ascontiguousarray(net["nodes"], np.int32).ravel()
+    edges = np.ascontiguousarray(net["edges"], np.int32)
+    ids = np.ascontiguousarray(net["ids"], np.int32)
+    U = int(net["U"])
+    rc = L.eddy_write_networks(path.encode(), input_name.encode(), class_name.encode(),
+                               set_name.encode(), U, _p(epn), names, g, _p(nodes), _p(edges),
+                               int(epn[U]), _p(ids))
+    if rc:
+        raise EddyError(f"eddy_write_networks failed ({rc})")
+
+
+def write_bdeu(path, input_name, class_name, set_name, class1, class2, lval):
+    L = library()
+    lv = np.ascontiguousarray(lval, np.float64).ravel()
+    rc = L.eddy_write_bdeu(path.encode(), input_name.encode(), class_name.encode(),
+                           set_name.encode(), class1.encode(), class2.encode(), lv.size // 2,
+                           _p(lv))
+    if rc:
+        raise EddyError(f"eddy_write_bdeu failed ({rc})")
+
+
+def write_edge_list(path, genes, el: dict, prior, class1, class2):
+    L = library()
+    g = len(genes)
+    names = (C.c_char_p * g)(*[s.encode() for s in genes])
+    nodes = np.ascontiguousarray(el["nodes"], np.int32).ravel()
+    edges = np.ascontiguousarray(el["edges"], np.int32)
+    epn = np.ascontiguousarray(el["epn"], np.int32)
+    pr = None if prior is None else np.ascontiguousarray(prior, np.uint8)
+    rc = L.eddy_write_edge_list(path.encode(), names, g, _p(nodes), _p(edges), _p(epn), _p(pr),
+                                class1.encode(), class2.encode())
+    if rc:
+        raise EddyError(f"eddy_write_edge_list failed ({rc})")
 
 
 def _p(a):
@@ -217,6 +268,20 @@ class Context:
         u = U.value
         return dict(U=u, js=js.value, ids=ids[:u], counts=cnt[:u], parents=par[:u],
                     dist=dist[:, :u], lval=lval[:, :u])
+
+    def run_permutations(self, set_id, first, count):
+        js = np.zeros(count, np.float64)
+        U = np.zeros(count, np.int32)
+        self._ck(self.L.eddy_run_permutations(self.h, set_id, int(first), int(count), _p(js),
+                                              _p(U)))
+        return js, U
+
+    def set_stream(self, stream_handle: int | None):
+        self._ck(self.L.eddy_set_stream(self.h, C.c_void_p(stream_handle or 0)))
+
+    def clear_sets(self):
+        self._ck(self.L.eddy_clear_sets(self.h))
+        self.g = {}
 
     def timing(self) -> dict:
         a, b, c = C.c_double(), C.c_double(), C.c_double()

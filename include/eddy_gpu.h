@@ -142,6 +142,45 @@ int eddy_debug_unit(eddy_ctx *ctx, int set_id, const uint8_t *labels, int mpk, i
                     double *js, int32_t *ids, int32_t *counts, int32_t *parents, double *dist,
                     double *lval);
 
+/* Batched hot path: iterations [first, first+count) of a set under the
+ * COUNTER stream (labellings generated on the device) or the EXTERNAL
+ * labellings; the set's data stays resident between calls.  js[count],
+ * unique[count].  The GLIBC stream is sequential and only runs in eddy_run. */
+int eddy_run_permutations(eddy_ctx *ctx, int set_id, int first, int count, double *js,
+                          int32_t *unique);
+
+/* Use the caller's CUDA stream (a cudaStream_t on the context's device) for
+ * every copy and kernel; NULL returns to the context's own stream. */
+int eddy_set_stream(eddy_ctx *ctx, void *stream);
+
+/* Drops every gene set and its results (the matrix stays loaded). */
+int eddy_clear_sets(eddy_ctx *ctx);
+
+/* ------------------------------------------------------------ output files
+ * The reference's per-set files, byte for byte (routines.cu:217-492).
+ * genes: g NUL-terminated names of the set's (adjusted) genes. */
+/* <set>_Networks.txt: the iteration-0 unique networks (writeNetworkFile,
+ * routines.cu:240-306); epn/nodes/edges/ids as eddy_get_networks returns. */
+int eddy_write_networks(const char *path, const char *input, const char *cls, const char *set,
+                        int U, const int32_t *epn, const char *const *genes, int g,
+                        const int32_t *nodes, const int32_t *edges, int total_edges,
+                        const int32_t *ids);
+/* <set>_BDEU_SCORES.txt: the normalised likelihoods (writeBdeuScores,
+ * routines.cu:217-238); lval[2*U]. */
+int eddy_write_bdeu(const char *path, const char *input, const char *cls, const char *set,
+                    const char *class1, const char *class2, int U, const double *lval);
+/* <set>_EdgeList.txt: class / Both / Neither-PRIOR edges of the uncapped
+ * full-data networks (writeEdgeListFile, routines.cu:308-492); nodes[2*g],
+ * edges, epn[3] as eddy_get_edge_list returns; prior g x g or NULL. */
+int eddy_write_edge_list(const char *path, const char *const *genes, int g, const int32_t *nodes,
+                         const int32_t *edges, const int32_t *epn, const uint8_t *prior,
+                         const char *class1, const char *class2);
+
+/* Name, SM count and compute capability of a device (the reference's
+ * device banner, main.cu:28-56, without the fields CUDA 13 removed). */
+int eddy_device_info(int device, char *name, int name_len, int *sms, int *cc_major,
+                     int *cc_minor);
+
 /* Timing of the last eddy_run / eddy_run_labellings, device side (CUDA
  * events around the kernels) in milliseconds, and the number of kernel
  * launches it made. */
