@@ -4,6 +4,7 @@
 #include <math.h>
 #include <stdarg.h>
 #include <stdio.h>
+#include <stdlib.h>
 #include <string.h>
 
 #include <algorithm>
@@ -14,6 +15,7 @@
 #include "eddy_host.h"
 #include "eddy_internal.h"
 #include "eddy_kernels.h"
+#include "eddy_mma.h"
 
 using namespace eddy;
 
@@ -75,9 +77,11 @@ struct eddy_ctx {
   std::vector<uint8_t> seen;
   std::vector<int> order;
   // device data
-  DevBuf d_lg, d_vals, d_planes, d_valid, d_ctot, d_prior, d_mask0;
+  DevBuf d_lg, d_vals, d_valsT, d_planes, d_valid, d_ctot, d_prior, d_mask0;
   DevBuf d_masks, d_dmask, d_scratch, d_js, d_U, d_status, d_keep, d_uset, d_uperm;
   DevBuf d_oids, d_ocnt, d_opar, d_odist, d_olval, d_orows, d_stats;
+  DevBuf d_Y, d_afp8, d_err;  // tensor-core contingency operands
+  int sms = 148;
   int lg_shift = 0;
   bool lg_ready = false;
   // timing of the last run
@@ -87,6 +91,7 @@ struct eddy_ctx {
   cudaStream_t own_stream = nullptr;
   int prepared_set = -1;  // set whose data is resident in d_vals/d_planes/d_ctot
   bool set_all_valid = true;
+  bool y_ready = false;
 };
 
 static int fail(eddy_ctx *c, int code, const char *fmt, ...) {
@@ -148,6 +153,7 @@ int prepare_set(eddy_ctx *ctx, int set_id, SetRun &sr) {
   if (!resident) {
     ctx->prepared_set = -1;
     CK(ctx->d_vals.ensure(vals.size() + 16));
+    CK(ctx->d_valsT.ensure(vals.size() + 16));
     CK(ctx->d_planes.ensure(sizeof(uint64_t) * (size_t)g * 3 * W));
     CK(ctx->d_valid.ensure(sizeof(uint64_t) * W));
     CK(ctx->d_ctot.ensure(sizeof(uint16_t) * 9 * (size_t)(c > 0 ? c : 1)));
@@ -155,10 +161,12 @@ int prepare_set(eddy_ctx *ctx, int set_id, SetRun &sr) {
     CK(cudaMemcpyAsync(ctx->d_vals.p, vals.data(), vals.size(), cudaMemcpyHostToDevice, ctx->stream));
     CK(cudaMemcpyAsync(ctx->d_prior.p, pbits.data(), pbits.size(), cudaMemcpyHostToDevice, ctx->stream));
     CK(launch_prep(ctx->d_vals.as<int8_t>(), g, n, W, c, ctx->d_planes.as<uint64_t>(),
-                   ctx->d_valid.as<uint64_t>(), ctx->d_ctot.as<uint16_t>(), ctx->stream));
-    ctx->launches += 1 + (c > 0);
+                   ctx->d_valid.as<uint64_t>(), ctx->d_ctot.as<uint16_t>(),
+                   ctx->d_valsT.as<int8_t>(), ctx->stream));
+    ctx->launches += 2 + (c > 0);
     ctx->set_all_valid = all_valid;
     ctx->prepared_set = set_id;
+    ctx->y_ready = false;
   }
   SetDev &sd = sr.sd;
   sd = SetDev{};
@@ -179,6 +187,7 @@ int prepare_set(eddy_ctx *ctx, int set_id, SetRun &sr) {
   sd.planes = ctx->d_planes.as<uint64_t>();
   sd.valid = ctx->d_valid.as<uint64_t>();
   sd.vals = ctx->d_vals.as<int8_t>();
+  sd.valsT = ctx->d_valsT.as<int8_t>();
   sd.ctot = ctx->d_ctot.as<uint16_t>();
   sd.prior = ctx->d_prior.as<uint8_t>();
   sd.lg = ctx->d_lg.as<int64_t>();
@@ -203,6 +212,45 @@ struct KeepOut {
   std::vector<uint32_t> rows;
   int mpk = 0;
 };
+
+// Contingency + decision kernel of a batch: the tcgen05 GEMM path unless
+// EDDY_PAIRS_KERNEL=popc selects the popcount kernel.
+bool use_popc() {
+  const char *e = getenv("EDDY_PAIRS_KERNEL");
+  return e && strcmp(e, "popc") == 0;
+}
+
+int launch_pairs_any(eddy_ctx *ctx, const SetDev &sd, const uint64_t *masks, int B, uint32_t *dmask,
+                     unsigned long long *stats) {
+  if (sd.c == 0) return EDDY_OK;
+  if (use_popc()) {
+    CK(launch_pairs(sd, masks, dmask, B, stats, ctx->stream));
+    ctx->launches += 1;
+    return EDDY_OK;
+  }
+  if (!ctx->y_ready) {
+    CK(ctx->d_Y.ensure(mma_y_bytes(sd.c, sd.n)));
+    CK(launch_build_y(sd, ctx->d_Y.as<uint8_t>(), ctx->stream));
+    ctx->launches += 1;
+    ctx->y_ready = true;
+  }
+  CK(ctx->d_afp8.ensure((size_t)mma_bpad(B) * mma_npad(sd.n)));
+  CK(ctx->d_err.ensure(sizeof(unsigned)));
+  CK(cudaMemsetAsync(ctx->d_err.p, 0, sizeof(unsigned), ctx->stream));
+  CK(launch_pairs_mma(sd, masks, B, ctx->d_afp8.as<uint8_t>(), ctx->d_Y.as<uint8_t>(), dmask, stats,
+                      ctx->d_err.as<unsigned>(), ctx->sms, ctx->stream));
+  ctx->launches += 2;
+  return EDDY_OK;
+}
+
+int check_mma_error(eddy_ctx *ctx) {
+  if (use_popc() || ctx->d_err.p == nullptr) return EDDY_OK;
+  unsigned e = 0;
+  CK(cudaMemcpyAsync(&e, ctx->d_err.p, sizeof e, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  if (e) return fail(ctx, EDDY_ERR_INTERNAL, "tensor-core pipeline wait timed out");
+  return EDDY_OK;
+}
 
 // Runs units of one set.  masks_host: B x W host masks, or null to
 // generate counter-mode masks for perms[] on the device.
@@ -289,11 +337,14 @@ int run_units(eddy_ctx *ctx, SetRun &sr, int nunits, const uint64_t *masks_host,
       bd.out_rows = ctx->d_orows.as<uint32_t>();
       bd.stats = ctx->d_stats.as<unsigned long long>();
       CK(cudaEventRecord(ctx->ev[0], ctx->stream));
-      CK(launch_pairs(sd, bd.masks, ctx->d_dmask.as<uint32_t>(), Bt, bd.stats, ctx->stream));
+      {
+        int rc = launch_pairs_any(ctx, sd, bd.masks, Bt, ctx->d_dmask.as<uint32_t>(), bd.stats);
+        if (rc) return rc;
+      }
       CK(cudaEventRecord(ctx->ev[1], ctx->stream));
       CK(launch_units(sd, bd, ctx->stream));
       CK(cudaEventRecord(ctx->ev[2], ctx->stream));
-      ctx->launches += 2;
+      ctx->launches += 1;
       std::vector<double> jsb(Bt);
       std::vector<int32_t> Ub(Bt);
       status.assign(Bt, 0);
@@ -301,6 +352,10 @@ int run_units(eddy_ctx *ctx, SetRun &sr, int nunits, const uint64_t *masks_host,
       CK(cudaMemcpyAsync(Ub.data(), ctx->d_U.p, 4 * Bt, cudaMemcpyDeviceToHost, ctx->stream));
       CK(cudaMemcpyAsync(status.data(), ctx->d_status.p, 4 * Bt, cudaMemcpyDeviceToHost, ctx->stream));
       CK(cudaStreamSynchronize(ctx->stream));
+      {
+        int rc = check_mma_error(ctx);
+        if (rc) return rc;
+      }
       float a = 0, bms = 0;
       cudaEventElapsedTime(&a, ctx->ev[0], ctx->ev[1]);
       cudaEventElapsedTime(&bms, ctx->ev[1], ctx->ev[2]);
@@ -434,6 +489,7 @@ int eddy_ctx_create(const eddy_opts *opts, eddy_ctx **out) {
   }
   ctx->stream = ctx->own_stream;
   for (auto &ev : ctx->ev) cudaEventCreate(&ev);
+  cudaDeviceGetAttribute(&ctx->sms, cudaDevAttrMultiProcessorCount, opts->device);
   *out = ctx;
   return EDDY_OK;
 }
@@ -442,11 +498,12 @@ int eddy_ctx_destroy(eddy_ctx *ctx) {
   if (!ctx) return EDDY_ERR_ARG;
   cudaSetDevice(ctx->o.device);
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
-  DevBuf *bufs[] = {&ctx->d_lg, &ctx->d_vals, &ctx->d_planes, &ctx->d_valid, &ctx->d_ctot,
+  DevBuf *bufs[] = {&ctx->d_lg, &ctx->d_vals, &ctx->d_valsT, &ctx->d_planes, &ctx->d_valid, &ctx->d_ctot,
                     &ctx->d_prior, &ctx->d_mask0, &ctx->d_masks, &ctx->d_dmask, &ctx->d_scratch,
                     &ctx->d_js, &ctx->d_U, &ctx->d_status, &ctx->d_keep, &ctx->d_uset,
                     &ctx->d_uperm, &ctx->d_oids, &ctx->d_ocnt, &ctx->d_opar, &ctx->d_odist,
-                    &ctx->d_olval, &ctx->d_orows, &ctx->d_stats};
+                    &ctx->d_olval, &ctx->d_orows, &ctx->d_stats, &ctx->d_Y, &ctx->d_afp8,
+                    &ctx->d_err};
   for (DevBuf *b : bufs) b->release();
   for (auto &ev : ctx->ev)
     if (ev) cudaEventDestroy(ev);
@@ -707,7 +764,10 @@ int eddy_debug_edges(eddy_ctx *ctx, int set_id, const uint8_t *labels, uint8_t *
   CK(ctx->d_masks.ensure(8 * W));
   CK(ctx->d_dmask.ensure(4 * (size_t)(c > 0 ? c : 1)));
   CK(cudaMemcpyAsync(ctx->d_masks.p, m.data(), 8 * W, cudaMemcpyHostToDevice, ctx->stream));
-  CK(launch_pairs(sd, ctx->d_masks.as<uint64_t>(), ctx->d_dmask.as<uint32_t>(), 1, nullptr, ctx->stream));
+  rc = launch_pairs_any(ctx, sd, ctx->d_masks.as<uint64_t>(), 1, ctx->d_dmask.as<uint32_t>(), nullptr);
+  if (rc) return rc;
+  rc = check_mma_error(ctx);
+  if (rc) return rc;
   std::vector<uint32_t> dm(c);
   CK(cudaMemcpyAsync(dm.data(), ctx->d_dmask.p, 4 * (size_t)c, cudaMemcpyDeviceToHost, ctx->stream));
   CK(cudaStreamSynchronize(ctx->stream));

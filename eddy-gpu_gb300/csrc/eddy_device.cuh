@@ -39,7 +39,7 @@ __device__ __forceinline__ void pair_rc(int p, int &row, int &col) {
 // ------------------------------------------------------------ decisions
 // Exact FP64 evaluation of one table exactly as kernel1.cu:121-203 and
 // 419-431 compute it, without FMA contraction (explicit _rn intrinsics).
-__device__ __noinline__ int exact_decision(const int *t9, int prior,
+static __device__ __noinline__ int exact_decision(const int *t9, int prior,
                                            const SetDev &sd) {
   int ex[7] = {0, 0, 0, 0, 0, 0, 0};
   for (int c = 0; c < 3; c++) {
@@ -199,7 +199,9 @@ __device__ __forceinline__ bool loo_safe(const TabInfo &ti, int prior, const Set
   } else {
     if (!((long long)(rm - 1) * (cm - 1) >= 5ll * (N - 1))) return false;
   }
-  const float emin = (float)((double)(rm - 1) * (double)(cm - 1) / (double)(N - 1));
+  // lower bound of the smallest expected count of any cell-removed table;
+  // FP32 (FP64 is the slowest pipe on this part), rounded down
+  const float emin = __fdiv_rd(__fmul_rd((float)(rm - 1), (float)(cm - 1)), (float)(N - 1));
   const float A = sqrtf(15.f / emin + 5.f / (float)(N - 1));
   const float ratio = ((float)rm / (float)(rm - 1)) * ((float)cm / (float)(cm - 1));
   const float B = fmaxf(sqrtf(ratio) - 1.f, 1.f / (float)(N - 1)) * 1.001f;
@@ -300,14 +302,14 @@ struct ListGen {
 };
 
 // ------------------------------------------------------------------ BDeu
-__device__ __constant__ int8_t c_dmap[82];
+static __device__ __constant__ int8_t c_dmap[82];
 
 // BDeu score of node t with parent set ps[0..np) over the samples of one
 // class (mask m), fixed point.  kernel5.cu:30-218: q = product of the
 // parents' observed-state counts, r = node's; score = sum over parent
 // configurations j of [-LG(q)[N_ij] + sum_k LG(q r)[N_ijk]] with
 // LG(d)[m] = lgamma(m + 4/d) - lgamma(4/d).
-__device__ int64_t bdeu_score(const SetDev &sd, int t, int np, const int *ps,
+static __device__ int64_t bdeu_score(const SetDev &sd, int t, int np, const int *ps,
                               const uint64_t *m, const uint16_t *cnt3 /*[g][3] of this class*/) {
   int nstate[4], st[4][3];
   int idx[4] = {t, np > 0 ? ps[0] : 0, np > 1 ? ps[1] : 0, np > 2 ? ps[2] : 0};

@@ -226,7 +226,7 @@ bool beta_pddn(const double *js, int R, double &alpha, double &beta, double &pdd
 }
 
 // ------------------------------------------------------------ BDeu table
-void bdeu_table(int n, std::vector<int64_t> &lg, int &shift, int8_t dmap[82]) {
+void bdeu_table_into(int n, int64_t *lg, int &shift, int8_t dmap[82]) {
   static const int D[kDivisors] = {1, 2, 3, 4, 6, 8, 9, 12, 16, 18, 24, 27, 36, 54, 81};
   memset(dmap, -1, 82);
   for (int i = 0; i < kDivisors; i++) dmap[D[i]] = (int8_t)i;
@@ -235,13 +235,17 @@ void bdeu_table(int n, std::vector<int64_t> &lg, int &shift, int8_t dmap[82]) {
   shift = (int)floor(log2(4.0e18 / bound));
   if (shift > 44) shift = 44;
   const long double scale = ldexpl(1.0L, shift);
-  lg.assign((size_t)kDivisors * (n + 1), 0);
   for (int i = 0; i < kDivisors; i++) {
     const long double a = 4.0L / (long double)D[i];
     const long double la = lgammal(a);
     for (int m = 0; m <= n; m++)
       lg[(size_t)i * (n + 1) + m] = (int64_t)llroundl((lgammal((long double)m + a) - la) * scale);
   }
+}
+
+void bdeu_table(int n, std::vector<int64_t> &lg, int &shift, int8_t dmap[82]) {
+  lg.assign((size_t)kDivisors * (n + 1), 0);
+  bdeu_table_into(n, lg.data(), shift, dmap);
 }
 
 }  // namespace eddy

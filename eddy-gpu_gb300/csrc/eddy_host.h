@@ -56,5 +56,7 @@ bool beta_pddn(const double *js, int R, double &alpha, double &beta, double &pdd
 
 // Fixed-point BDeu table lg[d][m] = (lgamma(m + 4/d) - lgamma(4/d)) * 2^shift.
 void bdeu_table(int n, std::vector<int64_t> &lg, int &shift, int8_t dmap[82]);
+// The same into a caller array of kDivisors * (n + 1) entries (no allocation).
+void bdeu_table_into(int n, int64_t *lg, int &shift, int8_t dmap[82]);
 
 }  // namespace eddy

@@ -43,6 +43,7 @@ struct SetDev {
   const uint64_t *planes; // [g][3][W]  bit s of plane (i, a) = (x_i(s) == a-1)
   const uint64_t *valid;  // [W] all-sample mask
   const int8_t *vals;     // [g][n]  -1/0/1, 2 = any other value
+  const int8_t *valsT;    // [n][g]  the same, sample-major
   const uint16_t *ctot;   // [c][9]  permutation-invariant full-sample table
   const uint8_t *prior;   // [c]     prior bit of pair p
   const int64_t *lg;      // [kDivisors][n+1] fixed-point lgamma(m+4/d)-lgamma(4/d)

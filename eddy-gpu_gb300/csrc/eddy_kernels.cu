@@ -50,6 +50,13 @@ __global__ void k_planes(const int8_t *vals, int g, int n, int W, uint64_t *plan
   if (i == 0) valid[w] = v;
 }
 
+__global__ void k_transpose(const int8_t *vals, int g, int n, int8_t *valsT) {
+  int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= g * n) return;
+  int s = idx / g, i = idx % g;
+  valsT[idx] = vals[(size_t)i * n + s];
+}
+
 __global__ void k_ctot(const uint64_t *planes, int g, int W, int c, uint16_t *ctot) {
   int p = blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= c) return;
@@ -181,7 +188,7 @@ __global__ void __launch_bounds__(128) k_pairs(SetDev sd, const uint64_t *masks,
 
 // ------------------------------------------------------------ k_units
 struct UnitLayout {
-  size_t phi[2], pcol[2], rec, htk, htv, dist, uid, urep, total;
+  size_t phi[2], pcol[2], rec, htk, htv, dist, uid, urep, sig, total;
   int HT, rec_words;  // rec_words: 64-bit words per network record
 };
 
@@ -210,6 +217,8 @@ __host__ __device__ inline UnitLayout unit_layout(int c, int S, int kmax) {
   L.uid = o;
   o = al(o + sizeof(int32_t) * (size_t)S);
   L.urep = o;
+  o = al(o + sizeof(int32_t) * (size_t)S);
+  L.sig = o;  // class-1 samples then class-2 samples, in index order
   o = al(o + sizeof(int32_t) * (size_t)S);
   L.total = o;
   return L;
@@ -242,25 +251,13 @@ __device__ __forceinline__ int block_scan(int v, int &total, int *sbuf) {
   return excl;
 }
 
-// k-th (0-based) set bit of mask words (pc = exclusive popcount prefix).
-__device__ __forceinline__ int select_bit(const uint64_t *m, const int *pc, int W, int k) {
-  int lo = 0, hi = W - 1;
-  while (lo < hi) {  // last word with pc[w] <= k
-    int mid = (lo + hi + 1) >> 1;
-    if (pc[mid] <= k) lo = mid; else hi = mid - 1;
-  }
-  uint64_t x = m[lo];
-  int r = k - pc[lo];
-  for (int i = 0; i < r; i++) x &= x - 1;
-  return lo * 64 + (__ffsll((long long)x) - 1);
-}
-
 struct UnitSmem {
   // fixed part; variable arrays follow in dynamic shared memory
   unsigned long long HF[2];
   long long base[2][2];  // [data class][full network of class]
   int nphi[2];
   int ndab;
+  int nrphi[2];
   int scan[32];
   unsigned status;
   int U;
@@ -280,6 +277,7 @@ struct UnitPtrs {
   unsigned long long *fh; // [2][g] node hash of full networks
   int *phs, *phe;         // [2][g] flip-entry range per row
   uint16_t *dab;          // [g] nodes whose full lists differ between classes
+  uint16_t *rphi;         // [2][g] rows that hold flip entries, per class
   int8_t *stsig;          // [nwarps][g] states at sigma
   unsigned long long *mkey;  // [kMemo]
   long long *mval;           // [kMemo][2]
@@ -298,6 +296,7 @@ __host__ __device__ inline size_t unit_smem_bytes(int g, int W, int GW, int nwar
   o = al(o) + 2 * sizeof(unsigned long long) * g;
   o = al(o) + 4 * sizeof(int) * g;
   o = al(o) + sizeof(uint16_t) * g;
+  o = al(o) + 2 * sizeof(uint16_t) * g;
   o = al(o) + (size_t)nwarps * g;
   o = al(o) + sizeof(unsigned long long) * kMemo;
   o = al(o) + 2 * sizeof(long long) * kMemo;
@@ -320,6 +319,7 @@ __device__ inline UnitPtrs carve(char *base, int g, int W, int GW, int nwarps) {
   o = al(o); P.fh = (unsigned long long *)(base + o); o += 2 * sizeof(unsigned long long) * g;
   o = al(o); P.phs = (int *)(base + o); P.phe = P.phs + 2 * g; o += 4 * sizeof(int) * g;
   o = al(o); P.dab = (uint16_t *)(base + o); o += sizeof(uint16_t) * g;
+  o = al(o); P.rphi = (uint16_t *)(base + o); o += 2 * sizeof(uint16_t) * g;
   o = al(o); P.stsig = (int8_t *)(base + o); o += (size_t)nwarps * g;
   o = al(o); P.mkey = (unsigned long long *)(base + o); o += sizeof(unsigned long long) * kMemo;
   o = al(o); P.mval = (long long *)(base + o); o += 2 * sizeof(long long) * kMemo;
@@ -329,17 +329,18 @@ __device__ inline UnitPtrs carve(char *base, int g, int W, int GW, int nwarps) {
 
 // Network s of a unit: class k (0 = class 1, 1 = class 2) and left-out
 // sample sigma (-1 for the two full networks), kernel1.cu:85-88, 412-416.
-__device__ __forceinline__ void net_of(int s, const SetDev &sd, const UnitPtrs &P, int &k, int &sigma) {
+// sig: class-1 samples then class-2 samples in index order.
+__device__ __forceinline__ void net_of(int s, const SetDev &sd, const int *sig, int &k, int &sigma) {
   if (s == 0) { k = 0; sigma = -1; return; }
   if (s == sd.S - 1) { k = 1; sigma = -1; return; }
-  if (s <= sd.nA) { k = 0; sigma = select_bit(P.mA, P.pcA, sd.W, s - 1); return; }
-  k = 1;
-  sigma = select_bit(P.mB, P.pcB, sd.W, s - sd.nA - 1);
+  // class-1 sample s-1 sits at s-1; class-2 sample s-nA-1 at nA+(s-nA-1) = s-1
+  k = (s <= sd.nA) ? 0 : 1;
+  sigma = sig[s - 1];
 }
 
 __device__ __forceinline__ void load_stsig(const SetDev &sd, int sigma, int8_t *dst, int lane) {
-  for (int i = lane; i < sd.g; i += 32)
-    dst[i] = (int8_t)(sigma >= 0 ? st_of(sd.vals[(size_t)i * sd.n + sigma]) : 3);
+  const int8_t *src = sd.valsT + (size_t)(sigma >= 0 ? sigma : 0) * sd.g;
+  for (int i = lane; i < sd.g; i += 32) dst[i] = (int8_t)(sigma >= 0 ? st_of(src[i]) : 3);
   __syncwarp();
 }
 
@@ -425,6 +426,7 @@ __global__ void __launch_bounds__(256) k_units(SetDev sd, BatchDev bd) {
   long long *dist = (long long *)(scr + L.dist);
   int *uid = (int *)(scr + L.uid);
   int *urep = (int *)(scr + L.urep);
+  int *sig = (int *)(scr + L.sig);
   const uint32_t *dm = bd.dmask + (size_t)u * c;
   const int tid = threadIdx.x, nt = blockDim.x;
 
@@ -483,53 +485,83 @@ __global__ void __launch_bounds__(256) k_units(SetDev sd, BatchDev bd) {
     }
   }
 
-  // ---- P1: full-network rows and ordered flip lists
-  for (int p0 = 0; p0 < c; p0 += nt) {
-    const int p = p0 + tid;
-    uint32_t m = (p < c) ? dm[p] : 0u;
-    int row = 0, col = 0;
-    if (p < c) {
-      pair_rc(p, row, col);
-      if (m & 1u) atomicOr(&P.rows[((size_t)0 * g + row) * GW + (col >> 5)], 1u << (col & 31));
-      if (m & (1u << 16)) atomicOr(&P.rows[((size_t)1 * g + row) * GW + (col >> 5)], 1u << (col & 31));
+  __syncthreads();
+  // sample lists of both classes in index order (network -> left-out sample)
+  for (int w = tid; w < W; w += nt) {
+    uint64_t a = P.mA[w], b = P.mB[w];
+    int ia = P.pcA[w], ib = sd.nA + P.pcB[w];
+    while (a) {
+      sig[ia++] = w * 64 + (__ffsll((long long)a) - 1);
+      a &= a - 1;
     }
-    for (int cls = 0; cls < 2; cls++) {
-      uint32_t mm = (m >> (16 * cls)) & 0x3FFu;
-      uint32_t fb = (mm >> 1) ^ ((mm & 1u) ? 0x1FFu : 0u);
-      int flag = (p < c && fb != 0u) ? 1 : 0;
-      int total;
-      int off = block_scan(flag, total, SM.scan);
-      if (flag) {
-        int idx = SM.nphi[cls] + off;
-        phi[cls][idx] = ((uint32_t)p << 9) | fb;
-        pcol[cls][idx] = (uint16_t)col;
+    while (b) {
+      sig[ib++] = w * 64 + (__ffsll((long long)b) - 1);
+      b &= b - 1;
+    }
+  }
+
+  // ---- P1: full-network rows and flip lists.  Warp w owns the rows whose
+  // pairs start in [w c/nw, (w+1) c/nw): a 32-lane chunk of a row is one row
+  // bitset word (ballot), and the row's flip entries land, in pair order, in
+  // the warp's own segment of the list (which starts at its first pair).
+  {
+    const long long p_lo = (long long)warp * c / nw, p_hi = (long long)(warp + 1) * c / nw;
+    int r0, c0;
+    pair_rc((int)(p_lo < c ? p_lo : 0), r0, c0);
+    if (c0 != 0) r0++;  // rows are owned by the warp holding their first pair
+    int r1 = g;
+    if (p_hi < c) {
+      int c1;
+      pair_rc((int)p_hi, r1, c1);
+      if (c1 != 0) r1++;
+    }
+    if (p_lo >= c) r0 = g;
+    int wpos[2];
+    wpos[0] = wpos[1] = (int)((long long)r0 * (r0 - 1) / 2);  // segment = first pair of r0
+    for (int t = r0; t < r1; t++) {
+      const int pbase = t * (t - 1) / 2;
+      if (lane == 0) {
+        P.phs[t] = wpos[0];
+        P.phs[g + t] = wpos[1];
       }
-      __syncthreads();
-      if (tid == 0) SM.nphi[cls] += total;
-      __syncthreads();
+      for (int j0 = 0; j0 < t; j0 += 32) {
+        const int j = j0 + lane;
+        const uint32_t m = (j < t) ? dm[pbase + j] : 0u;
+        const uint32_t wa = __ballot_sync(0xffffffffu, m & 1u);
+        const uint32_t wb = __ballot_sync(0xffffffffu, (m >> 16) & 1u);
+        if (lane == 0) {
+          P.rows[((size_t)0 * g + t) * GW + (j0 >> 5)] = wa;
+          P.rows[((size_t)1 * g + t) * GW + (j0 >> 5)] = wb;
+        }
+#pragma unroll
+        for (int cls = 0; cls < 2; cls++) {
+          const uint32_t mm = (m >> (16 * cls)) & 0x3FFu;
+          const uint32_t fb = (mm >> 1) ^ ((mm & 1u) ? 0x1FFu : 0u);
+          const bool flag = (j < t) && fb != 0u;
+          const uint32_t bal = __ballot_sync(0xffffffffu, flag);
+          if (flag) {
+            const int idx = wpos[cls] + __popc(bal & ((1u << lane) - 1u));
+            phi[cls][idx] = ((uint32_t)(pbase + j) << 9) | fb;
+            pcol[cls][idx] = (uint16_t)j;
+          }
+          wpos[cls] += __popc(bal);
+        }
+      }
+      if (lane == 0) {
+        P.phe[t] = wpos[0];
+        P.phe[g + t] = wpos[1];
+      }
     }
   }
   __syncthreads();
-  // flip ranges per row (entries sorted by p, rows contiguous)
-  for (int cls = 0; cls < 2; cls++) {
-    const int nphi = SM.nphi[cls];
-    for (int i = tid; i < nphi; i += nt) {
-      int r, cc;
-      pair_rc((int)(phi[cls][i] >> 9), r, cc);
-      int rp = -1;
-      if (i > 0) {
-        int r2, c2;
-        pair_rc((int)(phi[cls][i - 1] >> 9), r2, c2);
-        rp = r2;
-      }
-      if (rp != r) P.phs[cls * g + r] = i;
-      int rn = -1;
-      if (i + 1 < nphi) {
-        int r2, c2;
-        pair_rc((int)(phi[cls][i + 1] >> 9), r2, c2);
-        rn = r2;
-      }
-      if (rn != r) P.phe[cls * g + r] = i + 1;
+
+  if (tid == 0) SM.nrphi[0] = SM.nrphi[1] = 0;
+  __syncthreads();
+  for (int i = tid; i < 2 * g; i += nt) {
+    const int k = i / g, t = i % g;
+    if (P.phe[k * g + t] > P.phs[k * g + t]) {
+      int idx = atomicAdd(&SM.nrphi[k], 1);
+      P.rphi[k * g + idx] = (uint16_t)t;
     }
   }
   __syncthreads();
@@ -567,9 +599,18 @@ __global__ void __launch_bounds__(256) k_units(SetDev sd, BatchDev bd) {
   int8_t *myst = P.stsig + (size_t)warp * g;
   for (int s = warp; s < S; s += nw) {
     int k, sigma;
-    net_of(s, sd, P, k, sigma);
+    net_of(s, sd, sig, k, sigma);
     unsigned long long *R = rec + (size_t)s * L.rec_words;
     if (sigma < 0) {
+      if (lane == 0) {
+        R[0] = SM.HF[k];
+        R[1] = 0;
+      }
+      continue;
+    }
+    const int nrk = SM.nrphi[k];
+    if (nrk == 0) {
+      // no pair of this class flips for any left-out sample
       if (lane == 0) {
         R[0] = SM.HF[k];
         R[1] = 0;
@@ -579,13 +620,13 @@ __global__ void __launch_bounds__(256) k_units(SetDev sd, BatchDev bd) {
     load_stsig(sd, sigma, myst, lane);
     unsigned long long dh = 0;
     int nchg = 0;
-    for (int t0 = 0; t0 < g; t0 += 32) {
-      const int t = t0 + lane;
+    for (int t0 = 0; t0 < nrk; t0 += 32) {
+      const int t = (t0 + lane < nrk) ? (int)P.rphi[k * g + t0 + lane] : -1;
       bool changed = false;
       unsigned long long hn = 0;
       int ps[3] = {0xFFFF, 0xFFFF, 0xFFFF};
       int cnt = 0;
-      if (t < g && P.phe[k * g + t] > P.phs[k * g + t] && myst[t] <= 2) {
+      if (t >= 0 && myst[t] <= 2) {
         ListGen Gn, Go;
         gen_for(Gn, sd, P, phi[k], pcol[k], k, t, myst);
         gen_for(Go, sd, P, phi[k], pcol[k], k, t, nullptr);
@@ -685,11 +726,13 @@ __global__ void __launch_bounds__(256) k_units(SetDev sd, BatchDev bd) {
     if (code >= 0) continue;
     const int r = -1 - code;
     int ks, ss, kr, sr;
-    net_of(s, sd, P, ks, ss);
-    net_of(r, sd, P, kr, sr);
+    net_of(s, sd, sig, ks, ss);
+    net_of(r, sd, sig, kr, sr);
     const unsigned long long *Rs = rec + (size_t)s * L.rec_words;
     const unsigned long long *Rr = rec + (size_t)r * L.rec_words;
     const int ns = (int)Rs[1], nr = (int)Rr[1];
+    // both are their class's full network: equal by construction
+    if (ks == kr && ns == 0 && nr == 0) continue;
     bool ok = true;
     // states at both samples, shared by the warp
     load_stsig(sd, ss, myst, lane);
@@ -726,7 +769,8 @@ __global__ void __launch_bounds__(256) k_units(SetDev sd, BatchDev bd) {
         // list of t in r: states of sigma(r) for row t and the columns read
         // through a private lookup
         const int GWl = sd.GW;
-        const int strow_r = (sr >= 0) ? st_of(sd.vals[(size_t)t * sd.n + sr]) : 3;
+        const int8_t *rT = sd.valsT + (size_t)(sr >= 0 ? sr : 0) * sd.g;
+        const int strow_r = (sr >= 0) ? st_of(rT[t]) : 3;
         // b: manual generator with global-memory states
         const uint32_t *rowr = P.rows + ((size_t)kr * g + t) * GWl;
         int fi = P.phs[kr * g + t], fe = P.phe[kr * g + t];
@@ -738,7 +782,7 @@ __global__ void __launch_bounds__(256) k_units(SetDev sd, BatchDev bd) {
           while (fi < fe) {
             int col = pcol[kr][fi];
             if (col >= hi) break;
-            int sc = st_of(sd.vals[(size_t)col * sd.n + sr]);
+            int sc = st_of(rT[col]);
             if (sc <= 2 && ((phi[kr][fi] & 0x1FFu) >> (strow_r * 3 + sc)) & 1u) mm |= 1u << (col - 32 * ww);
             fi++;
           }
@@ -793,7 +837,7 @@ __global__ void __launch_bounds__(256) k_units(SetDev sd, BatchDev bd) {
   for (int uu = tid; uu < U; uu += nt) {
     const int s = urep[uu];
     int k, sigma;
-    net_of(s, sd, P, k, sigma);
+    net_of(s, sd, sig, k, sigma);
     const unsigned long long *R = rec + (size_t)s * L.rec_words;
     const int nchg = (int)R[1];
     long long d0 = SM.base[0][k], d1 = SM.base[1][k];
@@ -863,17 +907,12 @@ __global__ void __launch_bounds__(256) k_units(SetDev sd, BatchDev bd) {
     mean[cls] = SM.red_d[0] / (double)U;
     __syncthreads();
   }
-  // exp of the adjusted scores and their sums
+  // exp of the adjusted scores and their sums (FP64: U values per class)
   for (int cls = 0; cls < 2; cls++) {
     const double scale = 10.0 / (double)(mx[cls] - mn[cls]);  // inf when all equal
     double ls = 0.0;
-    for (int uu = tid; uu < U; uu += nt) {
-      double a = ((double)(dist[cls * S + uu] - mn[cls]) - mean[cls]) * scale;
-      float ah = (float)a;
-      float al = (float)(a - (double)ah);
-      double e = (double)expf(ah) * (1.0 + (double)al);
-      ls += e;
-    }
+    for (int uu = tid; uu < U; uu += nt)
+      ls += exp(((double)(dist[cls * S + uu] - mn[cls]) - mean[cls]) * scale);
     for (int o = 16; o > 0; o >>= 1) ls += __shfl_down_sync(0xffffffffu, ls, o);
     if (lane == 0) SM.red_d[warp] = ls;
     __syncthreads();
@@ -888,33 +927,17 @@ __global__ void __launch_bounds__(256) k_units(SetDev sd, BatchDev bd) {
   }
   {
     const double sA = 10.0 / (double)(mx[0] - mn[0]), sB = 10.0 / (double)(mx[1] - mn[1]);
-    const double iA = 1.0 / esum[0], iB = 1.0 / esum[1];
     double ls = 0.0;
     for (int uu = tid; uu < U; uu += nt) {
-      double a = ((double)(dist[uu] - mn[0]) - mean[0]) * sA;
-      double b = ((double)(dist[S + uu] - mn[1]) - mean[1]) * sB;
-      float ah = (float)a, bh = (float)b;
-      double eA = (double)expf(ah) * (1.0 + (double)(float)(a - (double)ah));
-      double eB = (double)expf(bh) * (1.0 + (double)(float)(b - (double)bh));
-      double Pu = eA * iA, Qu = eB * iB;
-      double M = 0.5 * (Pu + Qu);
-      // 1/2 P log(P/M) + 1/2 Q log(Q/M) = 1/2 M phi(delta), delta = (P-Q)/(P+Q)
-      float dl = (float)((Pu - Qu) / (Pu + Qu));
-      float ad = fabsf(dl);
-      float phi;
-      if (ad < 0.25f) {
-        float d2 = dl * dl, term = d2, acc = 0.f;
-        for (int kk = 1; kk <= 12; kk++) {
-          acc += term / (float)(kk * (2 * kk - 1));
-          term *= d2;
-        }
-        phi = acc;
-      } else if (ad >= 1.f) {
-        phi = 2.f * 0.69314718055994531f;
-      } else {
-        phi = (1.f + dl) * log1pf(dl) + (1.f - dl) * log1pf(-dl);
+      // likelihoods (main.cu:1360-1394) and the two KL terms of kool()
+      // (routines.cu:42-60): P log(P/M), Q log(Q/M), zeros skipped
+      const double Pu = exp(((double)(dist[uu] - mn[0]) - mean[0]) * sA) / esum[0];
+      const double Qu = exp(((double)(dist[S + uu] - mn[1]) - mean[1]) * sB) / esum[1];
+      const double M = (Pu + Qu) / 2;
+      if (M != 0) {
+        if (Pu != 0) ls += 0.5 * (Pu * log(Pu / M));
+        if (Qu != 0) ls += 0.5 * (Qu * log(Qu / M));
       }
-      ls += 0.5 * M * (double)phi;
       if (keep >= 0) {
         bd.out_lval[((size_t)keep * 2 + 0) * S + uu] = Pu;
         bd.out_lval[((size_t)keep * 2 + 1) * S + uu] = Qu;
@@ -926,7 +949,7 @@ __global__ void __launch_bounds__(256) k_units(SetDev sd, BatchDev bd) {
     if (tid == 0) {
       double a = 0;
       for (int w = 0; w < nw; w++) a += SM.red_d[w];
-      js = a / 0.69314718055994530942;
+      js = a / log(2.0);
       bool degenerate = (mx[0] == mn[0]) || (mx[1] == mn[1]);
       if (degenerate) js = __longlong_as_double(0x7ff8000000000000ll);
       bd.js[u] = js;
@@ -950,7 +973,7 @@ __global__ void __launch_bounds__(256) k_units(SetDev sd, BatchDev bd) {
     for (int uu = warp; uu < U; uu += nw) {
       const int s = urep[uu];
       int k, sigma;
-      net_of(s, sd, P, k, sigma);
+      net_of(s, sd, sig, k, sigma);
       load_stsig(sd, sigma, myst, lane);
       for (int t = lane; t < g; t += 32) {
         ListGen G;
@@ -971,9 +994,10 @@ __global__ void __launch_bounds__(256) k_units(SetDev sd, BatchDev bd) {
 
 // ------------------------------------------------------------ launchers
 cudaError_t launch_prep(const int8_t *vals, int g, int n, int W, int c, uint64_t *planes,
-                        uint64_t *valid, uint16_t *ctot, cudaStream_t st) {
+                        uint64_t *valid, uint16_t *ctot, int8_t *valsT, cudaStream_t st) {
   int tot = g * W;
   k_planes<<<(tot + 127) / 128, 128, 0, st>>>(vals, g, n, W, planes, valid);
+  k_transpose<<<(g * n + 255) / 256, 256, 0, st>>>(vals, g, n, valsT);
   if (c > 0) k_ctot<<<(c + 127) / 128, 128, 0, st>>>(planes, g, W, c, ctot);
   return cudaGetLastError();
 }

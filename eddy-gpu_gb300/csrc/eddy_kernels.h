@@ -10,7 +10,7 @@ namespace eddy {
 size_t unit_scratch_bytes(int c, int S, int kmax);
 size_t unit_smem_size(int g, int W, int nwarps);
 cudaError_t launch_prep(const int8_t *vals, int g, int n, int W, int c, uint64_t *planes,
-                        uint64_t *valid, uint16_t *ctot, cudaStream_t st);
+                        uint64_t *valid, uint16_t *ctot, int8_t *valsT, cudaStream_t st);
 cudaError_t launch_counter_masks(int n, int nA, int W, uint64_t seed, const int32_t *unit_set,
                                  const int32_t *unit_perm, const uint64_t *mask0, uint64_t *masks,
                                  int B, cudaStream_t st);

@@ -169,3 +169,33 @@ def test_glibc_stream_matches_reference_sampler(eddy_lib, oracle_lib):
         assert len(js) == len(ojs)
         assert np.array_equal(U, oU)
         assert js_close(js, ojs)
+
+
+@pytest.mark.parametrize("case", [CASES[2], CASES[4], CASES[5], CASES[6]],
+                         ids=["g20", "g50", "invalid", "g40prior"])
+def test_tensor_core_and_popcount_paths_agree(case, eddy_lib, monkeypatch):
+    """The tcgen05 contingency GEMM and the popcount kernel give the same
+    edge decisions for every network (bit for bit)."""
+    g, n, nA, mp, bonf, pw, npr, inv = case
+    rng = np.random.default_rng(g + 7 * n)
+    data = planted(rng, g, n, nA=nA, invalid=inv)
+    labels0 = np.concatenate([np.zeros(nA, np.uint8), np.ones(n - nA, np.uint8)])
+    pr = _prior(rng, g, npr) if npr else None
+    ctx = eddy_lib.Context(max_parents=mp, bonferroni=bonf, prior_weight=pw,
+                           rng=eddy_lib.RNG_EXTERNAL)
+    ctx.load_matrix(data, labels0)
+    sid = ctx.add_set(np.arange(g), pr)
+    for t in range(2):
+        lab = labels0 if t == 0 else make_labels(rng, n, nA)
+        monkeypatch.delenv("EDDY_PAIRS_KERNEL", raising=False)
+        a = ctx.debug_edges(sid, lab)
+        monkeypatch.setenv("EDDY_PAIRS_KERNEL", "popc")
+        b = ctx.debug_edges(sid, lab)
+        assert np.array_equal(a, b)
+    labs = np.stack([make_labels(rng, n, nA) for _ in range(300)])
+    monkeypatch.delenv("EDDY_PAIRS_KERNEL", raising=False)
+    js1, U1 = ctx.run_labellings(sid, labs)
+    monkeypatch.setenv("EDDY_PAIRS_KERNEL", "popc")
+    js2, U2 = ctx.run_labellings(sid, labs)
+    assert np.array_equal(U1, U2)
+    assert np.array_equal(js1, js2) or js_close(js1, js2)
