@@ -28,7 +28,7 @@ EXPORTS = ["eddy_ctx_create", "eddy_ctx_destroy", "eddy_last_error", "eddy_load_
            "eddy_get_js", "eddy_get_networks", "eddy_get_edge_list", "eddy_run_labellings",
            "eddy_debug_edges", "eddy_debug_unit", "eddy_run_permutations",
            "eddy_set_stream", "eddy_clear_sets", "eddy_write_networks", "eddy_write_bdeu",
-           "eddy_write_edge_list", "eddy_device_info", "eddy_last_timing"]
+           "eddy_write_edge_list", "eddy_unit_noalloc", "eddy_device_info", "eddy_last_timing"]
 
 
 class Opts(C.Structure):
@@ -82,6 +82,8 @@ def library(path: str | None = None):
     L.eddy_run_permutations.argtypes = [vp, C.c_int, C.c_int, C.c_int, vp, vp]
     L.eddy_set_stream.argtypes = [vp, vp]
     L.eddy_clear_sets.argtypes = [vp]
+    L.eddy_unit_noalloc.argtypes = [C.POINTER(Opts), vp, C.c_int, C.c_int, vp, vp, vp,
+                                     C.POINTER(C.c_double), C.POINTER(C.c_int32)]
     cp = C.c_char_p
     L.eddy_write_networks.argtypes = [cp, cp, cp, cp, C.c_int, vp, vp, C.c_int, vp, vp, C.c_int,
                                       vp]
@@ -132,6 +134,23 @@ def write_edge_list(path, genes, el: dict, prior, class1, class2):
                                 class1.encode(), class2.encode())
     if rc:
         raise EddyError(f"eddy_write_edge_list failed ({rc})")
+
+
+def unit_noalloc(opts: "Opts", data, labels, prior=None, stream=None):
+    """eddy_unit_noalloc: one labelling with no device allocation (host in,
+    host out).  Returns (js, U); raises on a non-zero status."""
+    L = library()
+    data = np.ascontiguousarray(data, np.int8)
+    labels = np.ascontiguousarray(labels, np.uint8)
+    pr = None if prior is None else np.ascontiguousarray(prior, np.uint8)
+    g, n = data.shape
+    js = C.c_double()
+    U = C.c_int32()
+    rc = L.eddy_unit_noalloc(C.byref(opts), _p(data), g, n, _p(labels), _p(pr),
+                             C.c_void_p(stream or 0), C.byref(js), C.byref(U))
+    if rc:
+        raise EddyError(f"eddy_unit_noalloc failed ({ERRORS.get(rc, rc)})")
+    return js.value, U.value
 
 
 def _p(a):

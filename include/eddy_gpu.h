@@ -176,6 +176,28 @@ int eddy_write_edge_list(const char *path, const char *const *genes, int g, cons
                          const int32_t *edges, const int32_t *epn, const uint8_t *prior,
                          const char *class1, const char *class2);
 
+/* ------------------------------------------------- no-allocation entry point
+ * No counterpart in the reference.  One labelling of one gene set (the
+ * S-network inference, BDeu, normalisation and JS of eddy_run_labellings)
+ * for callers that may not allocate GPU memory: programs embedding EDDY in a
+ * host application that owns every byte of device memory through its own
+ * pool, or pipelines that must avoid the device-wide synchronisation
+ * cudaFree can cause.  Inputs and results are HOST buffers; every
+ * intermediate lives in one fixed array (~2.6 MB) compiled into the library,
+ * held by each GPU that loads it until the process exits.  No cudaMalloc,
+ * cudaFree or allocating library call is made.
+ * Limits: 2 <= g <= 64 genes, 2 <= n <= 2048 samples (EDDY_ERR_CAPACITY
+ * beyond).  vals: g x n int8, labels: n entries 0/1 (both classes present),
+ * prior: g x g 0/1 or NULL, stream: a cudaStream_t of the current device or
+ * NULL.  *js and *unique receive the JS (NaN when U == 1) and U.
+ * The first call on a device looks up the array's device address (call it
+ * once before any stream capture).  Calls share the array: one process's
+ * calls are serialised by a lock and each call ends with a stream
+ * synchronisation; GPU work that overlaps a call from elsewhere races. */
+int eddy_unit_noalloc(const eddy_opts *opts, const int8_t *vals, int g, int n,
+                      const uint8_t *labels, const uint8_t *prior, void *stream, double *js,
+                      int32_t *unique);
+
 /* Name, SM count and compute capability of a device (the reference's
  * device banner, main.cu:28-56, without the fields CUDA 13 removed). */
 int eddy_device_info(int device, char *name, int name_len, int *sms, int *cc_major,
