@@ -133,9 +133,9 @@ def cpu_sample(w, genes, seed, first, count, threads):
     lab = oracle.counter_labels(seed, 0, w.labels, first + count)[first:first + count]
     prm = oracle.params(mp=w.flags["mp"], pw=w.flags["pw"])
     t0 = time.perf_counter()
-    oracle.units(w.data[genes], lab, None, prm, threads=threads)
+    js, U = oracle.units(w.data[genes], lab, None, prm, threads=threads)
     dt = time.perf_counter() - t0
-    return count / dt, dt
+    return count / dt, dt, js, U
 
 
 def run_reference(args, rank, world):
@@ -151,7 +151,7 @@ def run_reference(args, rank, world):
     threads = os.cpu_count() or 1
     per_step = args.cpu_units
     for i in range(args.warmup):
-        cpu_sample(w, genes, 4242, 1 + i * per_step, per_step, threads)
+        cpu_sample(w, genes, 4242, 1 + i * per_step, per_step, threads)[:2]
     t0 = time.perf_counter()
     done = 0
     for i in range(args.steps):
@@ -169,6 +169,51 @@ def run_reference(args, rank, world):
                              "sample": f"{per_step} permutations per step x {args.steps} steps"},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
+
+
+def run_multiset(args, rank, world, local):
+    """Configs 3 and 5: many gene sets of uneven size, -r permutations each,
+    every set's permutations on the device (counter stream); a sample of
+    `--sets` sets.  Prints its own JSON line."""
+    import torch
+
+    torch.cuda.set_device(local)
+    import build as _build
+    _build.build()
+    import eddy_gpu
+    from eddy_gpu import synth
+    w = synth.make(args.workload, seed=0, n_sets=args.sets)
+    R = args.perms or w.flags["r"]
+    ctx = eddy_gpu.Context(max_parents=w.flags["mp"], prior_weight=w.flags["pw"], permutations=R,
+                           rng=eddy_gpu.RNG_COUNTER, seed=77, device=local, keep_networks=False)
+    stream = torch.cuda.current_stream()
+    ctx.set_stream(stream.cuda_stream)
+    ctx.load_matrix(w.data, w.labels)
+    sids = [ctx.add_set(genes, prior) for _, genes, prior in w.sets]
+    ctx.run_permutations(sids[0], 1, R - 1)  # warm-up (also tunes the first shape)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    acc = {"ms_pairs": 0.0, "ms_units": 0.0}
+    for sid in sids:
+        ctx.run_permutations(sid, 1, R - 1)
+        t = ctx.timing()
+        acc["ms_pairs"] += t["ms_pairs"]
+        acc["ms_units"] += t["ms_units"]
+    e1.record(stream)
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
+    ms = e0.elapsed_time(e1)
+    units = len(sids) * (R - 1)
+    sizes = [len(gn) for _, gn, _ in w.sets]
+    line = {"metric": METRIC, "value": units / (ms / 1e3), "unit": UNIT, "n_gpus": 1,
+            "workload": f"config {args.workload}: {len(sids)} sets (sizes {min(sizes)}-"
+                        f"{max(sizes)}, median {int(np.median(sizes))}) x {R - 1} permutations, "
+                        f"{w.data.shape[0]} genes x {w.data.shape[1]} samples",
+            "wall_units_per_s": units / wall, "stage_ms": acc, "units": units}
+    print(json.dumps(line), flush=True)
+    ctx.close()
 
 
 def run_ours(args, rank, world, local):
@@ -221,6 +266,7 @@ def run_ours(args, rank, world, local):
         e1.record(stream)
         torch.cuda.synchronize()
     ms = e0.elapsed_time(e1)
+    stats = ctx.stats()  # decision counters of the last timed step
     if world > 1:
         dist.barrier()
         tt = torch.tensor([ms], device="cuda")
@@ -228,6 +274,28 @@ def run_ours(args, rank, world, local):
         ms = float(tt.item())
     total_units = B * args.steps * world
     value = total_units / (ms / 1e3)
+
+    # the plain FP64 form on the same GPU: every table decided by the
+    # reference's FP64 formula (no FP32 fast path, no filter); short sample
+    fp64 = None
+    if not args.no_fp64:
+        os.environ["EDDY_DECISIONS"] = "fp64"
+        ctx.clear_sets()
+        sid64 = ctx.add_set(genes)
+        Bf = max(128, B // 8)
+        ctx.run_permutations(sid64, base, Bf)  # warm-up
+        torch.cuda.synchronize()
+        f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        f0.record(stream)
+        ctx.run_permutations(sid64, base + Bf, Bf)
+        f1.record(stream)
+        torch.cuda.synchronize()
+        fms = f0.elapsed_time(f1)
+        del os.environ["EDDY_DECISIONS"]
+        ctx.clear_sets()
+        fp64 = {"value": Bf / (fms / 1e3), "unit": UNIT, "units": Bf,
+                "form": "same pipeline, every table decided in FP64 (reference formula), "
+                        "no FP32 fast path, no leave-one-out filter"}
 
     # end to end through the public API with host buffers
     data_pinned = torch.from_numpy(w.data).pin_memory().numpy()
@@ -269,25 +337,51 @@ def run_ours(args, rank, world, local):
         return
     hbm, bf16, peak_kind = load_peaks()
     bp, bu = algorithmic_bytes(g, n, mp)
+    c = g * (g - 1) // 2
     launches_per_kernel = args.steps  # one launch of each kernel per step (B units)
-    if acc["ms_pairs"] >= acc["ms_units"]:
-        kname, kms, kbytes = "k_pairs", acc["ms_pairs"], bp * B
-    else:
-        kname, kms, kbytes = "k_units", acc["ms_units"], bu * B
-    avg_ms = kms / launches_per_kernel
-    achieved = kbytes / (avg_ms / 1e3) / 1e9
-    traffic = None
-    tf = os.path.join(ROOT, "profiles", f"{kname}_traffic.json")
+    traffic_info = {}
+    tf = os.path.join(ROOT, "profiles", "traffic_config4.json")
     if os.path.exists(tf):
         with open(tf) as f:
-            tr = json.load(f)
-        traffic = tr.get("bytes_per_unit", 0) * B if tr.get("bytes_per_unit") else None
+            traffic_info = json.load(f)
+    # contingency GEMM + decisions on the tensor cores: useful GEMM work is
+    # 2 x (9 cells x c pairs) x n samples per unit (0/1 e4m3, FP32 accumulate)
+    k1_ms = acc["ms_pairs"] / launches_per_kernel
+    k1_flops = 2.0 * 9 * c * n * B
+    k1 = {"kernel": "k_pairs_mma", "bound": "tensor", "achieved": k1_flops / (k1_ms / 1e3) / 1e12,
+          "peak": bf16, "unit": "TFLOP/s", "ms_per_launch": k1_ms,
+          "algorithmic_flops_per_launch": k1_flops,
+          "traffic": traffic_info.get("k_pairs_mma_bytes_per_unit", 0) * B or None}
+    k1["frac"] = k1["achieved"] / bf16
+    # network assembly, dedup, BDeu, JS: algorithmic bytes (each stage's
+    # inputs and outputs once through HBM)
+    k2_ms = acc["ms_units"] / launches_per_kernel
+    k2 = {"kernel": "k_units", "bound": "hbm", "achieved": bu * B / (k2_ms / 1e3) / 1e9,
+          "peak": hbm, "unit": "GB/s", "ms_per_launch": k2_ms,
+          "algorithmic_bytes_per_launch": bu * B,
+          "traffic": traffic_info.get("k_units_bytes_per_unit", 0) * B or None}
+    k2["frac"] = k2["achieved"] / hbm
+    dom = k1 if k1_ms >= k2_ms else k2
+    roofline = dict(dom)
+    roofline["peak_source"] = (f"MEASURED_PEAKS.json {'bf16_tflops' if dom is k1 else 'hbm_gbs'} "
+                               f"({peak_kind}); the GEMM runs e4m3 operands, whose dense peak is "
+                               "twice the bf16 one" if dom is k1 else
+                               f"MEASURED_PEAKS.json hbm_gbs ({peak_kind})")
     cpu = None
+    precision = {"tables": int(stats["tables"]), "filtered": int(stats["filtered"]),
+                 "exact_rechecks": int(stats["exact_rechecks"])}
     if world == 1 and not args.no_cpu:
         try:
-            cu, cs = cpu_sample(w, genes, seed, 1, args.cpu_units, os.cpu_count() or 1)
+            cu, cs, ojs, oU = cpu_sample(w, genes, seed, 1, args.cpu_units, os.cpu_count() or 1)
             cpu = {"value": cu, "unit": UNIT, "cores": os.cpu_count() or 1, "kind": "port",
                    "sample": f"{args.cpu_units} permutations of the same set ({cs:.1f} s)"}
+            # the same permutations on the GPU, against the FP64 oracle
+            ctx.clear_sets()
+            gjs, gU = ctx.run_permutations(ctx.add_set(genes), 1, args.cpu_units)
+            precision.update({
+                "oracle_units": args.cpu_units,
+                "unique_networks_equal": bool(np.array_equal(gU, oU)),
+                "js_max_rel_err": float(np.max(np.abs(gjs - ojs) / np.maximum(np.abs(ojs), 1e-300)))})
         except Exception as e:  # pragma: no cover - reported, not hidden
             cpu = {"value": None, "unit": UNIT, "cores": 0, "kind": "port", "sample": f"failed: {e}"}
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -302,11 +396,12 @@ def run_ours(args, rank, world, local):
                     "d2h_bytes_per_step": d2h},
             "gpu_launches": acc["launches"],
             "stage_ms": {"k_pairs": acc["ms_pairs"], "k_units": acc["ms_units"]},
-            "roofline": {"kernel": kname, "bound": "hbm", "achieved": achieved, "peak": hbm,
-                         "unit": "GB/s", "frac": achieved / hbm, "traffic": traffic,
-                         "peak_source": f"MEASURED_PEAKS.json hbm_gbs ({peak_kind})",
-                         "algorithmic_bytes_per_launch": kbytes},
+            "roofline": roofline,
+            "kernels": {"k_pairs_mma": k1, "k_units": k2},
             "clocks": clk.summary(),
+            "plain_fp64_form": fp64,
+            "vs_plain_fp64": (value / world / fp64["value"]) if fp64 else None,
+            "precision": precision,
             "cpu_baseline": cpu}
     print(json.dumps(line), flush=True)
     ctx.close()
@@ -322,11 +417,18 @@ def main():
     ap.add_argument("--units", type=int, default=2048, help="permutations per step")
     ap.add_argument("--cpu-units", type=int, default=16, help="permutations in the CPU sample")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-fp64", action="store_true")
+    ap.add_argument("--workload", type=int, default=4, choices=[3, 4, 5],
+                    help="3 or 5: multi-set sample (prints its own line)")
+    ap.add_argument("--sets", type=int, default=100)
+    ap.add_argument("--perms", type=int, default=0)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     rank, world, local = dist_env()
     if args.impl == "reference":
         run_reference(args, rank, world)
+    elif args.workload != 4:
+        run_multiset(args, rank, world, local)
     else:
         run_ours(args, rank, world, local)
 

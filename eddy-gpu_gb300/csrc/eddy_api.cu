@@ -82,8 +82,13 @@ struct eddy_ctx {
   DevBuf d_oids, d_ocnt, d_opar, d_odist, d_olval, d_orows, d_stats;
   DevBuf d_Y, d_afp8, d_err;  // tensor-core contingency operands
   int sms = 148;
+  // autotuned contingency-kernel variant per set shape (g, n); -1 = untuned
+  int tuned_g = -1, tuned_n = -1, tuned_variant = -1;
+  float tuned_ms[4] = {0, 0, 0, 0};
   int lg_shift = 0;
   bool lg_ready = false;
+  int lg_n = -1;  // sample count the fixed-point lgamma table was built for
+  unsigned long long last_stats[4] = {0, 0, 0, 0};
   // timing of the last run
   double ms_total = 0, ms_pairs = 0, ms_units = 0;
   long long launches = 0;
@@ -126,7 +131,7 @@ int prepare_set(eddy_ctx *ctx, int set_id, SetRun &sr) {
   const int c = g * (g - 1) / 2;
   if (g > 512) return fail(ctx, EDDY_ERR_CAPACITY, "gene set %d has %d genes (> 512)", set_id, g);
   CK(cudaSetDevice(ctx->o.device));
-  if (!ctx->lg_ready) {
+  if (!ctx->lg_ready || ctx->lg_n != n) {
     std::vector<int64_t> lg;
     int8_t dmap[82];
     bdeu_table(n, lg, ctx->lg_shift, dmap);
@@ -134,6 +139,7 @@ int prepare_set(eddy_ctx *ctx, int set_id, SetRun &sr) {
     CK(cudaMemcpy(ctx->d_lg.p, lg.data(), lg.size() * sizeof(int64_t), cudaMemcpyHostToDevice));
     CK(set_divisor_map(dmap));
     ctx->lg_ready = true;
+    ctx->lg_n = n;
   }
   const bool resident = (ctx->prepared_set == set_id);
   std::vector<int8_t> vals(resident ? 0 : (size_t)g * n);
@@ -183,6 +189,13 @@ int prepare_set(eddy_ctx *ctx, int set_id, SetRun &sr) {
   sd.alpha_edge = ctx->o.alpha_edge;
   sd.alpha_edge_prior = ctx->o.alpha_edge_prior;
   sd.exact_all = compute_thresholds(sd.alpha_edge, sd.alpha_edge_prior, g, sd.bonf, sd.thr) ? 1 : 0;
+  {
+    // EDDY_DECISIONS=fp64: the plain FP64 form -- every table of every pair
+    // evaluated with the reference's FP64 formula, no FP32 fast path, no
+    // leave-one-out filter (the comparator of the batched FP32 form)
+    const char *dm = getenv("EDDY_DECISIONS");
+    if (dm && strcmp(dm, "fp64") == 0) sd.exact_all = 1;
+  }
   sd.all_valid = ctx->set_all_valid ? 1 : 0;
   sd.planes = ctx->d_planes.as<uint64_t>();
   sd.valid = ctx->d_valid.as<uint64_t>();
@@ -237,8 +250,39 @@ int launch_pairs_any(eddy_ctx *ctx, const SetDev &sd, const uint64_t *masks, int
   CK(ctx->d_afp8.ensure((size_t)mma_bpad(B) * mma_npad(sd.n)));
   CK(ctx->d_err.ensure(sizeof(unsigned)));
   CK(cudaMemsetAsync(ctx->d_err.p, 0, sizeof(unsigned), ctx->stream));
+  int variant = 0;
+  const char *ev = getenv("EDDY_MMA_VARIANT");
+  if (ev) {
+    variant = atoi(ev) % mma_variants();
+  } else if (ctx->tuned_g == sd.g && ctx->tuned_n == sd.n && ctx->tuned_variant >= 0) {
+    variant = ctx->tuned_variant;
+  } else if (B >= 512) {
+    // autotune on this batch: time every variant once (same results), keep
+    // the fastest for this (g, n); the last run leaves dmask filled
+    float best = 1e30f;
+    int bi = 0;
+    for (int v = mma_variants() - 1; v >= 0; v--) {
+      CK(cudaEventRecord(ctx->ev[2], ctx->stream));
+      CK(launch_pairs_mma(sd, masks, B, ctx->d_afp8.as<uint8_t>(), ctx->d_Y.as<uint8_t>(), dmask,
+                          nullptr, ctx->d_err.as<unsigned>(), ctx->sms, ctx->stream, v));
+      CK(cudaEventRecord(ctx->ev[3], ctx->stream));
+      CK(cudaEventSynchronize(ctx->ev[3]));
+      float ms = 0;
+      cudaEventElapsedTime(&ms, ctx->ev[2], ctx->ev[3]);
+      ctx->tuned_ms[v] = ms;
+      if (ms < best) {
+        best = ms;
+        bi = v;
+      }
+      ctx->launches += 2;
+    }
+    ctx->tuned_g = sd.g;
+    ctx->tuned_n = sd.n;
+    ctx->tuned_variant = bi;
+    variant = bi;
+  }
   CK(launch_pairs_mma(sd, masks, B, ctx->d_afp8.as<uint8_t>(), ctx->d_Y.as<uint8_t>(), dmask, stats,
-                      ctx->d_err.as<unsigned>(), ctx->sms, ctx->stream));
+                      ctx->d_err.as<unsigned>(), ctx->sms, ctx->stream, variant));
   ctx->launches += 2;
   return EDDY_OK;
 }
@@ -407,6 +451,7 @@ int run_units(eddy_ctx *ctx, SetRun &sr, int nunits, const uint64_t *masks_host,
   ctx->ms_pairs += t_pairs;
   ctx->ms_units += t_units;
   ctx->ms_total += t_pairs + t_units;
+  CK(cudaMemcpy(ctx->last_stats, ctx->d_stats.p, sizeof ctx->last_stats, cudaMemcpyDeviceToHost));
   return EDDY_OK;
 }
 
@@ -519,6 +564,9 @@ int eddy_load_matrix(eddy_ctx *ctx, const int8_t *data, int genes, int samples,
   if (!ctx) return EDDY_ERR_ARG;
   if (!data || !class_of_sample || genes < 1 || samples < 2)
     return fail(ctx, EDDY_ERR_ARG, "bad matrix shape %d x %d", genes, samples);
+  // class sizes and contingency counts are held as 16-bit integers on the GPU
+  if (samples > 65535)
+    return fail(ctx, EDDY_ERR_CAPACITY, "%d samples (> 65535)", samples);
   int nA = 0, nB = 0;
   for (int s = 0; s < samples; s++) {
     if (class_of_sample[s] == 0) nA++;
@@ -533,7 +581,6 @@ int eddy_load_matrix(eddy_ctx *ctx, const int8_t *data, int genes, int samples,
   ctx->W = (samples + 63) / 64;
   ctx->data.assign(data, data + (size_t)genes * samples);
   ctx->labels0.assign(class_of_sample, class_of_sample + samples);
-  ctx->lg_ready = false;
   ctx->prepared_set = -1;
   std::vector<uint64_t> m0(ctx->W);
   labels_to_mask(ctx->labels0.data(), samples, ctx->W, m0.data());
@@ -897,6 +944,13 @@ int eddy_device_info(int device, char *name, int name_len, int *sms, int *cc_maj
   if (sms) *sms = p.multiProcessorCount;
   if (cc_major) *cc_major = p.major;
   if (cc_minor) *cc_minor = p.minor;
+  return EDDY_OK;
+}
+
+int eddy_last_stats(const eddy_ctx *ctx, uint64_t *stats4, int *variant) {
+  if (!ctx || !stats4) return EDDY_ERR_ARG;
+  for (int i = 0; i < 4; i++) stats4[i] = ctx->last_stats[i];
+  if (variant) *variant = ctx->tuned_variant;
   return EDDY_OK;
 }
 

@@ -39,8 +39,10 @@ __device__ __forceinline__ void pair_rc(int p, int &row, int &col) {
 // ------------------------------------------------------------ decisions
 // Exact FP64 evaluation of one table exactly as kernel1.cu:121-203 and
 // 419-431 compute it, without FMA contraction (explicit _rn intrinsics).
-static __device__ __noinline__ int exact_decision(const int *t9, int prior,
-                                           const SetDev &sd) {
+static __device__ __noinline__ int exact_decision(int a0, int a1, int a2, int a3, int a4, int a5,
+                                                  int a6, int a7, int a8, int prior,
+                                                  const SetDev &sd) {
+  const int t9[9] = {a0, a1, a2, a3, a4, a5, a6, a7, a8};
   int ex[7] = {0, 0, 0, 0, 0, 0, 0};
   for (int c = 0; c < 3; c++) {
     for (int c1 = 0; c1 < 3; c1++) ex[c1] += t9[c * 3 + c1];
@@ -102,6 +104,7 @@ static __device__ __noinline__ int exact_decision(const int *t9, int prior,
 
 struct TabInfo {
   int R[3], C[3], N;
+  int rm, cm;   // smallest nonzero row / column marginal
   int dof;      // (2 - #zero cols)(2 - #zero rows)
   int yates;    // 1 if the Yates correction applies
   float chi;    // FP32 chi-square
@@ -110,7 +113,9 @@ struct TabInfo {
 __device__ __forceinline__ int dof_slot(int dof) { return dof == 1 ? 0 : dof == 2 ? 1 : dof == 4 ? 2 : -1; }
 
 // FP32 chi-square of a 3x3 table: (1/N) sum (|N o - R C| - yN)^2 / (R C),
-// numerators exact in integers.  Returns the marginals too.
+// numerators exact in 32-bit integers (tables of N <= 32767 samples; larger
+// ones take the exact FP64 path).  Returns the marginals too.
+constexpr int kFastMaxN = 32767;
 __device__ __forceinline__ void table_info(const int *t, TabInfo &ti) {
   ti.R[0] = t[0] + t[1] + t[2];
   ti.R[1] = t[3] + t[4] + t[5];
@@ -122,35 +127,49 @@ __device__ __forceinline__ void table_info(const int *t, TabInfo &ti) {
   int zr = (ti.R[0] == 0) + (ti.R[1] == 0) + (ti.R[2] == 0);
   int zc = (ti.C[0] == 0) + (ti.C[1] == 0) + (ti.C[2] == 0);
   ti.dof = (2 - zc) * (2 - zr);
+  const int N = ti.N;
   int rm = 0x7fffffff, cm = 0x7fffffff;
 #pragma unroll
   for (int a = 0; a < 3; a++) {
     if (ti.R[a] > 0 && ti.R[a] < rm) rm = ti.R[a];
     if (ti.C[a] > 0 && ti.C[a] < cm) cm = ti.C[a];
   }
-  ti.yates = (ti.N > 0 && (long long)rm * cm < 5ll * ti.N) ? 1 : 0;
+  ti.rm = rm;
+  ti.cm = cm;
+  if (N > kFastMaxN) {
+    ti.yates = 0;
+    ti.chi = 0.f;
+    return;
+  }
+  // rm * cm <= N^2 < 2^30 here
+  ti.yates = (N > 0 && rm * cm < 5 * N) ? 1 : 0;
+  // chi = (1/4N) sum_a (1/R_a) sum_b num_ab^2 / C_b: six reciprocals
+  float invC[3];
+#pragma unroll
+  for (int b = 0; b < 3; b++) invC[b] = ti.C[b] ? __frcp_rn((float)ti.C[b]) : 0.f;
   float chi = 0.f;
-  const int N = ti.N;
 #pragma unroll
   for (int a = 0; a < 3; a++) {
+    if (ti.R[a] == 0) continue;
+    float row = 0.f;
 #pragma unroll
     for (int b = 0; b < 3; b++) {
-      long long rc = (long long)ti.R[a] * ti.C[b];
-      if (rc != 0) {
-        long long d = (long long)N * t[a * 3 + b] - rc;
-        if (d < 0) d = -d;
-        long long num2 = ti.yates ? (2 * d - N) : (2 * d);  // 2(|d| - yN)
-        float nf = (float)num2;
-        chi += __fdividef(nf * nf, 4.f * (float)rc);
+      if (ti.C[b] != 0) {
+        int d = N * t[a * 3 + b] - ti.R[a] * ti.C[b];
+        d = d < 0 ? -d : d;
+        const int num2 = ti.yates ? (2 * d - N) : (2 * d);  // 2(|d| - yN), |.| < 2^31
+        const float nf = (float)num2;
+        row = fmaf(nf * nf, invC[b], row);
       }
     }
+    chi = fmaf(row, __frcp_rn((float)ti.R[a]), chi);
   }
-  ti.chi = (N > 0) ? chi / (float)N : 0.f;
+  ti.chi = (N > 0) ? chi * __frcp_rn(4.f * (float)N) : 0.f;
 }
 
 // 0/1 when certain from the FP32 value, 2 when the exact path must decide.
 __device__ __forceinline__ int fast_decision(const TabInfo &ti, int prior, const SetDev &sd) {
-  if (sd.exact_all || ti.N == 0) return 2;
+  if (sd.exact_all || ti.N == 0 || ti.N > kFastMaxN) return 2;
   int ds = dof_slot(ti.dof);
   if (ds < 0) return 0;  // dof 0: p = 1, never below an alpha <= 1
   const Thr &T = sd.thr[prior][ds];
@@ -167,7 +186,7 @@ __device__ __forceinline__ int decide(const int *t, int prior, const SetDev &sd,
   int d = fast_decision(ti, prior, sd);
   if (d == 2) {
     nexact++;
-    d = exact_decision(t, prior, sd);
+    d = exact_decision(t[0], t[1], t[2], t[3], t[4], t[5], t[6], t[7], t[8], prior, sd);
   }
   return d;
 }
@@ -179,35 +198,31 @@ __device__ __forceinline__ int decide(const int *t, int prior, const SetDev &sd,
 // B = max_rc |sqrt(e/e') - 1|; requires unchanged support (marginals >= 2),
 // unchanged Yates flag and N >= 32.
 __device__ __forceinline__ bool loo_safe(const TabInfo &ti, int prior, const SetDev &sd) {
-  if (sd.exact_all || ti.N < 32) return false;
-  int ds = dof_slot(ti.dof);
-  if (ds < 0) {
-    // dof 0 stays 0 only when the support cannot grow: it never grows under
-    // removal; it can shrink only if a nonzero marginal is 1.
-  }
-  int rm = 0x7fffffff, cm = 0x7fffffff;
-#pragma unroll
-  for (int a = 0; a < 3; a++) {
-    if (ti.R[a] > 0 && ti.R[a] < rm) rm = ti.R[a];
-    if (ti.C[a] > 0 && ti.C[a] < cm) cm = ti.C[a];
-  }
+  if (sd.exact_all || ti.N < 32 || ti.N > kFastMaxN) return false;
+  const int rm = ti.rm, cm = ti.cm;
   if (rm < 2 || cm < 2) return false;
+  const int ds = dof_slot(ti.dof);
   if (ds < 0) return true;  // support unchanged: dof stays 0, p = 1
-  const long long N = ti.N;
+  const int N = ti.N;  // <= 32767: the products below fit in 32 bits
   if (ti.yates) {
-    if (!((long long)rm * cm < 5ll * (N - 1))) return false;
+    if (!(rm * cm < 5 * (N - 1))) return false;
   } else {
-    if (!((long long)(rm - 1) * (cm - 1) >= 5ll * (N - 1))) return false;
+    if (!((rm - 1) * (cm - 1) >= 5 * (N - 1))) return false;
   }
-  // lower bound of the smallest expected count of any cell-removed table;
-  // FP32 (FP64 is the slowest pipe on this part), rounded down
-  const float emin = __fdiv_rd(__fmul_rd((float)(rm - 1), (float)(cm - 1)), (float)(N - 1));
-  const float A = sqrtf(15.f / emin + 5.f / (float)(N - 1));
-  const float ratio = ((float)rm / (float)(rm - 1)) * ((float)cm / (float)(cm - 1));
-  const float B = fmaxf(sqrtf(ratio) - 1.f, 1.f / (float)(N - 1)) * 1.001f;
+  // fast reciprocals / square roots (a few ulp) with explicit 1e-5 safety
+  // factors in the conservative direction
+  const float lo = 0.99999f, hi = 1.00001f;
+  const float inv_n1 = __frcp_rn((float)(N - 1));
+  const float emin = (float)((rm - 1) * (cm - 1)) * inv_n1 * lo;       // lower bound
+  const float a2 = (15.f * __frcp_rn(emin) + 5.f * inv_n1) * hi;
+  const float A = a2 * rsqrtf(a2) * hi;                                 // sqrt(a2), upper
+  const float ratio = (float)(rm * cm) * __frcp_rn((float)((rm - 1) * (cm - 1))) * hi;
+  const float B = fmaxf(ratio * rsqrtf(ratio) * hi - 1.f, inv_n1 * hi) * 1.001f;
   const float rel = 2e-5f;
-  const float sup = sqrtf(ti.chi * (1.f + rel));
-  const float slo = sqrtf(fmaxf(ti.chi * (1.f - rel), 0.f));
+  const float xs = ti.chi * (1.f + rel);
+  const float sup = (xs > 0.f ? xs * rsqrtf(xs) : 0.f) * hi;
+  const float xl = ti.chi * (1.f - rel);
+  const float slo = (xl > 0.f ? xl * rsqrtf(xl) : 0.f) * lo;
   const float D = (A + B * sup) * 1.01f + 1e-3f;
   const float whi = (sup + D) * (sup + D) * 1.0001f;
   const float wl = fmaxf(slo - D, 0.f);
@@ -219,17 +234,14 @@ __device__ __forceinline__ bool loo_safe(const TabInfo &ti, int prior, const Set
   return false;
 }
 
-// 10-bit decision mask of one (pair, class) table: bit 0 = full table,
-// bit 1+3a+b = table with one sample of cell (a,b) removed.
-__device__ __forceinline__ uint32_t pair_mask(int *t, int prior, const SetDev &sd,
-                                              unsigned &nexact, unsigned &nfilt) {
-  TabInfo ti;
-  const int bit0 = decide(t, prior, sd, ti, nexact);
-  if (loo_safe(ti, prior, sd)) {
-    nfilt++;
-    return bit0 ? 0x3FFu : 0u;
-  }
-  uint32_t m = (uint32_t)bit0;
+// Decisions of the nine cell-removed tables (the rare path: the filter did
+// not settle them); counts by value so nothing goes through local memory.
+static __device__ __noinline__ uint32_t removed_cell_bits(int a0, int a1, int a2, int a3, int a4,
+                                                          int a5, int a6, int a7, int a8, int bit0,
+                                                          int prior, const SetDev &sd,
+                                                          unsigned &nexact) {
+  int t[9] = {a0, a1, a2, a3, a4, a5, a6, a7, a8};
+  uint32_t m = 0;
 #pragma unroll 1
   for (int cell = 0; cell < 9; cell++) {
     int bit = bit0;
@@ -242,6 +254,20 @@ __device__ __forceinline__ uint32_t pair_mask(int *t, int prior, const SetDev &s
     m |= (uint32_t)bit << (1 + cell);
   }
   return m;
+}
+
+// 10-bit decision mask of one (pair, class) table: bit 0 = full table,
+// bit 1+3a+b = table with one sample of cell (a,b) removed.
+__device__ __forceinline__ uint32_t pair_mask(int *t, int prior, const SetDev &sd,
+                                              unsigned &nexact, unsigned &nfilt) {
+  TabInfo ti;
+  const int bit0 = decide(t, prior, sd, ti, nexact);
+  if (loo_safe(ti, prior, sd)) {
+    nfilt++;
+    return bit0 ? 0x3FFu : 0u;
+  }
+  return (uint32_t)bit0 | removed_cell_bits(t[0], t[1], t[2], t[3], t[4], t[5], t[6], t[7], t[8],
+                                            bit0, prior, sd, nexact);
 }
 
 // --------------------------------------------------- capped parent lists
@@ -323,6 +349,19 @@ static __device__ int64_t bdeu_score(const SetDev &sd, int t, int np, const int 
   int q = 1;
   for (int k = 1; k <= np; k++) q *= nstate[k];
   if (q == 0) return 0;
+  if (np == 0) {
+    // no parent: N_1k are the node's state counts in this class
+    if (r == 0) return 0;
+    const int64_t *LG1 = sd.lg + (size_t)c_dmap[r] * sd.lg_stride;
+    int nij = 0;
+    int64_t sc = 0;
+    for (int kk = 0; kk < r; kk++) {
+      const int cnt = cnt3[t * 3 + st[0][kk]];
+      nij += cnt;
+      sc += LG1[cnt];
+    }
+    return sc - sd.lg[(size_t)c_dmap[1] * sd.lg_stride + nij];
+  }
   const int64_t *LGq = sd.lg + (size_t)c_dmap[q] * sd.lg_stride;
   const int64_t *LGqr = (r > 0) ? sd.lg + (size_t)c_dmap[q * r] * sd.lg_stride : nullptr;
   const int W = sd.W;

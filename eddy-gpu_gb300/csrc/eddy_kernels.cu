@@ -258,6 +258,8 @@ struct UnitSmem {
   int nphi[2];
   int ndab;
   int nrphi[2];
+  int firstB0;  // first class-2 network equal to the class-2 full network
+  int repB;     // first occurrence of the class-2 full network
   int scan[32];
   unsigned status;
   int U;
@@ -409,7 +411,7 @@ __device__ void scores_of(const SetDev &sd, const UnitPtrs &P, int t, int np, co
   }
 }
 
-__global__ void __launch_bounds__(256) k_units(SetDev sd, BatchDev bd) {
+__global__ void __launch_bounds__(256, 3) k_units(SetDev sd, BatchDev bd) {
   extern __shared__ __align__(16) char smraw[];
   UnitSmem &SM = *reinterpret_cast<UnitSmem *>(smraw);
   const int nw = blockDim.x >> 5, lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -626,7 +628,16 @@ __global__ void __launch_bounds__(256) k_units(SetDev sd, BatchDev bd) {
       unsigned long long hn = 0;
       int ps[3] = {0xFFFF, 0xFFFF, 0xFFFF};
       int cnt = 0;
+      bool flips = false;
       if (t >= 0 && myst[t] <= 2) {
+        // does sample sigma trigger any flip entry of row t?
+        const int sr = myst[t] * 3;
+        for (int i = P.phs[k * g + t], e = P.phe[k * g + t]; i < e && !flips; i++) {
+          const int sc = myst[pcol[k][i]];
+          flips = sc <= 2 && (((phi[k][i] & 0x1FFu) >> (sr + sc)) & 1u);
+        }
+      }
+      if (flips) {
         ListGen Gn, Go;
         gen_for(Gn, sd, P, phi[k], pcol[k], k, t, myst);
         gen_for(Go, sd, P, phi[k], pcol[k], k, t, nullptr);
@@ -676,9 +687,29 @@ __global__ void __launch_bounds__(256) k_units(SetDev sd, BatchDev bd) {
     return;
   }
 
-  // ---- P4: first-occurrence dedup by hash, exact verification
+  // ---- P4: first-occurrence dedup.  A network with no changed node is its
+  // class's full network: class-1 ones duplicate network 0, class-2 ones the
+  // first class-2 network without changes (firstB0), whose own first
+  // occurrence the hash table decides.  Only changed networks and these two
+  // representatives go into the table (no hot key shared by hundreds of
+  // identical networks).
   const int HT = L.HT;
+  if (tid == 0) SM.firstB0 = S - 1;
+  __syncthreads();
+  for (int s = sd.nA + 1 + tid; s < S - 1; s += nt)
+    if (rec[(size_t)s * L.rec_words + 1] == 0) atomicMin(&SM.firstB0, s);
+  __syncthreads();
+  const int firstB0 = SM.firstB0;
+  auto inserted = [&](int s) -> bool {
+    return s == 0 || s == firstB0 || rec[(size_t)s * L.rec_words + 1] != 0;
+  };
+  auto slot_of = [&](unsigned long long key) -> unsigned {
+    unsigned slot = (unsigned)(mix64(key) & (HT - 1));
+    while (htk[slot] != key) slot = (slot + 1) & (HT - 1);
+    return slot;
+  };
   for (int s = tid; s < S; s += nt) {
+    if (!inserted(s)) continue;
     unsigned long long key = rec[(size_t)s * L.rec_words];
     if (key == ~0ull) key ^= 1ull;
     unsigned slot = (unsigned)(mix64(key) & (HT - 1));
@@ -692,17 +723,26 @@ __global__ void __launch_bounds__(256) k_units(SetDev sd, BatchDev bd) {
     }
   }
   __syncthreads();
+  if (tid == 0) {
+    unsigned long long kb = rec[(size_t)firstB0 * L.rec_words];
+    if (kb == ~0ull) kb ^= 1ull;
+    SM.repB = htv[slot_of(kb)];
+  }
+  __syncthreads();
+  const int repB = SM.repB;
   int running = 0;
   for (int s0 = 0; s0 < S; s0 += nt) {
     const int s = s0 + tid;
     int uq = 0;
     int rep = -1;
     if (s < S) {
-      unsigned long long key = rec[(size_t)s * L.rec_words];
-      if (key == ~0ull) key ^= 1ull;
-      unsigned slot = (unsigned)(mix64(key) & (HT - 1));
-      while (htk[slot] != key) slot = (slot + 1) & (HT - 1);
-      rep = htv[slot];
+      if (inserted(s)) {
+        unsigned long long key = rec[(size_t)s * L.rec_words];
+        if (key == ~0ull) key ^= 1ull;
+        rep = htv[slot_of(key)];
+      } else {
+        rep = (s <= sd.nA) ? 0 : repB;
+      }
       uq = (rep == s) ? 1 : 0;
     }
     int total;
@@ -724,6 +764,7 @@ __global__ void __launch_bounds__(256) k_units(SetDev sd, BatchDev bd) {
   for (int s = warp; s < S; s += nw) {
     int code = uid[s];
     if (code >= 0) continue;
+    if (!inserted(s)) continue;  // equal to its class's full network by construction
     const int r = -1 - code;
     int ks, ss, kr, sr;
     net_of(s, sd, sig, ks, ss);
@@ -860,73 +901,97 @@ __global__ void __launch_bounds__(256) k_units(SetDev sd, BatchDev bd) {
   }
   __syncthreads();
 
-  // ---- P6: normalisation (main.cu:1302-1404) and JS (main.cu:1406-1428)
+  // ---- P6: normalisation (main.cu:1302-1404) and JS (main.cu:1406-1428),
+  // both classes per reduction pass
   const int keep = bd.keep_slot ? bd.keep_slot[u] : -1;
   double js = 0.0;
-  // per class: min, max, mean of (d - min)
   long long mn[2], mx[2];
   double mean[2], esum[2];
-  for (int cls = 0; cls < 2; cls++) {
-    long long lmn = LLONG_MAX, lmx = LLONG_MIN;
+  {
+    long long l0 = LLONG_MAX, h0 = LLONG_MIN, l1 = LLONG_MAX, h1 = LLONG_MIN;
     for (int uu = tid; uu < U; uu += nt) {
-      long long d = dist[cls * S + uu];
-      lmn = d < lmn ? d : lmn;
-      lmx = d > lmx ? d : lmx;
+      const long long a = dist[uu], b = dist[S + uu];
+      l0 = a < l0 ? a : l0;
+      h0 = a > h0 ? a : h0;
+      l1 = b < l1 ? b : l1;
+      h1 = b > h1 ? b : h1;
     }
     for (int o = 16; o > 0; o >>= 1) {
-      long long a = __shfl_down_sync(0xffffffffu, lmn, o), b = __shfl_down_sync(0xffffffffu, lmx, o);
-      lmn = a < lmn ? a : lmn;
-      lmx = b > lmx ? b : lmx;
+      long long x;
+      x = __shfl_down_sync(0xffffffffu, l0, o); l0 = x < l0 ? x : l0;
+      x = __shfl_down_sync(0xffffffffu, h0, o); h0 = x > h0 ? x : h0;
+      x = __shfl_down_sync(0xffffffffu, l1, o); l1 = x < l1 ? x : l1;
+      x = __shfl_down_sync(0xffffffffu, h1, o); h1 = x > h1 ? x : h1;
     }
-    if (lane == 0) { SM.red_l[warp] = lmn; SM.red_l[16 + warp] = lmx; }
-    __syncthreads();
-    if (tid == 0) {
-      long long a = SM.red_l[0], b = SM.red_l[16];
-      for (int w = 1; w < nw; w++) {
-        a = SM.red_l[w] < a ? SM.red_l[w] : a;
-        b = SM.red_l[16 + w] > b ? SM.red_l[16 + w] : b;
-      }
-      SM.red_l[0] = a;
-      SM.red_l[16] = b;
+    if (lane == 0) {
+      SM.red_l[warp] = l0;
+      SM.red_l[8 + warp] = h0;
+      SM.red_l[16 + warp] = l1;
+      SM.red_l[24 + warp] = h1;
     }
     __syncthreads();
-    mn[cls] = SM.red_l[0];
-    mx[cls] = SM.red_l[16];
-    __syncthreads();
-    double ls = 0.0;
-    for (int uu = tid; uu < U; uu += nt) ls += (double)(dist[cls * S + uu] - mn[cls]);
-    for (int o = 16; o > 0; o >>= 1) ls += __shfl_down_sync(0xffffffffu, ls, o);
-    if (lane == 0) SM.red_d[warp] = ls;
-    __syncthreads();
-    if (tid == 0) {
-      double a = 0;
-      for (int w = 0; w < nw; w++) a += SM.red_d[w];
-      SM.red_d[0] = a;
+    l0 = SM.red_l[0], h0 = SM.red_l[8], l1 = SM.red_l[16], h1 = SM.red_l[24];
+    for (int w = 1; w < nw; w++) {
+      l0 = SM.red_l[w] < l0 ? SM.red_l[w] : l0;
+      h0 = SM.red_l[8 + w] > h0 ? SM.red_l[8 + w] : h0;
+      l1 = SM.red_l[16 + w] < l1 ? SM.red_l[16 + w] : l1;
+      h1 = SM.red_l[24 + w] > h1 ? SM.red_l[24 + w] : h1;
     }
-    __syncthreads();
-    mean[cls] = SM.red_d[0] / (double)U;
-    __syncthreads();
-  }
-  // exp of the adjusted scores and their sums (FP64: U values per class)
-  for (int cls = 0; cls < 2; cls++) {
-    const double scale = 10.0 / (double)(mx[cls] - mn[cls]);  // inf when all equal
-    double ls = 0.0;
-    for (int uu = tid; uu < U; uu += nt)
-      ls += exp(((double)(dist[cls * S + uu] - mn[cls]) - mean[cls]) * scale);
-    for (int o = 16; o > 0; o >>= 1) ls += __shfl_down_sync(0xffffffffu, ls, o);
-    if (lane == 0) SM.red_d[warp] = ls;
-    __syncthreads();
-    if (tid == 0) {
-      double a = 0;
-      for (int w = 0; w < nw; w++) a += SM.red_d[w];
-      SM.red_d[0] = a;
-    }
-    __syncthreads();
-    esum[cls] = SM.red_d[0];
-    __syncthreads();
+    mn[0] = l0, mx[0] = h0, mn[1] = l1, mx[1] = h1;
   }
   {
-    const double sA = 10.0 / (double)(mx[0] - mn[0]), sB = 10.0 / (double)(mx[1] - mn[1]);
+    double s0 = 0.0, s1 = 0.0;
+    for (int uu = tid; uu < U; uu += nt) {
+      s0 += (double)(dist[uu] - mn[0]);
+      s1 += (double)(dist[S + uu] - mn[1]);
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      s0 += __shfl_down_sync(0xffffffffu, s0, o);
+      s1 += __shfl_down_sync(0xffffffffu, s1, o);
+    }
+    __syncthreads();  // red_l readers done
+    if (lane == 0) {
+      SM.red_d[warp] = s0;
+      SM.red_d[8 + warp] = s1;
+    }
+    __syncthreads();
+    s0 = 0.0;
+    s1 = 0.0;
+    for (int w = 0; w < nw; w++) {
+      s0 += SM.red_d[w];
+      s1 += SM.red_d[8 + w];
+    }
+    mean[0] = s0 / (double)U;
+    mean[1] = s1 / (double)U;
+  }
+  // likelihoods exp((d - mean) * 10 / (max - min)) (FP64: U values per class)
+  const double sA = 10.0 / (double)(mx[0] - mn[0]), sB = 10.0 / (double)(mx[1] - mn[1]);
+  {
+    double e0 = 0.0, e1 = 0.0;
+    for (int uu = tid; uu < U; uu += nt) {
+      e0 += exp(((double)(dist[uu] - mn[0]) - mean[0]) * sA);
+      e1 += exp(((double)(dist[S + uu] - mn[1]) - mean[1]) * sB);
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      e0 += __shfl_down_sync(0xffffffffu, e0, o);
+      e1 += __shfl_down_sync(0xffffffffu, e1, o);
+    }
+    __syncthreads();
+    if (lane == 0) {
+      SM.red_d[16 + warp] = e0;
+      SM.red_d[24 + warp] = e1;
+    }
+    __syncthreads();
+    e0 = 0.0;
+    e1 = 0.0;
+    for (int w = 0; w < nw; w++) {
+      e0 += SM.red_d[16 + w];
+      e1 += SM.red_d[24 + w];
+    }
+    esum[0] = e0;
+    esum[1] = e1;
+  }
+  {
     double ls = 0.0;
     for (int uu = tid; uu < U; uu += nt) {
       // likelihoods (main.cu:1360-1394) and the two KL terms of kool()
@@ -944,6 +1009,7 @@ __global__ void __launch_bounds__(256) k_units(SetDev sd, BatchDev bd) {
       }
     }
     for (int o = 16; o > 0; o >>= 1) ls += __shfl_down_sync(0xffffffffu, ls, o);
+    __syncthreads();
     if (lane == 0) SM.red_d[warp] = ls;
     __syncthreads();
     if (tid == 0) {

@@ -11,12 +11,14 @@
 // of TMEM and makes the 10-bit leave-one-out decision masks of both classes
 // (kernel1.cu:121-203, 419-431) in the same kernel.
 //
-// Tile: 128 units (TMEM lanes) x 128 pair-cells (two halves of 64 columns,
-// each 7 pairs x 9 cells + 1 pad column) x K in 128-sample chunks; operands staged by TMA
-// (cp.async.bulk.tensor, 128B swizzle) through a 4-stage mbarrier ring.
-// Warp roles: 0 = TMA producer, 1 = TMEM owner + MMA issuer, 2..9 =
-// epilogue (two warps per TMEM lane quadrant, 7 pairs each).  Accumulators
-// are double-buffered (2 x 128 TMEM columns).  Every mbarrier wait is
+// Tile: 128 units (TMEM lanes) x 128 pair-cells (four 32-column groups, each
+// 3 pairs x 9 cells + 5 pad columns) x K in 128-sample chunks; operands
+// staged by TMA (cp.async.bulk.tensor, 128B swizzle) through an mbarrier
+// ring.  Warp roles: 0 = TMA producer, 1 = TMEM owner + MMA issuer, 2.. =
+// epilogue warps (kEpi of them; each owns one TMEM lane quadrant and one or
+// two column groups, reads them with one tcgen05.ld each and decides their
+// pairs from registers).  Accumulators are double-buffered (2 x 128 TMEM
+// columns).  Every mbarrier wait is
 // bounded (2 s on %globaltimer); a timeout sets an error word, every role
 // drains, and TMEM is released before the block exits.
 #include <cuda.h>
@@ -30,9 +32,8 @@
 namespace eddy {
 
 namespace {
-constexpr int kTM = 128, kTN = 128, kPairsPerTile = 14, kKC = 128, kStages = 4;
-constexpr int kEpiWarps = 8;
-constexpr int kThreads = 32 * (2 + kEpiWarps);
+constexpr int kTM = 128, kTN = 128, kGroups = 4, kPairsPerGroup = 3, kKC = 128;
+constexpr int kPairsPerTile = kGroups * kPairsPerGroup;
 constexpr uint32_t kStageBytes = (kTM + kTN) * kKC;  // 32 KB
 constexpr unsigned long long kTimeoutNs = 2000000000ull;
 
@@ -132,20 +133,25 @@ __device__ __forceinline__ void tmem_ld_wait() {
 }
 }  // namespace
 
+template <int kStages>
 struct MmaSmem {
   unsigned long long full[kStages], empty[kStages], accfull[2], accempty[2];
   uint32_t tmem_base;
 };
 
-__global__ void __launch_bounds__(kThreads, 1)
+// kStages: depth of the TMA ring; kEpi: epilogue warps (8 or 16);
+// kMinBlocks: CTAs per SM the register budget is sized for (two CTAs share
+// TMEM's 512 columns).  All variants produce identical masks; the autotuner
+// picks by time.
+template <int kStages, int kEpi, int kMinBlocks>
+__global__ void __launch_bounds__(32 * (2 + kEpi), kMinBlocks)
     k_pairs_mma(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
                 SetDev sd, int B, int nk, int ntiles, int mblocks, uint32_t *dmask,
                 unsigned long long *stats, unsigned *err) {
   extern __shared__ __align__(1024) uint8_t smraw[];
   // 1024-byte aligned stage ring, then barriers, then the epilogue buffer
   uint8_t *base = (uint8_t *)(((uintptr_t)smraw + 1023) & ~(uintptr_t)1023);
-  MmaSmem &S = *reinterpret_cast<MmaSmem *>(base + kStages * kStageBytes);
-  uint16_t *ebuf = reinterpret_cast<uint16_t *>(base + kStages * kStageBytes + 1024);
+  MmaSmem<kStages> &S = *reinterpret_cast<MmaSmem<kStages> *>(base + kStages * kStageBytes);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   volatile unsigned *verr = err;
   const int ntot = ntiles * mblocks;
@@ -157,7 +163,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     }
     for (int a = 0; a < 2; a++) {
       mbar_init(smem_u32(&S.accfull[a]), 1);
-      mbar_init(smem_u32(&S.accempty[a]), 32 * kEpiWarps);
+      mbar_init(smem_u32(&S.accempty[a]), 32 * kEpi);
     }
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
@@ -227,10 +233,11 @@ __global__ void __launch_bounds__(kThreads, 1)
       }
     }
   } else {
-    // epilogue: warps 2..9; TMEM lane quadrant = warp % 4, pair half = (warp-2)/4
-    const int quad = warp & 3, half = (warp - 2) >> 2;
+    // epilogue: TMEM lane quadrant = warp % 4; the kEpi/4 warps of a quadrant
+    // split the four column groups (one or two each)
+    constexpr int kPerQuad = kEpi / 4, kGpw = kGroups / kPerQuad;
+    const int quad = warp & 3, wq = (warp - 2) >> 2;
     const int row = quad * 32 + lane;  // TMEM lane = unit within the tile
-    const int et = threadIdx.x - 64;   // 0..255
     int acc = 0;
     uint32_t accphase = 0;
     unsigned nexact = 0, nfilt = 0, ntab = 0;
@@ -238,17 +245,19 @@ __global__ void __launch_bounds__(kThreads, 1)
       const int tn = t / mblocks, mb = t % mblocks;
       if (!mbar_wait(smem_u32(&S.accfull[acc]), accphase, verr)) break;
       tc_fence_after();
-      // this warp's 63 columns (7 pairs x 9 cells) -> u16 in smem
-      const uint32_t taddr = tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)(acc * kTN + half * 64);
-      uint32_t r[32];
-      tmem_ld32(taddr, r);
-      tmem_ld_wait();
+      // counts of the warp's group(s), packed two u16 per register
+      uint32_t pk[kGpw][14];
 #pragma unroll
-      for (int j = 0; j < 32; j++) ebuf[j * 256 + et] = (uint16_t)__float2uint_rn(__uint_as_float(r[j]));
-      tmem_ld32(taddr + 32, r);
-      tmem_ld_wait();
+      for (int gi = 0; gi < kGpw; gi++) {
+        const int grp = wq + gi * kPerQuad;
+        uint32_t r[32];
+        tmem_ld32(tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)(acc * kTN + grp * 32), r);
+        tmem_ld_wait();
 #pragma unroll
-      for (int j = 0; j < 31; j++) ebuf[(32 + j) * 256 + et] = (uint16_t)__float2uint_rn(__uint_as_float(r[j]));
+        for (int i = 0; i < 14; i++)
+          pk[gi][i] = __float2uint_rn(__uint_as_float(r[2 * i])) |
+                      (__float2uint_rn(__uint_as_float(r[2 * i + 1])) << 16);
+      }
       tc_fence_before();
       mbar_arrive(smem_u32(&S.accempty[acc]));
       if (++acc == 2) {
@@ -257,14 +266,31 @@ __global__ void __launch_bounds__(kThreads, 1)
       }
       const int u = mb * kTM + row;
       if (u < B) {
-        for (int q = 0; q < 7; q++) {
-          const int p = tn * kPairsPerTile + half * 7 + q;
-          if (p >= sd.c) break;
+        // rolled loop over the warp's pairs; a pair's nine counts are picked
+        // out of the packed registers by selects (no dynamic register index)
+#pragma unroll 1
+        for (int j = 0; j < kGpw * kPairsPerGroup; j++) {
+          const int gi = j / kPairsPerGroup, q = j % kPairsPerGroup;
+          const int grp = wq + gi * kPerQuad;
+          const int p = tn * kPairsPerTile + grp * kPairsPerGroup + q;
+          if (p >= sd.c) continue;
           int tA[9], tB[9];
           const uint16_t *ct = sd.ctot + (size_t)p * 9;
 #pragma unroll
           for (int k = 0; k < 9; k++) {
-            tA[k] = ebuf[(q * 9 + k) * 256 + et];
+            // cell k of pair q sits at column 9q + k of the group
+            uint32_t v0 = (pk[0][k >> 1] >> (16 * (k & 1))) & 0xFFFFu;
+            uint32_t v1 = (pk[0][(9 + k) >> 1] >> (16 * ((9 + k) & 1))) & 0xFFFFu;
+            uint32_t v2 = (pk[0][(18 + k) >> 1] >> (16 * ((18 + k) & 1))) & 0xFFFFu;
+            uint32_t v = (q == 0) ? v0 : (q == 1) ? v1 : v2;
+            if (kGpw > 1) {
+              uint32_t w0 = (pk[kGpw - 1][k >> 1] >> (16 * (k & 1))) & 0xFFFFu;
+              uint32_t w1 = (pk[kGpw - 1][(9 + k) >> 1] >> (16 * ((9 + k) & 1))) & 0xFFFFu;
+              uint32_t w2 = (pk[kGpw - 1][(18 + k) >> 1] >> (16 * ((18 + k) & 1))) & 0xFFFFu;
+              const uint32_t w = (q == 0) ? w0 : (q == 1) ? w1 : w2;
+              v = gi ? w : v;
+            }
+            tA[k] = (int)v;
             tB[k] = (int)ct[k] - tA[k];
           }
           const int prior = sd.prior[p] ? 1 : 0;
@@ -297,9 +323,10 @@ __global__ void __launch_bounds__(kThreads, 1)
 }
 
 // -------------------------------------------------------------- operands
-// Y: row (tile*128 + h*64 + q*9 + 3a + b), h < 2, q < 7 = indicator over the
-// samples of pair tile*14 + h*7 + q having (x_row = a-1, x_col = b-1);
-// e4m3 1.0 = 0x38; column 63 of each half and out-of-range pairs are zero.
+// Y: row (tile*128 + h*32 + q*9 + 3a + b), h < 4, q < 3 = indicator over the
+// samples of pair tile*12 + h*3 + q having (x_row = a-1, x_col = b-1);
+// e4m3 1.0 = 0x38; columns 27..31 of each group and out-of-range pairs are
+// zero.
 __global__ void k_build_y(const uint64_t *planes, int g, int W, int c, int n_pad, int ntiles,
                           uint8_t *Y) {
   const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;  // 16-sample chunk
@@ -308,12 +335,12 @@ __global__ void k_build_y(const uint64_t *planes, int g, int W, int c, int n_pad
   if (idx >= rows * chunks) return;
   const int rr = (int)(idx / chunks), ch = (int)(idx % chunks);
   const int tile = rr / kTN, r = rr % kTN;
-  const int h = r / 64, r64 = r % 64;
-  const int q = r64 / 9, cell = r64 % 9;
-  const int p = tile * kPairsPerTile + h * 7 + q;
+  const int h = r / 32, r32 = r % 32;
+  const int q = r32 / 9, cell = r32 % 9;
+  const int p = tile * kPairsPerTile + h * kPairsPerGroup + q;
   uint8_t v[16];
   uint32_t bits = 0;
-  if (r64 < 63 && p < c) {
+  if (r32 < kPairsPerGroup * 9 && p < c) {
     int row, col;
     pair_rc(p, row, col);
     const int a = cell / 3, b = cell % 3;
@@ -391,24 +418,36 @@ cudaError_t launch_build_y(const SetDev &sd, uint8_t *Y, cudaStream_t st) {
   return cudaGetLastError();
 }
 
+template <int kStages, int kEpi, int kMinBlocks>
+static cudaError_t launch_variant(const CUtensorMap &ma, const CUtensorMap &mb, const SetDev &sd,
+                                  int B, int np, int nt, int mblocks, uint32_t *dmask,
+                                  unsigned long long *stats, unsigned *err, int sms,
+                                  cudaStream_t st) {
+  const size_t smem = 1024 + kStages * kStageBytes + 1024;
+  auto kern = k_pairs_mma<kStages, kEpi, kMinBlocks>;
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  const int ntot = nt * mblocks;
+  const int grid = ntot < sms * kMinBlocks ? ntot : sms * kMinBlocks;
+  kern<<<grid, 32 * (2 + kEpi), smem, st>>>(ma, mb, sd, B, np / kKC, nt, mblocks, dmask, stats, err);
+  return cudaGetLastError();
+}
+
+int mma_variants() { return 2; }
+
 cudaError_t launch_pairs_mma(const SetDev &sd, const uint64_t *masks, int B, uint8_t *Afp8,
                              const uint8_t *Y, uint32_t *dmask, unsigned long long *stats,
-                             unsigned *err, int sms, cudaStream_t st) {
+                             unsigned *err, int sms, cudaStream_t st, int variant) {
   const int np = mma_npad(sd.n), Bp = mma_bpad(B), nt = mma_ntiles(sd.c);
   const long long work = (long long)Bp * (np / 16);
   k_masks_fp8<<<(unsigned)((work + 255) / 256), 256, 0, st>>>(masks, B, Bp, sd.W, np, Afp8);
   CUtensorMap ma, mb;
   if (!make_map(&ma, Afp8, np, Bp) || !make_map(&mb, (void *)Y, np, nt * kTN))
     return cudaErrorNotSupported;
-  const size_t smem = 1024 + kStages * kStageBytes + 1024 + 2 * 256 * 64;
-  cudaError_t e = cudaFuncSetAttribute(k_pairs_mma, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       (int)smem);
-  if (e != cudaSuccess) return e;
-  const int mblocks = Bp / kTM, ntot = nt * mblocks;
-  const int grid = ntot < sms ? ntot : sms;
-  k_pairs_mma<<<grid, kThreads, smem, st>>>(ma, mb, sd, B, np / kKC, nt, mblocks, dmask, stats,
-                                            err);
-  return cudaGetLastError();
+  const int mblocks = Bp / kTM;
+  if (variant == 1)
+    return launch_variant<4, 8, 1>(ma, mb, sd, B, np, nt, mblocks, dmask, stats, err, sms, st);
+  return launch_variant<4, 16, 1>(ma, mb, sd, B, np, nt, mblocks, dmask, stats, err, sms, st);
 }
 
 }  // namespace eddy

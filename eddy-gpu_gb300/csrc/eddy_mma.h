@@ -15,7 +15,10 @@ size_t mma_y_bytes(int c, int n);
 cudaError_t launch_build_y(const SetDev &sd, uint8_t *Y, cudaStream_t st);
 // Masks -> e4m3 operand (Afp8, mma_bpad(B) x mma_npad(n) bytes), then the
 // GEMM + decision kernel; *err is set on a bounded-wait timeout.
+// variant 0: 16 epilogue warps (one column group each); variant 1: 8
+// epilogue warps (two groups each); both a 4-stage ring, one CTA per SM.
+int mma_variants();
 cudaError_t launch_pairs_mma(const SetDev &sd, const uint64_t *masks, int B, uint8_t *Afp8,
                              const uint8_t *Y, uint32_t *dmask, unsigned long long *stats,
-                             unsigned *err, int sms, cudaStream_t st);
+                             unsigned *err, int sms, cudaStream_t st, int variant);
 }  // namespace eddy

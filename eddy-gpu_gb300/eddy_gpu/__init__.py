@@ -28,7 +28,8 @@ EXPORTS = ["eddy_ctx_create", "eddy_ctx_destroy", "eddy_last_error", "eddy_load_
            "eddy_get_js", "eddy_get_networks", "eddy_get_edge_list", "eddy_run_labellings",
            "eddy_debug_edges", "eddy_debug_unit", "eddy_run_permutations",
            "eddy_set_stream", "eddy_clear_sets", "eddy_write_networks", "eddy_write_bdeu",
-           "eddy_write_edge_list", "eddy_unit_noalloc", "eddy_device_info", "eddy_last_timing"]
+           "eddy_write_edge_list", "eddy_unit_noalloc", "eddy_last_stats", "eddy_device_info",
+           "eddy_last_timing"]
 
 
 class Opts(C.Structure):
@@ -89,6 +90,7 @@ def library(path: str | None = None):
                                       vp]
     L.eddy_write_bdeu.argtypes = [cp, cp, cp, cp, cp, cp, C.c_int, vp]
     L.eddy_write_edge_list.argtypes = [cp, vp, C.c_int, vp, vp, vp, vp, cp, cp]
+    L.eddy_last_stats.argtypes = [vp, vp, C.POINTER(C.c_int)]
     L.eddy_last_timing.argtypes = [vp, C.POINTER(C.c_double), C.POINTER(C.c_double),
                                    C.POINTER(C.c_double), C.POINTER(C.c_longlong)]
     _lib = L
@@ -301,6 +303,13 @@ class Context:
     def clear_sets(self):
         self._ck(self.L.eddy_clear_sets(self.h))
         self.g = {}
+
+    def stats(self) -> dict:
+        st = np.zeros(4, np.uint64)
+        v = C.c_int()
+        self._ck(self.L.eddy_last_stats(self.h, _p(st), C.byref(v)))
+        return dict(exact_rechecks=int(st[0]), tables=int(st[1]), filtered=int(st[2]),
+                    duplicates=int(st[3]), variant=v.value)
 
     def timing(self) -> dict:
         a, b, c = C.c_double(), C.c_double(), C.c_double()

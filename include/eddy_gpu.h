@@ -31,7 +31,7 @@ extern "C" {
 #define EDDY_ERR_ARG 1        /* invalid argument or size */
 #define EDDY_ERR_CUDA 2       /* CUDA runtime error (message via eddy_last_error) */
 #define EDDY_ERR_STATE 3      /* call out of order (e.g. results before eddy_run) */
-#define EDDY_ERR_CAPACITY 4   /* set too large for the GPU path (g > 512) */
+#define EDDY_ERR_CAPACITY 4   /* too large for the GPU path (g > 512 genes, > 65535 samples) */
 #define EDDY_ERR_BETAFIT 5    /* beta fit has alpha/beta <= 0 or non-finite */
 #define EDDY_ERR_INTERNAL 6   /* an internal consistency check failed */
 
@@ -197,6 +197,12 @@ int eddy_write_edge_list(const char *path, const char *const *genes, int g, cons
 int eddy_unit_noalloc(const eddy_opts *opts, const int8_t *vals, int g, int n,
                       const uint8_t *labels, const uint8_t *prior, void *stream, double *js,
                       int32_t *unique);
+
+/* Decision-path counters of the last batch run: [0] tables re-evaluated in
+ * FP64 (guard-band rechecks), [1] (pair, class) tables decided, [2] of them
+ * whose ten leave-one-out tables the filter settled at once, [3] duplicate
+ * networks; *variant: the autotuned contingency-kernel variant (-1: none). */
+int eddy_last_stats(const eddy_ctx *ctx, uint64_t *stats4, int *variant);
 
 /* Name, SM count and compute capability of a device (the reference's
  * device banner, main.cu:28-56, without the fields CUDA 13 removed). */

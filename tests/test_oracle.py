@@ -204,3 +204,100 @@ def test_reference_emulator_matches_oracle_random(oracle_lib):
         assert a["U"] == b["U"] and np.array_equal(a["unique_ids"], b["unique_ids"])
         assert np.allclose(a["out5"], b["out5"], rtol=1e-13, atol=1e-12)
         assert (np.isnan(a["js"]) and np.isnan(b["js"])) or abs(a["js"] - b["js"]) < 1e-12
+
+
+def _edges_of(g, parent_sets):
+    """Edge vector of one network: pair (row t, parent j < t) sits at
+    t(t-1)/2 + j (main.cu:615-643)."""
+    e = np.zeros(g * (g - 1) // 2, np.uint8)
+    for t, ps in parent_sets.items():
+        for j in ps:
+            e[t * (t - 1) // 2 + j] = 1
+    return e
+
+
+def test_parent_cap_and_first_occurrence_uniqueness(oracle_lib):
+    """Crafted edge matrices: the -mp cap keeps the lowest-index parents
+    (kernel3.cu:41-165), networks equal after capping are duplicates, and a
+    duplicate is marked at its later occurrence only (main.cu:1060-1121)."""
+    O = oracle_lib
+    g, mp = 5, 2
+    nets = [
+        {3: [0, 1, 2], 4: [1]},     # row 3 capped to {0, 1}
+        {3: [0, 1], 4: [1]},        # equal to net 0 after the cap
+        {3: [0, 2], 4: [1]},        # differs
+        {3: [0, 1, 2, 2], 4: [1]},  # same as net 0
+        {},                         # empty network
+        {2: [0]},
+        {},                         # equal to net 4
+    ]
+    E = np.stack([_edges_of(g, n) for n in nets])
+    pn, epn, pe = O.parents(E, g, mp)
+    assert list(np.diff(epn)) == [3, 3, 3, 3, 0, 1, 0]
+    # parent list of row 3 in network 0: the first two parents only
+    assert list(pe[epn[0] + pn[0][3]: epn[0] + pn[0][4]]) == [0, 1]
+    uniq = np.zeros(len(nets), np.uint8)
+    U = O.lib().or_unique(len(nets), g, pn, epn, np.ascontiguousarray(pe, np.int32), uniq)
+    assert U == 4
+    assert list(uniq) == [1, 0, 1, 0, 1, 1, 0]
+
+
+def _bdeu_closed_form(child, parent, nprime=4.0):
+    """BDeu of one node from its counts: observed child states r, observed
+    parent configurations q (all combinations of observed parent states)."""
+    from math import lgamma
+    cs = sorted(set(child.tolist()))
+    r = len(cs)
+    if parent is None:
+        confs = [np.ones(len(child), bool)]
+    else:
+        confs = [parent == v for v in sorted(set(parent.tolist()))]
+    q = len(confs)
+    total = 0.0
+    for m in confs:
+        nij = int(m.sum())
+        total += lgamma(nprime / q) - lgamma(nij + nprime / q)
+        for k in cs:
+            nijk = int(((child == k) & m).sum())
+            total += lgamma(nijk + nprime / (q * r)) - lgamma(nprime / (q * r))
+    return total
+
+
+@pytest.mark.parametrize("seed", [0, 1, 2])
+def test_bdeu_closed_form_zero_and_one_parent(seed, oracle_lib):
+    """K5 (kernel5.cu:4-236) for one node with no parent and with one
+    parent against the BDeu closed form with N' = 4."""
+    O = oracle_lib
+    rng = np.random.default_rng(seed)
+    ns = 57
+    d = rng.integers(-1, 2, (2, ns)).astype(np.int8)
+    if seed == 2:
+        d[1][d[1] == 0] = 1  # the parent misses a state: q = 2
+    ppn = np.zeros(2, np.int32)
+    stf = np.zeros(6, np.int32)
+    for i in range(2):
+        for k, v in enumerate((-1, 0, 1)):
+            stf[3 * i + k] = int((d[i] == v).any())
+        ppn[i] = stf[3 * i: 3 * i + 3].sum()
+    dd = np.ascontiguousarray(d)
+    s0 = O.lib().or_bdeu_node(2, ns, dd, ppn, stf, 0, 0, np.zeros(1, np.int32))
+    s1 = O.lib().or_bdeu_node(2, ns, dd, ppn, stf, 0, 1, np.array([1], np.int32))
+    assert abs(s0 - _bdeu_closed_form(d[0], None)) < 1e-10 * abs(s0)
+    assert abs(s1 - _bdeu_closed_form(d[0], d[1])) < 1e-10 * abs(s1)
+
+
+def test_normaliser_branches(oracle_lib):
+    """main.cu:1302-1404: the shifted, scaled log-scores stay <= 10, so for
+    finite scores exp() never overflows and the inf branch is not taken
+    (lval sums to 1); equal scores make the scale 10/0 and give NaN."""
+    O = oracle_lib
+    rng = np.random.default_rng(3)
+    for U in (2, 5, 1000):
+        d = -rng.uniform(1e3, 1e6, U)
+        out = np.zeros(U)
+        O.lib().or_normalise(U, d, out)
+        assert abs(out.sum() - 1.0) < 1e-12 and np.all(np.isfinite(out))
+        assert out.argmax() == d.argmax()
+    out = np.zeros(3)
+    O.lib().or_normalise(3, np.full(3, -42.0), out)
+    assert np.all(np.isnan(out))
