@@ -112,6 +112,14 @@ struct TabInfo {
 
 __device__ __forceinline__ int dof_slot(int dof) { return dof == 1 ? 0 : dof == 2 ? 1 : dof == 4 ? 2 : -1; }
 
+// Hardware reciprocal approximation (relative error a few 1e-8 for normal
+// inputs): every use below sits inside an error budget of >= 1e-5.
+__device__ __forceinline__ float rcp_approx(float x) {
+  float r;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+}
+
 // FP32 chi-square of a 3x3 table: (1/N) sum (|N o - R C| - yN)^2 / (R C),
 // numerators exact in 32-bit integers (tables of N <= 32767 samples; larger
 // ones take the exact FP64 path).  Returns the marginals too.
@@ -146,7 +154,7 @@ __device__ __forceinline__ void table_info(const int *t, TabInfo &ti) {
   // chi = (1/4N) sum_a (1/R_a) sum_b num_ab^2 / C_b: six reciprocals
   float invC[3];
 #pragma unroll
-  for (int b = 0; b < 3; b++) invC[b] = ti.C[b] ? __frcp_rn((float)ti.C[b]) : 0.f;
+  for (int b = 0; b < 3; b++) invC[b] = ti.C[b] ? rcp_approx((float)ti.C[b]) : 0.f;
   float chi = 0.f;
 #pragma unroll
   for (int a = 0; a < 3; a++) {
@@ -162,9 +170,9 @@ __device__ __forceinline__ void table_info(const int *t, TabInfo &ti) {
         row = fmaf(nf * nf, invC[b], row);
       }
     }
-    chi = fmaf(row, __frcp_rn((float)ti.R[a]), chi);
+    chi = fmaf(row, rcp_approx((float)ti.R[a]), chi);
   }
-  ti.chi = (N > 0) ? chi * __frcp_rn(4.f * (float)N) : 0.f;
+  ti.chi = (N > 0) ? chi * rcp_approx(4.f * (float)N) : 0.f;
 }
 
 // 0/1 when certain from the FP32 value, 2 when the exact path must decide.
@@ -212,11 +220,11 @@ __device__ __forceinline__ bool loo_safe(const TabInfo &ti, int prior, const Set
   // fast reciprocals / square roots (a few ulp) with explicit 1e-5 safety
   // factors in the conservative direction
   const float lo = 0.99999f, hi = 1.00001f;
-  const float inv_n1 = __frcp_rn((float)(N - 1));
+  const float inv_n1 = rcp_approx((float)(N - 1));
   const float emin = (float)((rm - 1) * (cm - 1)) * inv_n1 * lo;       // lower bound
-  const float a2 = (15.f * __frcp_rn(emin) + 5.f * inv_n1) * hi;
+  const float a2 = (15.f * rcp_approx(emin) + 5.f * inv_n1) * hi;
   const float A = a2 * rsqrtf(a2) * hi;                                 // sqrt(a2), upper
-  const float ratio = (float)(rm * cm) * __frcp_rn((float)((rm - 1) * (cm - 1))) * hi;
+  const float ratio = (float)(rm * cm) * rcp_approx((float)((rm - 1) * (cm - 1))) * hi;
   const float B = fmaxf(ratio * rsqrtf(ratio) * hi - 1.f, inv_n1 * hi) * 1.001f;
   const float rel = 2e-5f;
   const float xs = ti.chi * (1.f + rel);
@@ -234,14 +242,42 @@ __device__ __forceinline__ bool loo_safe(const TabInfo &ti, int prior, const Set
   return false;
 }
 
-// Decisions of the nine cell-removed tables (the rare path: the filter did
-// not settle them); counts by value so nothing goes through local memory.
-static __device__ __noinline__ uint32_t removed_cell_bits(int a0, int a1, int a2, int a3, int a4,
-                                                          int a5, int a6, int a7, int a8, int bit0,
-                                                          int prior, const SetDev &sd,
-                                                          unsigned &nexact) {
+// Cheap rigorous filter for the common case "no edge in any of the ten
+// tables".  With every marginal >= 2 and every expected count >= 5 in t and
+// in each t' = t - e_ab (support, dof and the Yates flag unchanged), chi^2 =
+// N(Q - 1) with Q = sum o^2/(R C), and o' <= o, R' >= R - 1, C' >= C - 1 give
+// Q' <= rho Q with rho = rm cm / ((rm - 1)(cm - 1)), so
+//   chi^2(t') = (N - 1)(Q' - 1) <= N (rho - 1) + rho chi^2(t).
+// Below the dof's no-edge threshold, all ten decisions are 0.
+__device__ __forceinline__ bool quick_zero(const TabInfo &ti, int prior, const SetDev &sd) {
+  const int N = ti.N, rm = ti.rm, cm = ti.cm;
+  if (sd.exact_all || N < 32 || N > kFastMaxN || rm < 2 || cm < 2) return false;
+  const int ds = dof_slot(ti.dof);
+  if (ds < 0) return false;
+  const int q = (rm - 1) * (cm - 1);  // products < 2^30 for N <= 32767
+  if (q < 5 * (N - 1) || rm * cm < 5 * N) return false;
+  // rho - 1 = (rm + cm - 1) / q; FP32 errors covered by the 1e-4 factors
+  const float r1 = (float)(rm + cm - 1) * rcp_approx((float)q) * 1.0001f;
+  const float xs = ti.chi * (1.f + 2e-5f);
+  const float bound = fmaf((float)N, r1, (1.f + r1) * xs) * 1.0001f + 1e-3f;
+  return bound < sd.thr[prior][ds].chiA;
+}
+
+// The general path: full-table decision, the Minkowski leave-one-out filter
+// and, when that cannot settle them, the nine cell-removed tables one by one.
+// Counts by value and not inlined: it runs for a small share of the tables.
+// Returns the mask in bits 0-9, the number of exact evaluations in bits
+// 32-47 and 1 in bit 48 when the filter settled the table.
+static __device__ __noinline__ uint64_t pair_mask_general(int a0, int a1, int a2, int a3, int a4,
+                                                          int a5, int a6, int a7, int a8,
+                                                          int prior, const SetDev &sd) {
   int t[9] = {a0, a1, a2, a3, a4, a5, a6, a7, a8};
-  uint32_t m = 0;
+  TabInfo ti;
+  unsigned nexact = 0;
+  const int bit0 = decide(t, prior, sd, ti, nexact);
+  if (loo_safe(ti, prior, sd))
+    return (bit0 ? 0x3FFull : 0ull) | ((uint64_t)nexact << 32) | (1ull << 48);
+  uint32_t m = (uint32_t)bit0;
 #pragma unroll 1
   for (int cell = 0; cell < 9; cell++) {
     int bit = bit0;
@@ -253,21 +289,24 @@ static __device__ __noinline__ uint32_t removed_cell_bits(int a0, int a1, int a2
     }
     m |= (uint32_t)bit << (1 + cell);
   }
-  return m;
+  return m | ((uint64_t)nexact << 32);
 }
 
 // 10-bit decision mask of one (pair, class) table: bit 0 = full table,
 // bit 1+3a+b = table with one sample of cell (a,b) removed.
-__device__ __forceinline__ uint32_t pair_mask(int *t, int prior, const SetDev &sd,
+__device__ __forceinline__ uint32_t pair_mask(const int *t, int prior, const SetDev &sd,
                                               unsigned &nexact, unsigned &nfilt) {
   TabInfo ti;
-  const int bit0 = decide(t, prior, sd, ti, nexact);
-  if (loo_safe(ti, prior, sd)) {
+  table_info(t, ti);
+  if (quick_zero(ti, prior, sd)) {
     nfilt++;
-    return bit0 ? 0x3FFu : 0u;
+    return 0u;
   }
-  return (uint32_t)bit0 | removed_cell_bits(t[0], t[1], t[2], t[3], t[4], t[5], t[6], t[7], t[8],
-                                            bit0, prior, sd, nexact);
+  const uint64_t r =
+      pair_mask_general(t[0], t[1], t[2], t[3], t[4], t[5], t[6], t[7], t[8], prior, sd);
+  nexact += (unsigned)(r >> 32) & 0xFFFFu;
+  nfilt += (unsigned)(r >> 48) & 1u;
+  return (uint32_t)r & 0x3FFu;
 }
 
 // --------------------------------------------------- capped parent lists

@@ -138,7 +138,7 @@ __global__ void k_counter_masks(int n, int nA, int W, uint64_t seed, const int32
 }
 
 // ------------------------------------------------------------ k_pairs
-__global__ void __launch_bounds__(128) k_pairs(SetDev sd, const uint64_t *masks, uint32_t *dmask,
+__global__ void __launch_bounds__(128) k_pairs(const __grid_constant__ SetDev sd, const uint64_t *masks, uint32_t *dmask,
                                                unsigned long long *stats) {
   extern __shared__ uint64_t smask[];
   const int u = blockIdx.y;
@@ -411,7 +411,8 @@ __device__ void scores_of(const SetDev &sd, const UnitPtrs &P, int t, int np, co
   }
 }
 
-__global__ void __launch_bounds__(256, 3) k_units(SetDev sd, BatchDev bd) {
+__global__ void __launch_bounds__(256, 3) k_units(const __grid_constant__ SetDev sd,
+                                                 const __grid_constant__ BatchDev bd) {
   extern __shared__ __align__(16) char smraw[];
   UnitSmem &SM = *reinterpret_cast<UnitSmem *>(smraw);
   const int nw = blockDim.x >> 5, lane = threadIdx.x & 31, warp = threadIdx.x >> 5;

@@ -146,7 +146,7 @@ struct MmaSmem {
 template <int kStages, int kEpi, int kMinBlocks>
 __global__ void __launch_bounds__(32 * (2 + kEpi), kMinBlocks)
     k_pairs_mma(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
-                SetDev sd, int B, int nk, int ntiles, int mblocks, uint32_t *dmask,
+                const __grid_constant__ SetDev sd, int B, int nk, int ntiles, int mblocks, uint32_t *dmask,
                 unsigned long long *stats, unsigned *err) {
   extern __shared__ __align__(1024) uint8_t smraw[];
   // 1024-byte aligned stage ring, then barriers, then the epilogue buffer
