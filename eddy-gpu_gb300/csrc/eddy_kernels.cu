@@ -188,7 +188,8 @@ __global__ void __launch_bounds__(128) k_pairs(const __grid_constant__ SetDev sd
 
 // ------------------------------------------------------------ k_units
 struct UnitLayout {
-  size_t phi[2], pcol[2], rec, htk, htv, dist, uid, urep, sig, total;
+  size_t phi[2], pcol[2], rec, htk, htv, dist, uid, urep, sig;
+  size_t skey, sbits, srep, hsk, hsv, wl, total;
   int HT, rec_words;  // rec_words: 64-bit words per network record
 };
 
@@ -219,6 +220,18 @@ __host__ __device__ inline UnitLayout unit_layout(int c, int S, int kmax) {
   L.urep = o;
   o = al(o + sizeof(int32_t) * (size_t)S);
   L.sig = o;  // class-1 samples then class-2 samples, in index order
+  o = al(o + sizeof(int32_t) * (size_t)S);
+  L.skey = o;  // per network: signature key (0 = no flip entry triggered)
+  o = al(o + sizeof(uint64_t) * (size_t)S);
+  L.sbits = o;  // per network: triggered entries as a bitset (<= 64 entries)
+  o = al(o + sizeof(uint64_t) * (size_t)S);
+  L.srep = o;  // per network: first network with the same signature
+  o = al(o + sizeof(int32_t) * (size_t)S);
+  L.hsk = o;  // signature hash table
+  o = al(o + sizeof(uint64_t) * (size_t)HT);
+  L.hsv = o;
+  o = al(o + sizeof(int32_t) * (size_t)HT);
+  L.wl = o;  // work list of networks
   o = al(o + sizeof(int32_t) * (size_t)S);
   L.total = o;
   return L;
@@ -258,6 +271,8 @@ struct UnitSmem {
   int nphi[2];
   int ndab;
   int nrphi[2];
+  int nent[2];  // flip entries per class
+  int nwl;      // work-list length
   int firstB0;  // first class-2 network equal to the class-2 full network
   int repB;     // first occurrence of the class-2 full network
   int scan[32];
@@ -430,6 +445,12 @@ __global__ void __launch_bounds__(256, 3) k_units(const __grid_constant__ SetDev
   int *uid = (int *)(scr + L.uid);
   int *urep = (int *)(scr + L.urep);
   int *sig = (int *)(scr + L.sig);
+  unsigned long long *skey = (unsigned long long *)(scr + L.skey);
+  unsigned long long *sbits = (unsigned long long *)(scr + L.sbits);
+  int *srep = (int *)(scr + L.srep);
+  unsigned long long *hsk = (unsigned long long *)(scr + L.hsk);
+  int *hsv = (int *)(scr + L.hsv);
+  int *wl = (int *)(scr + L.wl);
   const uint32_t *dm = bd.dmask + (size_t)u * c;
   const int tid = threadIdx.x, nt = blockDim.x;
 
@@ -457,6 +478,8 @@ __global__ void __launch_bounds__(256, 3) k_units(const __grid_constant__ SetDev
   for (int i = tid; i < L.HT; i += nt) {
     htk[i] = ~0ull;
     htv[i] = 0x7fffffff;
+    hsk[i] = 0ull;
+    hsv[i] = 0x7fffffff;
   }
   __syncthreads();
   for (int i = tid; i < g * 3; i += nt) {
@@ -558,14 +581,22 @@ __global__ void __launch_bounds__(256, 3) k_units(const __grid_constant__ SetDev
   }
   __syncthreads();
 
-  if (tid == 0) SM.nrphi[0] = SM.nrphi[1] = 0;
-  __syncthreads();
-  for (int i = tid; i < 2 * g; i += nt) {
-    const int k = i / g, t = i % g;
-    if (P.phe[k * g + t] > P.phs[k * g + t]) {
-      int idx = atomicAdd(&SM.nrphi[k], 1);
-      P.rphi[k * g + idx] = (uint16_t)t;
+  // rows holding flip entries, ascending, per class, and entry totals
+  if (tid == 0) SM.nent[0] = SM.nent[1] = 0;
+  for (int k = 0; k < 2; k++) {
+    int running = 0;
+    for (int t0 = 0; t0 < g; t0 += nt) {
+      const int t = t0 + tid;
+      const int ne = (t < g) ? P.phe[k * g + t] - P.phs[k * g + t] : 0;
+      int total;
+      const int off = block_scan(ne > 0 ? 1 : 0, total, SM.scan);
+      if (ne > 0) {
+        P.rphi[k * g + running + off] = (uint16_t)t;
+        atomicAdd(&SM.nent[k], ne);
+      }
+      running += total;
     }
+    if (tid == 0) SM.nrphi[k] = running;
   }
   __syncthreads();
 
@@ -598,28 +629,129 @@ __global__ void __launch_bounds__(256, 3) k_units(const __grid_constant__ SetDev
   }
   __syncthreads();
 
-  // ---- P3: every network as a delta of its class's full network
-  int8_t *myst = P.stsig + (size_t)warp * g;
-  for (int s = warp; s < S; s += nw) {
-    int k, sigma;
-    net_of(s, sd, sig, k, sigma);
-    unsigned long long *R = rec + (size_t)s * L.rec_words;
-    if (sigma < 0) {
-      if (lane == 0) {
-        R[0] = SM.HF[k];
-        R[1] = 0;
-      }
-      continue;
-    }
+  // ---- P3: networks grouped by signature.  The network of left-out sample
+  // sigma is its class's full network with the pair tables of sigma's cells
+  // removed, i.e. the full rows XOR the flip entries that sigma triggers (entry
+  // (t, j, fb) fires when fb holds the bit of sigma's states at t and j).
+  // Samples that trigger the same entries have equal networks, so lists are
+  // generated once per distinct signature.  Signature = additive hash of the
+  // triggered entry ordinals (salted per class; never 0 when non-empty), with
+  // the exact bitset alongside when the class has <= 64 entries.
+  const unsigned long long ksalt0 = mix64(sd.salt ^ 0x243F6A8885A308D3ull);
+  const unsigned long long ksalt1 = mix64(sd.salt ^ 0x13198A2E03707344ull);
+  const int n = sd.n;
+  const int HTs = L.HT;
+  auto class_of = [&](int s) -> int { return (s == 0) ? 0 : (s == S - 1) ? 1 : (s <= sd.nA ? 0 : 1); };
+  // triggered entries of sample sigma in class k: hash (0 when none) and bits
+  auto signature = [&](int k, int sigma, unsigned long long &bits) -> unsigned long long {
     const int nrk = SM.nrphi[k];
-    if (nrk == 0) {
-      // no pair of this class flips for any left-out sample
-      if (lane == 0) {
-        R[0] = SM.HF[k];
-        R[1] = 0;
+    const bool exact = SM.nent[k] <= 64;
+    const unsigned long long ks = k ? ksalt1 : ksalt0;
+    const uint32_t *ph = phi[k];
+    const uint16_t *pc = pcol[k];
+    unsigned long long key = 0;
+    bits = 0;
+    int ord = 0, any = 0;
+    for (int r = 0; r < nrk; r++) {
+      const int t = P.rphi[k * g + r];
+      const int e0 = P.phs[k * g + t], e1 = P.phe[k * g + t];
+      const int a = st_of(sd.vals[(size_t)t * n + sigma]);
+      if (a <= 2) {
+        for (int e = e0; e < e1; e++) {
+          const int b = st_of(sd.vals[(size_t)pc[e] * n + sigma]);
+          if (b <= 2 && ((ph[e] >> (3 * a + b)) & 1u)) {
+            const int o = ord + (e - e0);
+            key += mix64(ks + (unsigned long long)o);
+            if (exact) bits |= 1ull << o;
+            any = 1;
+          }
+        }
       }
-      continue;
+      ord += e1 - e0;
     }
+    return any ? (key | 1ull) : 0ull;
+  };
+  if (tid == 0) {
+    skey[0] = skey[S - 1] = 0ull;
+    sbits[0] = sbits[S - 1] = 0ull;
+    srep[0] = 0;
+    srep[S - 1] = S - 1;
+  }
+  for (int s = 1 + tid; s < S - 1; s += nt) {
+    unsigned long long bits;
+    const unsigned long long key = signature(class_of(s), sig[s - 1], bits);
+    skey[s] = key;
+    sbits[s] = bits;
+    if (key) {
+      unsigned slot = (unsigned)(mix64(key) & (HTs - 1));
+      while (true) {
+        const unsigned long long prev = atomicCAS(&hsk[slot], 0ull, key);
+        if (prev == 0ull || prev == key) {
+          atomicMin(&hsv[slot], s);
+          break;
+        }
+        slot = (slot + 1) & (HTs - 1);
+      }
+    }
+  }
+  if (tid == 0) SM.nwl = 0;
+  __syncthreads();
+  // representatives, the work list of distinct signatures, and an exact check
+  // that every network shares its representative's triggered entries
+  for (int s = 1 + tid; s < S - 1; s += nt) {
+    const unsigned long long key = skey[s];
+    int rep = s;
+    if (key) {
+      unsigned slot = (unsigned)(mix64(key) & (HTs - 1));
+      while (hsk[slot] != key) slot = (slot + 1) & (HTs - 1);
+      rep = hsv[slot];
+      if (rep == s) {
+        wl[atomicAdd(&SM.nwl, 1)] = s;
+      } else {
+        const int k = class_of(s);
+        bool ok = (class_of(rep) == k);
+        if (ok && SM.nent[k] <= 64) {
+          ok = (sbits[s] == sbits[rep]);
+        } else if (ok) {
+          // more than 64 entries: compare the triggered sets entry by entry
+          const int sa = sig[s - 1], sb = sig[rep - 1];
+          const int nrk = SM.nrphi[k];
+          for (int r = 0; ok && r < nrk; r++) {
+            const int t = P.rphi[k * g + r];
+            const int aa = st_of(sd.vals[(size_t)t * n + sa]), ab = st_of(sd.vals[(size_t)t * n + sb]);
+            for (int e = P.phs[k * g + t]; ok && e < P.phe[k * g + t]; e++) {
+              const int j = pcol[k][e];
+              const int ba = st_of(sd.vals[(size_t)j * n + sa]), bb = st_of(sd.vals[(size_t)j * n + sb]);
+              const bool fa = aa <= 2 && ba <= 2 && ((phi[k][e] >> (3 * aa + ba)) & 1u);
+              const bool fbb = ab <= 2 && bb <= 2 && ((phi[k][e] >> (3 * ab + bb)) & 1u);
+              ok = (fa == fbb);
+            }
+          }
+        }
+        if (!ok) atomicOr(&SM.status, kUnitHashCollision);
+      }
+    }
+    srep[s] = rep;
+  }
+  if (tid == 0) {
+    unsigned long long *R0 = rec;
+    unsigned long long *R1 = rec + (size_t)(S - 1) * L.rec_words;
+    R0[0] = SM.HF[0];
+    R0[1] = 0;
+    R1[0] = SM.HF[1];
+    R1[1] = 0;
+  }
+  __syncthreads();
+  // one record per distinct signature: changed nodes (capped list differs
+  // from the full network's) with their lists, and the network hash
+  int8_t *myst = P.stsig + (size_t)warp * g;
+  const int nwl = SM.nwl;
+  for (int wi = warp; wi < nwl; wi += nw) {
+    const int s = wl[wi];
+    const int k = class_of(s);
+    const int sigma = sig[s - 1];
+    unsigned long long *R = rec + (size_t)s * L.rec_words;
+    const int nrk = SM.nrphi[k];
     load_stsig(sd, sigma, myst, lane);
     unsigned long long dh = 0;
     int nchg = 0;
@@ -687,22 +819,28 @@ __global__ void __launch_bounds__(256, 3) k_units(const __grid_constant__ SetDev
     }
     return;
   }
+  // record of any network: the full network's for an empty signature, else
+  // its signature representative's
+  auto rec_of = [&](int s) -> const unsigned long long * {
+    const int r = (s == 0 || s == S - 1) ? s : (skey[s] == 0 ? (class_of(s) ? S - 1 : 0) : srep[s]);
+    return rec + (size_t)r * L.rec_words;
+  };
 
-  // ---- P4: first-occurrence dedup.  A network with no changed node is its
-  // class's full network: class-1 ones duplicate network 0, class-2 ones the
-  // first class-2 network without changes (firstB0), whose own first
-  // occurrence the hash table decides.  Only changed networks and these two
-  // representatives go into the table (no hot key shared by hundreds of
-  // identical networks).
+  // ---- P4: first-occurrence dedup.  Networks without changed nodes are
+  // their class's full network: class-1 ones duplicate network 0, class-2
+  // ones the first class-2 network without changes (firstB0), whose own first
+  // occurrence the hash table decides.  Only network 0, firstB0 and the
+  // signature representatives with changes go into the table.
   const int HT = L.HT;
   if (tid == 0) SM.firstB0 = S - 1;
   __syncthreads();
   for (int s = sd.nA + 1 + tid; s < S - 1; s += nt)
-    if (rec[(size_t)s * L.rec_words + 1] == 0) atomicMin(&SM.firstB0, s);
+    if (rec_of(s)[1] == 0) atomicMin(&SM.firstB0, s);
   __syncthreads();
   const int firstB0 = SM.firstB0;
   auto inserted = [&](int s) -> bool {
-    return s == 0 || s == firstB0 || rec[(size_t)s * L.rec_words + 1] != 0;
+    return s == 0 || s == firstB0 ||
+           (s != S - 1 && skey[s] != 0 && srep[s] == s && rec[(size_t)s * L.rec_words + 1] != 0);
   };
   auto slot_of = [&](unsigned long long key) -> unsigned {
     unsigned slot = (unsigned)(mix64(key) & (HT - 1));
@@ -711,7 +849,7 @@ __global__ void __launch_bounds__(256, 3) k_units(const __grid_constant__ SetDev
   };
   for (int s = tid; s < S; s += nt) {
     if (!inserted(s)) continue;
-    unsigned long long key = rec[(size_t)s * L.rec_words];
+    unsigned long long key = rec_of(s)[0];
     if (key == ~0ull) key ^= 1ull;
     unsigned slot = (unsigned)(mix64(key) & (HT - 1));
     while (true) {
@@ -725,9 +863,10 @@ __global__ void __launch_bounds__(256, 3) k_units(const __grid_constant__ SetDev
   }
   __syncthreads();
   if (tid == 0) {
-    unsigned long long kb = rec[(size_t)firstB0 * L.rec_words];
+    unsigned long long kb = rec_of(firstB0)[0];
     if (kb == ~0ull) kb ^= 1ull;
     SM.repB = htv[slot_of(kb)];
+    SM.nwl = 0;
   }
   __syncthreads();
   const int repB = SM.repB;
@@ -737,14 +876,17 @@ __global__ void __launch_bounds__(256, 3) k_units(const __grid_constant__ SetDev
     int uq = 0;
     int rep = -1;
     if (s < S) {
-      if (inserted(s)) {
-        unsigned long long key = rec[(size_t)s * L.rec_words];
+      const unsigned long long *Rs = rec_of(s);
+      if (Rs[1] == 0) {
+        rep = (class_of(s) == 0) ? 0 : repB;
+      } else {
+        unsigned long long key = Rs[0];
         if (key == ~0ull) key ^= 1ull;
         rep = htv[slot_of(key)];
-      } else {
-        rep = (s <= sd.nA) ? 0 : repB;
       }
       uq = (rep == s) ? 1 : 0;
+      // inserted networks merged by hash are checked list by list below
+      if (rep != s && inserted(s)) wl[atomicAdd(&SM.nwl, 1)] = s;
     }
     int total;
     int off = block_scan(uq, total, SM.scan);
@@ -761,28 +903,25 @@ __global__ void __launch_bounds__(256, 3) k_units(const __grid_constant__ SetDev
   if (tid == 0) SM.U = running;
   __syncthreads();
   const int U = SM.U;
-  // verify every duplicate against its representative (warp per network)
-  for (int s = warp; s < S; s += nw) {
-    int code = uid[s];
-    if (code >= 0) continue;
-    if (!inserted(s)) continue;  // equal to its class's full network by construction
-    const int r = -1 - code;
+  // exact check of every hash merge (warp per merged network)
+  const int nver = SM.nwl;
+  for (int wi = warp; wi < nver; wi += nw) {
+    const int s = wl[wi];
+    const int r = -1 - uid[s];
     int ks, ss, kr, sr;
     net_of(s, sd, sig, ks, ss);
     net_of(r, sd, sig, kr, sr);
-    const unsigned long long *Rs = rec + (size_t)s * L.rec_words;
-    const unsigned long long *Rr = rec + (size_t)r * L.rec_words;
+    const unsigned long long *Rs = rec_of(s);
+    const unsigned long long *Rr = rec_of(r);
     const int ns = (int)Rs[1], nr = (int)Rr[1];
     // both are their class's full network: equal by construction
     if (ks == kr && ns == 0 && nr == 0) continue;
     bool ok = true;
-    // states at both samples, shared by the warp
+    // states at the left-out sample of s, shared by the warp
     load_stsig(sd, ss, myst, lane);
-    int8_t str_local[1];
-    (void)str_local;
     if (ks == kr) {
       if (ns != nr) ok = false;
-      // every changed node of s must be changed in r with an equal list
+      // every changed node of s must be changed in r
       for (int i = lane; ok && i < ns; i += 32) {
         int t = (int)(Rs[2 + i] & 0x3FFF);
         bool found = false;
@@ -792,10 +931,8 @@ __global__ void __launch_bounds__(256, 3) k_units(const __grid_constant__ SetDev
       }
       ok = __all_sync(0xffffffffu, ok);
     }
-    // list comparisons need sigma(r) states too: compare node by node,
-    // generating r's list with its own states loaded into a second buffer
-    // (the neighbouring warp's buffer is not free, so states of r are read
-    // directly from global memory inside a private generator buffer)
+    // node-by-node list comparison: s's lists from the shared states, r's
+    // lists with the states of r's left-out sample read from global memory
     if (ok) {
       // nodes to compare: changed of s, changed of r, and DAB when classes differ
       const int nd = (ks != kr) ? SM.ndab : 0;
@@ -805,15 +942,11 @@ __global__ void __launch_bounds__(256, 3) k_units(const __grid_constant__ SetDev
         if (i < ns) t = (int)(Rs[2 + i] & 0x3FFF);
         else if (i < ns + nr) t = (int)(Rr[2 + (i - ns)] & 0x3FFF);
         else t = P.dab[i - ns - nr];
-        // list of t in s
-        ListGen a, b;
+        ListGen a;
         gen_for(a, sd, P, phi[ks], pcol[ks], ks, t, ss >= 0 ? myst : nullptr);
-        // list of t in r: states of sigma(r) for row t and the columns read
-        // through a private lookup
         const int GWl = sd.GW;
         const int8_t *rT = sd.valsT + (size_t)(sr >= 0 ? sr : 0) * sd.g;
         const int strow_r = (sr >= 0) ? st_of(rT[t]) : 3;
-        // b: manual generator with global-memory states
         const uint32_t *rowr = P.rows + ((size_t)kr * g + t) * GWl;
         int fi = P.phs[kr * g + t], fe = P.phe[kr * g + t];
         int w = 0;
@@ -842,7 +975,6 @@ __global__ void __launch_bounds__(256, 3) k_units(const __grid_constant__ SetDev
             word = rowr[w] ^ flipw(w);
           }
         };
-        (void)b;
         for (int q = 0; q < sd.mp; q++) {
           int x = a.next(), y = nextb();
           if (x != y) { ok = false; break; }
@@ -880,7 +1012,7 @@ __global__ void __launch_bounds__(256, 3) k_units(const __grid_constant__ SetDev
     const int s = urep[uu];
     int k, sigma;
     net_of(s, sd, sig, k, sigma);
-    const unsigned long long *R = rec + (size_t)s * L.rec_words;
+    const unsigned long long *R = rec_of(s);
     const int nchg = (int)R[1];
     long long d0 = SM.base[0][k], d1 = SM.base[1][k];
     for (int i = 0; i < nchg; i++) {
