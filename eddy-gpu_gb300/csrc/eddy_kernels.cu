@@ -392,28 +392,25 @@ __device__ __forceinline__ unsigned long long memo_key(int t, int np, const int 
   return k;
 }
 
-// Scores of (t, parents) for both data classes, memoised per unit.
-__device__ void scores_of(const SetDev &sd, const UnitPtrs &P, int t, int np, const int *ps,
-                          long long out[2]) {
-  const unsigned long long key = memo_key(t, np, ps);
-  unsigned h = (unsigned)(mix64(key) & (kMemo - 1));
+// Memo of node scores per unit: open addressing over kMemo slots, 8 probes;
+// a slot whose values are not yet written counts as a miss.
+__device__ __forceinline__ bool memo_get(const UnitPtrs &P, unsigned h, unsigned long long key,
+                                         long long &a, long long &b) {
   for (int probe = 0; probe < 8; probe++) {
     unsigned slot = (h + probe) & (kMemo - 1);
     unsigned long long kk = P.mkey[slot];
     if (kk == key) {
       __threadfence_block();
-      long long a = P.mval[2 * slot], b = P.mval[2 * slot + 1];
-      if (a != LLONG_MIN && b != LLONG_MIN) {
-        out[0] = a;
-        out[1] = b;
-        return;
-      }
-      break;
+      a = P.mval[2 * slot];
+      b = P.mval[2 * slot + 1];
+      return a != LLONG_MIN && b != LLONG_MIN;
     }
-    if (kk == ~0ull) break;
+    if (kk == ~0ull) return false;
   }
-  out[0] = bdeu_score(sd, t, np, ps, P.mA, P.cnt3);
-  out[1] = bdeu_score(sd, t, np, ps, P.mB, P.cnt3 + 3 * sd.g);
+  return false;
+}
+__device__ __forceinline__ void memo_put(const UnitPtrs &P, unsigned h, unsigned long long key,
+                                         const long long out[2]) {
   for (int probe = 0; probe < 8; probe++) {
     unsigned slot = (h + probe) & (kMemo - 1);
     unsigned long long prev = atomicCAS(&P.mkey[slot], ~0ull, key);
@@ -424,6 +421,27 @@ __device__ void scores_of(const SetDev &sd, const UnitPtrs &P, int t, int np, co
     }
     if (prev == key) return;
   }
+}
+
+// Scores of (t, parents) for both data classes, memoised per unit, one warp
+// per node (np >= 1): lanes share the counting; every lane returns them.
+__device__ void scores_of_warp(const SetDev &sd, const UnitPtrs &P, int t, int np, const int *ps,
+                               long long out[2], int lane) {
+  const unsigned long long key = memo_key(t, np, ps);
+  const unsigned h = (unsigned)(mix64(key) & (kMemo - 1));
+  int hit = 0;
+  long long a = 0, b = 0;
+  if (lane == 0) hit = memo_get(P, h, key, a, b) ? 1 : 0;
+  hit = __shfl_sync(0xffffffffu, hit, 0);
+  if (hit) {
+    out[0] = __shfl_sync(0xffffffffu, a, 0);
+    out[1] = __shfl_sync(0xffffffffu, b, 0);
+    return;
+  }
+  out[0] = bdeu_score_warp(sd, t, np, ps, P.mA, P.cnt3, lane);
+  out[1] = bdeu_score_warp(sd, t, np, ps, P.mB, P.cnt3 + 3 * sd.g, lane);
+  if (lane == 0) memo_put(P, h, key, out);
+  __syncwarp();
 }
 
 __global__ void __launch_bounds__(256, 3) k_units(const __grid_constant__ SetDev sd,
@@ -527,9 +545,11 @@ __global__ void __launch_bounds__(256, 3) k_units(const __grid_constant__ SetDev
   }
 
   // ---- P1: full-network rows and flip lists.  Warp w owns the rows whose
-  // pairs start in [w c/nw, (w+1) c/nw): a 32-lane chunk of a row is one row
-  // bitset word (ballot), and the row's flip entries land, in pair order, in
-  // the warp's own segment of the list (which starts at its first pair).
+  // pairs start in [w c/nw, (w+1) c/nw) and walks their pairs in 32-pair
+  // chunks (loads issued four chunks ahead).  Edge bits go into the row
+  // bitsets; the flip entries land, in pair order, in the warp's own segment
+  // of the list (which starts at its first pair); each row's entry range is
+  // marked by the lanes holding its first and last pair.
   {
     const long long p_lo = (long long)warp * c / nw, p_hi = (long long)(warp + 1) * c / nw;
     int r0, c0;
@@ -542,40 +562,52 @@ __global__ void __launch_bounds__(256, 3) k_units(const __grid_constant__ SetDev
       if (c1 != 0) r1++;
     }
     if (p_lo >= c) r0 = g;
-    int wpos[2];
-    wpos[0] = wpos[1] = (int)((long long)r0 * (r0 - 1) / 2);  // segment = first pair of r0
-    for (int t = r0; t < r1; t++) {
-      const int pbase = t * (t - 1) / 2;
-      if (lane == 0) {
-        P.phs[t] = wpos[0];
-        P.phs[g + t] = wpos[1];
-      }
-      for (int j0 = 0; j0 < t; j0 += 32) {
-        const int j = j0 + lane;
-        const uint32_t m = (j < t) ? dm[pbase + j] : 0u;
-        const uint32_t wa = __ballot_sync(0xffffffffu, m & 1u);
-        const uint32_t wb = __ballot_sync(0xffffffffu, (m >> 16) & 1u);
-        if (lane == 0) {
-          P.rows[((size_t)0 * g + t) * GW + (j0 >> 5)] = wa;
-          P.rows[((size_t)1 * g + t) * GW + (j0 >> 5)] = wb;
-        }
+    if (r0 < 1) r0 = 1;  // row 0 has no pairs
+    const int pa = r0 * (r0 - 1) / 2, pb = r0 < r1 ? r1 * (r1 - 1) / 2 : pa;
+    int wpos0 = pa, wpos1 = pa;
+    int t = 0, j = 0;
+    if (pa + lane < c) pair_rc(pa + lane, t, j);
+    constexpr int kAhead = 4;
+    uint32_t buf[kAhead];
 #pragma unroll
-        for (int cls = 0; cls < 2; cls++) {
-          const uint32_t mm = (m >> (16 * cls)) & 0x3FFu;
-          const uint32_t fb = (mm >> 1) ^ ((mm & 1u) ? 0x1FFu : 0u);
-          const bool flag = (j < t) && fb != 0u;
-          const uint32_t bal = __ballot_sync(0xffffffffu, flag);
-          if (flag) {
-            const int idx = wpos[cls] + __popc(bal & ((1u << lane) - 1u));
-            phi[cls][idx] = ((uint32_t)(pbase + j) << 9) | fb;
-            pcol[cls][idx] = (uint16_t)j;
-          }
-          wpos[cls] += __popc(bal);
-        }
+    for (int d = 0; d < kAhead; d++) {
+      const int p = pa + 32 * d + lane;
+      buf[d] = (p < pb) ? dm[p] : 0u;
+    }
+    const uint32_t below = (1u << lane) - 1u;
+    for (int base = pa; base < pb; base += 32) {
+      const uint32_t m = buf[0];
+#pragma unroll
+      for (int d = 0; d < kAhead - 1; d++) buf[d] = buf[d + 1];
+      {
+        const int p = base + 32 * kAhead + lane;
+        buf[kAhead - 1] = (p < pb) ? dm[p] : 0u;
       }
-      if (lane == 0) {
-        P.phe[t] = wpos[0];
-        P.phe[g + t] = wpos[1];
+      const bool in = base + lane < pb;
+      if (in && (m & 1u)) atomicOr(&P.rows[((size_t)0 * g + t) * GW + (j >> 5)], 1u << (j & 31));
+      if (in && ((m >> 16) & 1u))
+        atomicOr(&P.rows[((size_t)1 * g + t) * GW + (j >> 5)], 1u << (j & 31));
+#pragma unroll
+      for (int cls = 0; cls < 2; cls++) {
+        const uint32_t mm = (m >> (16 * cls)) & 0x3FFu;
+        const uint32_t fb = (mm >> 1) ^ ((mm & 1u) ? 0x1FFu : 0u);
+        const bool flag = in && fb != 0u;
+        const uint32_t bal = __ballot_sync(0xffffffffu, flag);
+        const int wpos = cls ? wpos1 : wpos0;
+        const int before = wpos + __popc(bal & below);
+        if (flag) {
+          phi[cls][before] = ((uint32_t)(base + lane) << 9) | fb;
+          pcol[cls][before] = (uint16_t)j;
+        }
+        if (in && j == 0) P.phs[cls * g + t] = before;
+        if (in && j == t - 1) P.phe[cls * g + t] = before + (flag ? 1 : 0);
+        if (cls) wpos1 += __popc(bal); else wpos0 += __popc(bal);
+      }
+      // this lane's next pair: 32 further on
+      j += 32;
+      while (t < g && j >= t) {
+        j -= t;
+        t++;
       }
     }
   }
@@ -989,15 +1021,30 @@ __global__ void __launch_bounds__(256, 3) k_units(const __grid_constant__ SetDev
   __syncthreads();
   if (bd.stats && tid == 0) atomicAdd(&bd.stats[3], (unsigned long long)(S - U));
 
-  // ---- P5: BDeu.  Base node scores of the two full networks.
+  // ---- P5: BDeu.  Base node scores of the two full networks: nodes
+  // without parents thread by thread (from the state counts), the others
+  // warp by warp.
   for (int i = tid; i < 2 * g; i += nt) {
+    if (P.fcnt[i] != 0) continue;
+    const int k = i / g, t = i % g;
+    int ps[3] = {0xFFFF, 0xFFFF, 0xFFFF};
+    long long sc[2];
+    sc[0] = bdeu_score(sd, t, 0, ps, P.mA, P.cnt3);
+    sc[1] = bdeu_score(sd, t, 0, ps, P.mB, P.cnt3 + 3 * g);
+    P.fsc[(k * 2 + 0) * g + t] = sc[0];
+    P.fsc[(k * 2 + 1) * g + t] = sc[1];
+  }
+  for (int i = warp; i < 2 * g; i += nw) {
+    if (P.fcnt[i] == 0) continue;
     const int k = i / g, t = i % g;
     int np = P.fcnt[i] < 3 ? P.fcnt[i] : 3;
     int ps[3] = {P.fps[i * 3], P.fps[i * 3 + 1], P.fps[i * 3 + 2]};
     long long sc[2];
-    scores_of(sd, P, t, np, ps, sc);
-    P.fsc[(k * 2 + 0) * g + t] = sc[0];
-    P.fsc[(k * 2 + 1) * g + t] = sc[1];
+    scores_of_warp(sd, P, t, np, ps, sc, lane);
+    if (lane == 0) {
+      P.fsc[(k * 2 + 0) * g + t] = sc[0];
+      P.fsc[(k * 2 + 1) * g + t] = sc[1];
+    }
   }
   __syncthreads();
   for (int i = tid; i < 4; i += nt) {
@@ -1007,8 +1054,8 @@ __global__ void __launch_bounds__(256, 3) k_units(const __grid_constant__ SetDev
     SM.base[cls][k] = s;
   }
   __syncthreads();
-  // per unique network: base + deltas of its changed nodes
-  for (int uu = tid; uu < U; uu += nt) {
+  // per unique network (warp by warp): base + deltas of its changed nodes
+  for (int uu = warp; uu < U; uu += nw) {
     const int s = urep[uu];
     int k, sigma;
     net_of(s, sd, sig, k, sigma);
@@ -1025,12 +1072,19 @@ __global__ void __launch_bounds__(256, 3) k_units(const __grid_constant__ SetDev
       for (int q = 0; same && q < np; q++) same = (ps[q] == (int)P.fps[(k * g + t) * 3 + q]);
       if (same) continue;
       long long sc[2];
-      scores_of(sd, P, t, np, ps, sc);
+      if (np == 0) {
+        sc[0] = bdeu_score(sd, t, 0, ps, P.mA, P.cnt3);
+        sc[1] = bdeu_score(sd, t, 0, ps, P.mB, P.cnt3 + 3 * g);
+      } else {
+        scores_of_warp(sd, P, t, np, ps, sc, lane);
+      }
       d0 += sc[0] - P.fsc[(k * 2 + 0) * g + t];
       d1 += sc[1] - P.fsc[(k * 2 + 1) * g + t];
     }
-    dist[uu] = d0;
-    dist[S + uu] = d1;
+    if (lane == 0) {
+      dist[uu] = d0;
+      dist[S + uu] = d1;
+    }
   }
   __syncthreads();
 
