@@ -36,6 +36,10 @@ constexpr int kTM = 128, kTN = 128, kGroups = 4, kPairsPerGroup = 3, kKC = 128;
 constexpr int kPairsPerTile = kGroups * kPairsPerGroup;
 constexpr uint32_t kStageBytes = (kTM + kTN) * kKC;  // 32 KB
 constexpr unsigned long long kTimeoutNs = 2000000000ull;
+// general-path queue of an epilogue warp: room for every table of its tile
+// share (32 units x 12 pairs x 2 classes / warps of a quadrant), 6 words each
+constexpr int kQWords = 6;
+constexpr uint32_t kBarBytes = 1024;  // barrier block after the stage ring
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p) {
   return (uint32_t)__cvta_generic_to_shared(p);
@@ -138,6 +142,7 @@ struct MmaSmem {
   unsigned long long full[kStages], empty[kStages], accfull[2], accempty[2];
   uint32_t tmem_base;
 };
+static_assert(sizeof(MmaSmem<8>) <= kBarBytes, "barrier block");
 
 // kStages: depth of the TMA ring; kEpi: epilogue warps (8 or 16);
 // kMinBlocks: CTAs per SM the register budget is sized for (two CTAs share
@@ -146,8 +151,10 @@ struct MmaSmem {
 template <int kStages, int kEpi, int kMinBlocks>
 __global__ void __launch_bounds__(32 * (2 + kEpi), kMinBlocks)
     k_pairs_mma(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
-                const __grid_constant__ SetDev sd, int B, int nk, int ntiles, int mblocks, uint32_t *dmask,
-                unsigned long long *stats, unsigned *err) {
+                const __grid_constant__ SetDev sd, const float *__restrict__ ctotf, int B, int nk,
+                int ntiles, int mblocks, uint32_t *dmask, unsigned long long *stats,
+                unsigned *err) {
+  constexpr int kQCap = 32 * 2 * kPairsPerGroup * (kGroups / (kEpi / 4));
   extern __shared__ __align__(1024) uint8_t smraw[];
   // 1024-byte aligned stage ring, then barriers, then the epilogue buffer
   uint8_t *base = (uint8_t *)(((uintptr_t)smraw + 1023) & ~(uintptr_t)1023);
@@ -241,23 +248,25 @@ __global__ void __launch_bounds__(32 * (2 + kEpi), kMinBlocks)
     int acc = 0;
     uint32_t accphase = 0;
     unsigned nexact = 0, nfilt = 0, ntab = 0;
+    // no-edge thresholds of dof 4 without / with a prior (quick_zero_f)
+    const float thr0 = sd.exact_all ? -1.f : sd.thr[0][2].chiA;
+    const float thr1 = sd.exact_all ? -1.f : sd.thr[1][2].chiA;
+    const uint32_t below = (1u << lane) - 1u;
+    // this warp's queue of tables for the general path
+    uint32_t *gq = reinterpret_cast<uint32_t *>(base + kStages * kStageBytes + kBarBytes) +
+                   (size_t)(warp - 2) * kQCap * kQWords;
     for (int t = blockIdx.x; t < ntot && !*verr; t += gridDim.x) {
       const int tn = t / mblocks, mb = t % mblocks;
       if (!mbar_wait(smem_u32(&S.accfull[acc]), accphase, verr)) break;
       tc_fence_after();
-      // counts of the warp's group(s), packed two u16 per register
-      uint32_t pk[kGpw][14];
+      // counts of the warp's group(s): FP32 integers straight from TMEM
+      uint32_t r[kGpw][32];
 #pragma unroll
       for (int gi = 0; gi < kGpw; gi++) {
         const int grp = wq + gi * kPerQuad;
-        uint32_t r[32];
-        tmem_ld32(tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)(acc * kTN + grp * 32), r);
-        tmem_ld_wait();
-#pragma unroll
-        for (int i = 0; i < 14; i++)
-          pk[gi][i] = __float2uint_rn(__uint_as_float(r[2 * i])) |
-                      (__float2uint_rn(__uint_as_float(r[2 * i + 1])) << 16);
+        tmem_ld32(tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)(acc * kTN + grp * 32), r[gi]);
       }
+      tmem_ld_wait();
       tc_fence_before();
       mbar_arrive(smem_u32(&S.accempty[acc]));
       if (++acc == 2) {
@@ -265,41 +274,68 @@ __global__ void __launch_bounds__(32 * (2 + kEpi), kMinBlocks)
         accphase ^= 1u;
       }
       const int u = mb * kTM + row;
-      if (u < B) {
-        // rolled loop over the warp's pairs; a pair's nine counts are picked
-        // out of the packed registers by selects (no dynamic register index)
-#pragma unroll 1
-        for (int j = 0; j < kGpw * kPairsPerGroup; j++) {
-          const int gi = j / kPairsPerGroup, q = j % kPairsPerGroup;
-          const int grp = wq + gi * kPerQuad;
+      const bool valid = u < B;
+      // tables the quick filter cannot settle are queued (counts, class,
+      // prior, pair, row) and decided after the loop, with the TMEM values
+      // no longer live
+      int nq = 0;
+      auto enqueue = [&](bool flag, const float *o, int cls, int prior, int p) {
+        const uint32_t bal = __ballot_sync(0xffffffffu, flag);
+        if (flag) {
+          uint32_t *it = gq + (size_t)(nq + __popc(bal & below)) * kQWords;
+          it[0] = (uint32_t)o[0] | ((uint32_t)o[1] << 16);
+          it[1] = (uint32_t)o[2] | ((uint32_t)o[3] << 16);
+          it[2] = (uint32_t)o[4] | ((uint32_t)o[5] << 16);
+          it[3] = (uint32_t)o[6] | ((uint32_t)o[7] << 16);
+          it[4] = (uint32_t)o[8] | ((uint32_t)row << 16) | ((uint32_t)cls << 24) |
+                  ((uint32_t)prior << 25);
+          it[5] = (uint32_t)p;
+        }
+        nq += __popc(bal);
+      };
+#pragma unroll
+      for (int gi = 0; gi < kGpw; gi++) {
+        const int grp = wq + gi * kPerQuad;
+#pragma unroll
+        for (int q = 0; q < kPairsPerGroup; q++) {
           const int p = tn * kPairsPerTile + grp * kPairsPerGroup + q;
           if (p >= sd.c) continue;
-          int tA[9], tB[9];
-          const uint16_t *ct = sd.ctot + (size_t)p * 9;
+          // full-sample table (nine counts) and the prior flag of pair p
+          const float4 *cf = reinterpret_cast<const float4 *>(ctotf + (size_t)p * 12);
+          const float4 f0 = cf[0], f1 = cf[1], f2 = cf[2];
+          float oA[9], oB[9];
 #pragma unroll
-          for (int k = 0; k < 9; k++) {
-            // cell k of pair q sits at column 9q + k of the group
-            uint32_t v0 = (pk[0][k >> 1] >> (16 * (k & 1))) & 0xFFFFu;
-            uint32_t v1 = (pk[0][(9 + k) >> 1] >> (16 * ((9 + k) & 1))) & 0xFFFFu;
-            uint32_t v2 = (pk[0][(18 + k) >> 1] >> (16 * ((18 + k) & 1))) & 0xFFFFu;
-            uint32_t v = (q == 0) ? v0 : (q == 1) ? v1 : v2;
-            if (kGpw > 1) {
-              uint32_t w0 = (pk[kGpw - 1][k >> 1] >> (16 * (k & 1))) & 0xFFFFu;
-              uint32_t w1 = (pk[kGpw - 1][(9 + k) >> 1] >> (16 * ((9 + k) & 1))) & 0xFFFFu;
-              uint32_t w2 = (pk[kGpw - 1][(18 + k) >> 1] >> (16 * ((18 + k) & 1))) & 0xFFFFu;
-              const uint32_t w = (q == 0) ? w0 : (q == 1) ? w1 : w2;
-              v = gi ? w : v;
-            }
-            tA[k] = (int)v;
-            tB[k] = (int)ct[k] - tA[k];
+          for (int k = 0; k < 9; k++) oA[k] = __uint_as_float(r[gi][9 * q + k]);
+          oB[0] = f0.x - oA[0]; oB[1] = f0.y - oA[1]; oB[2] = f0.z - oA[2];
+          oB[3] = f0.w - oA[3]; oB[4] = f1.x - oA[4]; oB[5] = f1.y - oA[5];
+          oB[6] = f1.z - oA[6]; oB[7] = f1.w - oA[7]; oB[8] = f2.x - oA[8];
+          const int prior = (f2.y != 0.f) ? 1 : 0;
+          const float chiA = prior ? thr1 : thr0;
+          const bool qa = quick_zero_f(oA, chiA), qb = quick_zero_f(oB, chiA);
+          enqueue(valid && !qa, oA, 0, prior, p);
+          enqueue(valid && !qb, oB, 1, prior, p);
+          if (valid) {
+            dmask[(size_t)u * sd.c + p] = 0u;
+            nfilt += (unsigned)qa + (unsigned)qb;
+            ntab += 2;
           }
-          const int prior = sd.prior[p] ? 1 : 0;
-          const uint32_t mA = pair_mask(tA, prior, sd, nexact, nfilt);
-          const uint32_t mB = pair_mask(tB, prior, sd, nexact, nfilt);
-          dmask[(size_t)u * sd.c + p] = mA | (mB << 16);
-          ntab += 2;
         }
       }
+      __syncwarp();
+      for (int i = lane; i < nq; i += 32) {
+        const uint32_t *it = gq + (size_t)i * kQWords;
+        const int cls = (it[4] >> 24) & 1, prior = (it[4] >> 25) & 1;
+        const int uu = mb * kTM + (int)((it[4] >> 16) & 0xFFu), p = (int)it[5];
+        const uint64_t rr = pair_mask_general(
+            (int)(it[0] & 0xFFFFu), (int)(it[0] >> 16), (int)(it[1] & 0xFFFFu), (int)(it[1] >> 16),
+            (int)(it[2] & 0xFFFFu), (int)(it[2] >> 16), (int)(it[3] & 0xFFFFu), (int)(it[3] >> 16),
+            (int)(it[4] & 0xFFFFu), prior, sd);
+        const uint32_t m = (uint32_t)rr & 0x3FFu;
+        if (m) atomicOr(&dmask[(size_t)uu * sd.c + p], m << (16 * cls));
+        nexact += (unsigned)(rr >> 32) & 0xFFFFu;
+        nfilt += (unsigned)(rr >> 48) & 1u;
+      }
+      __syncwarp();
     }
     if (stats) {
       for (int o = 16; o > 0; o >>= 1) {
@@ -358,6 +394,22 @@ __global__ void k_build_y(const uint64_t *planes, int g, int W, int c, int n_pad
   *reinterpret_cast<uint4 *>(Y + (size_t)rr * n_pad + ch * 16) = o;
 }
 
+// Full-sample tables as FP32 for the epilogue: pair p -> 12 floats (nine
+// counts, the prior flag, two pad), 48 bytes, float4-aligned.
+__global__ void k_ctot_f(const uint16_t *ctot, const uint8_t *prior, int c, float *out) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= c) return;
+  float v[12];
+#pragma unroll
+  for (int k = 0; k < 9; k++) v[k] = (float)ctot[(size_t)p * 9 + k];
+  v[9] = prior[p] ? 1.f : 0.f;
+  v[10] = v[11] = 0.f;
+  float4 *o = reinterpret_cast<float4 *>(out + (size_t)p * 12);
+  o[0] = make_float4(v[0], v[1], v[2], v[3]);
+  o[1] = make_float4(v[4], v[5], v[6], v[7]);
+  o[2] = make_float4(v[8], v[9], v[10], v[11]);
+}
+
 // A: row u = class-1 mask of unit u over the samples, e4m3 0/1; rows >= B zero.
 __global__ void k_masks_fp8(const uint64_t *masks, int B, int B_pad, int W, int n_pad, uint8_t *A) {
   const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -408,28 +460,37 @@ static bool make_map(CUtensorMap *m, void *ptr, int cols, int rows) {
 
 int mma_ntiles(int c) { return (c + kPairsPerTile - 1) / kPairsPerTile; }
 int mma_npad(int n) { return (n + kKC - 1) / kKC * kKC; }
-size_t mma_y_bytes(int c, int n) { return (size_t)mma_ntiles(c) * kTN * mma_npad(n); }
+// the operand Y, then the FP32 full-sample tables (a multiple of 128 bytes in)
+static size_t y_operand_bytes(int c, int n) { return (size_t)mma_ntiles(c) * kTN * mma_npad(n); }
+size_t mma_y_bytes(int c, int n) { return y_operand_bytes(c, n) + 48 * (size_t)(c > 0 ? c : 1); }
 int mma_bpad(int B) { return (B + kTM - 1) / kTM * kTM; }
 
 cudaError_t launch_build_y(const SetDev &sd, uint8_t *Y, cudaStream_t st) {
   const int nt = mma_ntiles(sd.c), np = mma_npad(sd.n);
   const long long work = (long long)nt * kTN * (np / 16);
   k_build_y<<<(unsigned)((work + 255) / 256), 256, 0, st>>>(sd.planes, sd.g, sd.W, sd.c, np, nt, Y);
+  if (sd.c > 0)
+    k_ctot_f<<<(sd.c + 255) / 256, 256, 0, st>>>(sd.ctot, sd.prior, sd.c,
+                                                  (float *)(Y + y_operand_bytes(sd.c, sd.n)));
   return cudaGetLastError();
 }
 
 template <int kStages, int kEpi, int kMinBlocks>
 static cudaError_t launch_variant(const CUtensorMap &ma, const CUtensorMap &mb, const SetDev &sd,
-                                  int B, int np, int nt, int mblocks, uint32_t *dmask,
+                                  const float *ctotf, int B, int np, int nt, int mblocks,
+                                  uint32_t *dmask,
                                   unsigned long long *stats, unsigned *err, int sms,
                                   cudaStream_t st) {
-  const size_t smem = 1024 + kStages * kStageBytes + 1024;
+  constexpr int kQCap = 32 * 2 * kPairsPerGroup * (kGroups / (kEpi / 4));
+  const size_t smem = 1024 + kStages * kStageBytes + kBarBytes +
+                      (size_t)kEpi * kQCap * kQWords * sizeof(uint32_t);
   auto kern = k_pairs_mma<kStages, kEpi, kMinBlocks>;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   const int ntot = nt * mblocks;
   const int grid = ntot < sms * kMinBlocks ? ntot : sms * kMinBlocks;
-  kern<<<grid, 32 * (2 + kEpi), smem, st>>>(ma, mb, sd, B, np / kKC, nt, mblocks, dmask, stats, err);
+  kern<<<grid, 32 * (2 + kEpi), smem, st>>>(ma, mb, sd, ctotf, B, np / kKC, nt, mblocks, dmask,
+                                            stats, err);
   return cudaGetLastError();
 }
 
@@ -445,9 +506,12 @@ cudaError_t launch_pairs_mma(const SetDev &sd, const uint64_t *masks, int B, uin
   if (!make_map(&ma, Afp8, np, Bp) || !make_map(&mb, (void *)Y, np, nt * kTN))
     return cudaErrorNotSupported;
   const int mblocks = Bp / kTM;
+  const float *ctotf = (const float *)(Y + y_operand_bytes(sd.c, sd.n));
   if (variant == 1)
-    return launch_variant<4, 8, 1>(ma, mb, sd, B, np, nt, mblocks, dmask, stats, err, sms, st);
-  return launch_variant<4, 16, 1>(ma, mb, sd, B, np, nt, mblocks, dmask, stats, err, sms, st);
+    return launch_variant<4, 8, 1>(ma, mb, sd, ctotf, B, np, nt, mblocks, dmask, stats, err, sms,
+                                   st);
+  return launch_variant<4, 16, 1>(ma, mb, sd, ctotf, B, np, nt, mblocks, dmask, stats, err, sms,
+                                  st);
 }
 
 }  // namespace eddy

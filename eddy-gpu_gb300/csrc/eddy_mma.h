@@ -11,7 +11,8 @@ int mma_ntiles(int c);
 int mma_npad(int n);
 int mma_bpad(int B);
 size_t mma_y_bytes(int c, int n);
-// Builds the pair-cell indicator operand Y of the current set.
+// Builds the pair-cell indicator operand Y of the current set and, after it,
+// the FP32 copy of the full-sample tables the epilogue reads.
 cudaError_t launch_build_y(const SetDev &sd, uint8_t *Y, cudaStream_t st);
 // Masks -> e4m3 operand (Afp8, mma_bpad(B) x mma_npad(n) bytes), then the
 // GEMM + decision kernel; *err is set on a bounded-wait timeout.
