@@ -493,11 +493,14 @@ __global__ void __launch_bounds__(256, 3) k_units(const __grid_constant__ SetDev
     P.mval[2 * i] = LLONG_MIN;
     P.mval[2 * i + 1] = LLONG_MIN;
   }
-  for (int i = tid; i < L.HT; i += nt) {
-    htk[i] = ~0ull;
-    htv[i] = 0x7fffffff;
-    hsk[i] = 0ull;
-    hsv[i] = 0x7fffffff;
+  // hash tables, 16 bytes per store (HT is a power of two >= 8)
+  for (int i = tid; i < L.HT / 2; i += nt) {
+    reinterpret_cast<uint4 *>(htk)[i] = make_uint4(~0u, ~0u, ~0u, ~0u);
+    reinterpret_cast<uint4 *>(hsk)[i] = make_uint4(0u, 0u, 0u, 0u);
+  }
+  for (int i = tid; i < L.HT / 4; i += nt) {
+    reinterpret_cast<uint4 *>(htv)[i] = make_uint4(0x7fffffffu, 0x7fffffffu, 0x7fffffffu, 0x7fffffffu);
+    reinterpret_cast<uint4 *>(hsv)[i] = make_uint4(0x7fffffffu, 0x7fffffffu, 0x7fffffffu, 0x7fffffffu);
   }
   __syncthreads();
   for (int i = tid; i < g * 3; i += nt) {
@@ -530,18 +533,14 @@ __global__ void __launch_bounds__(256, 3) k_units(const __grid_constant__ SetDev
   }
 
   __syncthreads();
-  // sample lists of both classes in index order (network -> left-out sample)
-  for (int w = tid; w < W; w += nt) {
-    uint64_t a = P.mA[w], b = P.mB[w];
-    int ia = P.pcA[w], ib = sd.nA + P.pcB[w];
-    while (a) {
-      sig[ia++] = w * 64 + (__ffsll((long long)a) - 1);
-      a &= a - 1;
-    }
-    while (b) {
-      sig[ib++] = w * 64 + (__ffsll((long long)b) - 1);
-      b &= b - 1;
-    }
+  // sample lists of both classes in index order (network -> left-out
+  // sample): thread per sample bit
+  for (int i = tid; i < 64 * W; i += nt) {
+    const int w = i >> 6, bit = i & 63;
+    const uint64_t below64 = (bit ? (~0ull >> (64 - bit)) : 0ull);
+    const uint64_t a = P.mA[w], b = P.mB[w];
+    if ((a >> bit) & 1ull) sig[P.pcA[w] + __popcll(a & below64)] = i;
+    else if ((b >> bit) & 1ull) sig[sd.nA + P.pcB[w] + __popcll(b & below64)] = i;
   }
 
   // ---- P1: full-network rows and flip lists.  Warp w owns the rows whose
@@ -575,13 +574,17 @@ __global__ void __launch_bounds__(256, 3) k_units(const __grid_constant__ SetDev
       buf[d] = (p < pb) ? dm[p] : 0u;
     }
     const uint32_t below = (1u << lane) - 1u;
-    for (int base = pa; base < pb; base += 32) {
-      const uint32_t m = buf[0];
+    // unrolled by the prefetch depth: slot d is consumed and refilled with
+    // the chunk kAhead further on, so no register waits on a pending load
+    for (int base0 = pa; base0 < pb; base0 += 32 * kAhead)
 #pragma unroll
-      for (int d = 0; d < kAhead - 1; d++) buf[d] = buf[d + 1];
+    for (int d = 0; d < kAhead; d++) {
+      const int base = base0 + 32 * d;
+      if (base >= pb) break;
+      const uint32_t m = buf[d];
       {
         const int p = base + 32 * kAhead + lane;
-        buf[kAhead - 1] = (p < pb) ? dm[p] : 0u;
+        buf[d] = (p < pb) ? dm[p] : 0u;
       }
       const bool in = base + lane < pb;
       if (in && (m & 1u)) atomicOr(&P.rows[((size_t)0 * g + t) * GW + (j >> 5)], 1u << (j & 31));
@@ -1089,8 +1092,59 @@ __global__ void __launch_bounds__(256, 3) k_units(const __grid_constant__ SetDev
   __syncthreads();
 
   // ---- P6: normalisation (main.cu:1302-1404) and JS (main.cu:1406-1428),
-  // both classes per reduction pass
+  // both classes per reduction pass; one warp with shuffles when U <= 32
   const int keep = bd.keep_slot ? bd.keep_slot[u] : -1;
+  if (U <= 32) {
+    if (warp == 0) {
+      const bool on = lane < U;
+      const long long a = on ? dist[lane] : 0, b = on ? dist[S + lane] : 0;
+      long long l0 = on ? a : LLONG_MAX, h0 = on ? a : LLONG_MIN;
+      long long l1 = on ? b : LLONG_MAX, h1 = on ? b : LLONG_MIN;
+      for (int o = 16; o > 0; o >>= 1) {
+        long long x;
+        x = __shfl_xor_sync(0xffffffffu, l0, o); l0 = x < l0 ? x : l0;
+        x = __shfl_xor_sync(0xffffffffu, h0, o); h0 = x > h0 ? x : h0;
+        x = __shfl_xor_sync(0xffffffffu, l1, o); l1 = x < l1 ? x : l1;
+        x = __shfl_xor_sync(0xffffffffu, h1, o); h1 = x > h1 ? x : h1;
+      }
+      const double da = on ? (double)(a - l0) : 0.0, db = on ? (double)(b - l1) : 0.0;
+      double s0 = da, s1 = db;
+      for (int o = 16; o > 0; o >>= 1) {
+        s0 += __shfl_xor_sync(0xffffffffu, s0, o);
+        s1 += __shfl_xor_sync(0xffffffffu, s1, o);
+      }
+      const double m0 = s0 / (double)U, m1 = s1 / (double)U;
+      const double sA = 10.0 / (double)(h0 - l0), sB = 10.0 / (double)(h1 - l1);
+      const double xa = on ? exp((da - m0) * sA) : 0.0, xb = on ? exp((db - m1) * sB) : 0.0;
+      double e0 = xa, e1 = xb;
+      for (int o = 16; o > 0; o >>= 1) {
+        e0 += __shfl_xor_sync(0xffffffffu, e0, o);
+        e1 += __shfl_xor_sync(0xffffffffu, e1, o);
+      }
+      double ls = 0.0;
+      if (on) {
+        const double Pu = xa / e0, Qu = xb / e1;
+        const double M = (Pu + Qu) / 2;
+        if (M != 0) {
+          if (Pu != 0) ls += 0.5 * (Pu * log(Pu / M));
+          if (Qu != 0) ls += 0.5 * (Qu * log(Qu / M));
+        }
+        if (keep >= 0) {
+          bd.out_lval[((size_t)keep * 2 + 0) * S + lane] = Pu;
+          bd.out_lval[((size_t)keep * 2 + 1) * S + lane] = Qu;
+        }
+      }
+      for (int o = 16; o > 0; o >>= 1) ls += __shfl_xor_sync(0xffffffffu, ls, o);
+      if (lane == 0) {
+        double js = ls / log(2.0);
+        if (h0 == l0 || h1 == l1) js = __longlong_as_double(0x7ff8000000000000ll);
+        bd.js[u] = js;
+        bd.U[u] = U;
+        bd.status[u] = SM.status;
+      }
+    }
+  } else {
+
   double js = 0.0;
   long long mn[2], mx[2];
   double mean[2], esum[2];
@@ -1209,6 +1263,7 @@ __global__ void __launch_bounds__(256, 3) k_units(const __grid_constant__ SetDev
       bd.U[u] = U;
       bd.status[u] = SM.status;
     }
+  }
   }
 
   // ---- P7: detailed outputs of kept units
