@@ -247,7 +247,7 @@ int launch_pairs_any(eddy_ctx *ctx, const SetDev &sd, const uint64_t *masks, int
     ctx->launches += 1;
     ctx->y_ready = true;
   }
-  CK(ctx->d_afp8.ensure((size_t)mma_bpad(B) * mma_npad(sd.n)));
+  CK(ctx->d_afp8.ensure(mma_a_bytes(B, sd.n, ctx->sms)));
   CK(ctx->d_err.ensure(sizeof(unsigned)));
   CK(cudaMemsetAsync(ctx->d_err.p, 0, sizeof(unsigned), ctx->stream));
   int variant = 0;

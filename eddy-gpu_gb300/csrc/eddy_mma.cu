@@ -11,16 +11,18 @@
 // of TMEM and makes the 10-bit leave-one-out decision masks of both classes
 // (kernel1.cu:121-203, 419-431) in the same kernel.
 //
-// Tile: 128 units (TMEM lanes) x 128 pair-cells (four 32-column groups, each
-// 3 pairs x 9 cells + 5 pad columns) x K in 128-sample chunks; operands
-// staged by TMA (cp.async.bulk.tensor, 128B swizzle) through an mbarrier
-// ring.  Warp roles: 0 = TMA producer, 1 = TMEM owner + MMA issuer, 2.. =
-// epilogue warps (kEpi of them; each owns one TMEM lane quadrant and one or
-// two column groups, reads them with one tcgen05.ld each and decides their
-// pairs from registers).  Accumulators are double-buffered (2 x 128 TMEM
-// columns).  Every mbarrier wait is
+// Tile: 128 units (TMEM lanes) x kGroups column groups of 32 pair-cells
+// (3 pairs x 9 cells + 5 pad columns; N = 128, 192 or 256) x K in
+// 128-sample chunks; operands staged by TMA (cp.async.bulk.tensor, 128B
+// swizzle) through an mbarrier ring.  Warp roles: 0 = TMA producer, 1 =
+// TMEM owner + MMA issuer (it also stages each tile's full-sample tables
+// into shared memory with cp.async.bulk), 2.. = epilogue warps (kEpi of
+// them; each owns one TMEM lane quadrant and kGroups / (kEpi / 4) column
+// groups, reads them with tcgen05.ld and decides their pairs from
+// registers).  Accumulators are double-buffered.  Every mbarrier wait is
 // bounded (2 s on %globaltimer); a timeout sets an error word, every role
-// drains, and TMEM is released before the block exits.
+// drains its own asynchronous work, and TMEM is released before the block
+// exits.
 #include <cuda.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -32,14 +34,19 @@
 namespace eddy {
 
 namespace {
-constexpr int kTM = 128, kTN = 128, kGroups = 4, kPairsPerGroup = 3, kKC = 128;
-constexpr int kPairsPerTile = kGroups * kPairsPerGroup;
-constexpr uint32_t kStageBytes = (kTM + kTN) * kKC;  // 32 KB
+constexpr int kTM = 128, kPairsPerGroup = 3, kKC = 128;
+// the pair groups of Y are padded to a multiple of every variant's groups
+// per tile (4, 6, 8)
+constexpr int kGroupPad = 24;
+constexpr int kMaxGroups = 8;
 constexpr unsigned long long kTimeoutNs = 2000000000ull;
 // general-path queue of an epilogue warp: room for every table of its tile
-// share (32 units x 12 pairs x 2 classes / warps of a quadrant), 6 words each
+// share (32 units x its pairs x 2 classes), 6 words each
 constexpr int kQWords = 6;
-constexpr uint32_t kBarBytes = 1024;  // barrier block after the stage ring
+// full-sample tables of one group: 3 pairs x 12 floats
+constexpr uint32_t kGroupCtBytes = kPairsPerGroup * 12 * sizeof(float);
+constexpr uint32_t kBarBytes = 4096;  // barriers and table buffers after the stage ring
+constexpr uint32_t kCtOff = 256;      // table buffers inside the barrier block
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p) {
   return (uint32_t)__cvta_generic_to_shared(p);
@@ -72,14 +79,31 @@ __device__ __forceinline__ bool mbar_try(uint32_t a, uint32_t parity) {
 __device__ __forceinline__ bool mbar_wait(uint32_t a, uint32_t parity, volatile unsigned *err) {
   if (mbar_try(a, parity)) return true;
   const unsigned long long t0 = gtimer();
-  while (true) {
+  for (unsigned it = 1;; it++) {
     if (mbar_try(a, parity)) return true;
-    if (*err) return false;
+    // another role's timeout: checked every 256 tries (a global read)
+    if ((it & 255u) == 0 && *err) return false;
     if (gtimer() - t0 > kTimeoutNs) {
       atomicExch((unsigned *)err, 1u);
       return false;
     }
   }
+}
+// Wait for this block's own asynchronous work before it exits: bounded by
+// the same limit, regardless of the error word.
+__device__ __forceinline__ void mbar_drain(uint32_t a, uint32_t parity) {
+  const unsigned long long t0 = gtimer();
+  while (!mbar_try(a, parity))
+    if (gtimer() - t0 > kTimeoutNs) return;
+}
+// 1-D bulk copy global -> shared, completion counted on an mbarrier
+__device__ __forceinline__ void bulk_load(uint32_t dst, const void *src, uint32_t bytes,
+                                          uint32_t mbar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+          dst),
+      "l"((uint64_t)src), "r"(bytes), "r"(mbar)
+      : "memory");
 }
 __device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap *map, int x, int y,
                                             uint32_t mbar) {
@@ -100,15 +124,18 @@ __device__ __forceinline__ uint64_t sdesc(uint32_t saddr) {
   d |= (uint64_t)2 << 61;                    // SWIZZLE_128B
   return d;
 }
-// Instruction descriptor: D f32, A/B e4m3, both K-major, N = 128, M = 128.
-constexpr uint32_t kIdesc = (1u << 4) | (0u << 7) | (0u << 10) | ((uint32_t)(kTN >> 3) << 17) |
-                            ((uint32_t)(kTM >> 4) << 24);
+// Instruction descriptor: D f32, A/B e4m3, both K-major, M = 128, N = n.
+__host__ __device__ constexpr uint32_t idesc_for(int n) {
+  return (1u << 4) | (0u << 7) | (0u << 10) | ((uint32_t)(n >> 3) << 17) |
+         ((uint32_t)(kTM >> 4) << 24);
+}
 
-__device__ __forceinline__ void umma(uint32_t tmem_d, uint64_t da, uint64_t db, uint32_t acc) {
+__device__ __forceinline__ void umma(uint32_t tmem_d, uint64_t da, uint64_t db, uint32_t idesc,
+                                     uint32_t acc) {
   asm volatile(
       "{.reg .pred p; setp.ne.b32 p, %4, 0;"
       " tcgen05.mma.cta_group::1.kind::f8f6f4 [%0], %1, %2, %3, p;}" ::"r"(tmem_d),
-      "l"(da), "l"(db), "r"(kIdesc), "r"(acc));
+      "l"(da), "l"(db), "r"(idesc), "r"(acc));
 }
 __device__ __forceinline__ void umma_commit(uint32_t mbar) {
   asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
@@ -132,6 +159,15 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
         "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
       : "r"(taddr));
 }
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t *r) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,"
+      "%15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
+        "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+}
 __device__ __forceinline__ void tmem_ld_wait() {
   asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 }
@@ -139,22 +175,40 @@ __device__ __forceinline__ void tmem_ld_wait() {
 
 template <int kStages>
 struct MmaSmem {
-  unsigned long long full[kStages], empty[kStages], accfull[2], accempty[2];
+  unsigned long long full[kStages], empty[kStages], accfull[2], accempty[2], ctfull[2], drain;
   uint32_t tmem_base;
 };
-static_assert(sizeof(MmaSmem<8>) <= kBarBytes, "barrier block");
+static_assert(sizeof(MmaSmem<8>) <= kCtOff &&
+                  kCtOff + 2 * kMaxGroups * kGroupCtBytes <= kBarBytes,
+              "barrier block");
 
-// kStages: depth of the TMA ring; kEpi: epilogue warps (8 or 16);
-// kMinBlocks: CTAs per SM the register budget is sized for (two CTAs share
-// TMEM's 512 columns).  All variants produce identical masks; the autotuner
-// picks by time.
-template <int kStages, int kEpi, int kMinBlocks>
-__global__ void __launch_bounds__(32 * (2 + kEpi), kMinBlocks)
+// registers per thread for one CTA of 2 + kEpi warps: each of the four SM
+// sub-partitions holds 16384 registers and ceil((2 + kEpi) / 4) of the warps
+template <int kEpi>
+constexpr int max_regs() {
+  return (16384 / (32 * ((2 + kEpi + 3) / 4))) / 8 * 8 > 255
+             ? 255
+             : (16384 / (32 * ((2 + kEpi + 3) / 4))) / 8 * 8;
+}
+
+// kStages: depth of the TMA ring; kEpi: epilogue warps (a multiple of 4);
+// kGroups: 32-column pair groups per tile (N = 32 kGroups).  One CTA per SM.
+// All variants produce identical masks; the autotuner picks by time.
+template <int kStages, int kEpi, int kGroups>
+__global__ void __maxnreg__(max_regs<kEpi>())
     k_pairs_mma(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
                 const __grid_constant__ SetDev sd, const float *__restrict__ ctotf, int B, int nk,
                 int ntiles, int mblocks, uint32_t *dmask, unsigned long long *stats,
-                unsigned *err) {
-  constexpr int kQCap = 32 * 2 * kPairsPerGroup * (kGroups / (kEpi / 4));
+                unsigned *err, uint32_t *gqueue) {
+  constexpr int kTN = 32 * kGroups;
+  constexpr int kPairsPerTile = kGroups * kPairsPerGroup;
+  constexpr uint32_t kStageBytes = (kTM + kTN) * kKC;
+  constexpr uint32_t kCtBytes = kGroups * kGroupCtBytes;
+  constexpr uint32_t kTmemCols = 2 * kTN <= 256 ? 256u : 512u;
+  constexpr uint32_t kIdesc = idesc_for(kTN);
+  constexpr int kPerQuad = kEpi / 4, kGpw = kGroups / kPerQuad;
+  static_assert(kEpi % 4 == 0 && kGroups % kPerQuad == 0 && kGroups <= kMaxGroups, "shape");
+  constexpr int kQCap = 32 * 2 * kPairsPerGroup * kGpw;
   extern __shared__ __align__(1024) uint8_t smraw[];
   // 1024-byte aligned stage ring, then barriers, then the epilogue buffer
   uint8_t *base = (uint8_t *)(((uintptr_t)smraw + 1023) & ~(uintptr_t)1023);
@@ -171,13 +225,16 @@ __global__ void __launch_bounds__(32 * (2 + kEpi), kMinBlocks)
     for (int a = 0; a < 2; a++) {
       mbar_init(smem_u32(&S.accfull[a]), 1);
       mbar_init(smem_u32(&S.accempty[a]), 32 * kEpi);
+      mbar_init(smem_u32(&S.ctfull[a]), 1);
     }
+    mbar_init(smem_u32(&S.drain), 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   if (warp == 1) {
-    // 256 TMEM columns: two 128-column fp32 accumulators
-    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 256;" ::"r"(
-                     smem_u32(&S.tmem_base)));
+    // two kTN-column fp32 accumulators
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     smem_u32(&S.tmem_base)),
+                 "n"(kTmemCols));
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
   }
   tc_fence_before();
@@ -189,6 +246,7 @@ __global__ void __launch_bounds__(32 * (2 + kEpi), kMinBlocks)
     if (lane == 0) {
       int stage = 0;
       uint32_t phase = 0;
+      long long nfill = 0;
       for (int t = blockIdx.x; t < ntot && !*verr; t += gridDim.x) {
         const int tn = t / mblocks, mb = t % mblocks;
         for (int kc = 0; kc < nk; kc++) {
@@ -198,20 +256,34 @@ __global__ void __launch_bounds__(32 * (2 + kEpi), kMinBlocks)
           const uint32_t sa = smem_u32(base + stage * kStageBytes);
           tma_load_2d(sa, &tmA, kc * kKC, mb * kTM, fb);
           tma_load_2d(sa + kTM * kKC, &tmB, kc * kKC, tn * kTN, fb);
+          nfill++;
           if (++stage == kStages) {
             stage = 0;
             phase ^= 1u;
           }
         }
       }
+      // the last fills have landed before the block may exit
+      for (long long i = nfill > kStages ? nfill - kStages : 0; i < nfill; i++)
+        mbar_drain(smem_u32(&S.full[i % kStages]), (uint32_t)((i / kStages) & 1));
     }
   } else if (warp == 1) {
     if (lane == 0) {
       int stage = 0, acc = 0;
       uint32_t phase = 0, accphase = 0;
+      long long nct = 0;
       for (int t = blockIdx.x; t < ntot && !*verr; t += gridDim.x) {
         if (!mbar_wait(smem_u32(&S.accempty[acc]), accphase ^ 1u, verr)) break;
         tc_fence_after();
+        {
+          // the tile's full-sample tables into the slot's buffer
+          const int tn = t / mblocks;
+          const uint32_t cb = smem_u32(&S.ctfull[acc]);
+          mbar_expect_tx(cb, kCtBytes);
+          bulk_load(smem_u32(base + kStages * kStageBytes + kCtOff + acc * kCtBytes),
+                    ctotf + (size_t)tn * kPairsPerTile * 12, kCtBytes, cb);
+          nct++;
+        }
         const uint32_t dcol = tmem + (uint32_t)(acc * kTN);
         bool ok = true;
         for (int kc = 0; kc < nk; kc++) {
@@ -224,7 +296,7 @@ __global__ void __launch_bounds__(32 * (2 + kEpi), kMinBlocks)
           const uint32_t sb = sa + kTM * kKC;
 #pragma unroll
           for (int k = 0; k < kKC / 32; k++)
-            umma(dcol, sdesc(sa + 32 * k), sdesc(sb + 32 * k), (kc | k) ? 1u : 0u);
+            umma(dcol, sdesc(sa + 32 * k), sdesc(sb + 32 * k), kIdesc, (kc | k) ? 1u : 0u);
           umma_commit(smem_u32(&S.empty[stage]));
           if (++stage == kStages) {
             stage = 0;
@@ -238,11 +310,15 @@ __global__ void __launch_bounds__(32 * (2 + kEpi), kMinBlocks)
           accphase ^= 1u;
         }
       }
+      // every MMA issued here and the last table copies complete before exit
+      umma_commit(smem_u32(&S.drain));
+      mbar_drain(smem_u32(&S.drain), 0);
+      for (long long i = nct > 2 ? nct - 2 : 0; i < nct; i++)
+        mbar_drain(smem_u32(&S.ctfull[i & 1]), (uint32_t)((i >> 1) & 1));
     }
   } else {
     // epilogue: TMEM lane quadrant = warp % 4; the kEpi/4 warps of a quadrant
-    // split the four column groups (one or two each)
-    constexpr int kPerQuad = kEpi / 4, kGpw = kGroups / kPerQuad;
+    // split the column groups (kGpw each)
     const int quad = warp & 3, wq = (warp - 2) >> 2;
     const int row = quad * 32 + lane;  // TMEM lane = unit within the tile
     int acc = 0;
@@ -252,27 +328,16 @@ __global__ void __launch_bounds__(32 * (2 + kEpi), kMinBlocks)
     const float thr0 = sd.exact_all ? -1.f : sd.thr[0][2].chiA;
     const float thr1 = sd.exact_all ? -1.f : sd.thr[1][2].chiA;
     const uint32_t below = (1u << lane) - 1u;
-    // this warp's queue of tables for the general path
-    uint32_t *gq = reinterpret_cast<uint32_t *>(base + kStages * kStageBytes + kBarBytes) +
-                   (size_t)(warp - 2) * kQCap * kQWords;
+    // this warp's queue of tables for the general path (global memory: it
+    // is written for a small share of the tables)
+    uint32_t *gq = gqueue + ((size_t)blockIdx.x * kEpi + (warp - 2)) * kQCap * kQWords;
     for (int t = blockIdx.x; t < ntot && !*verr; t += gridDim.x) {
       const int tn = t / mblocks, mb = t % mblocks;
       if (!mbar_wait(smem_u32(&S.accfull[acc]), accphase, verr)) break;
+      if (!mbar_wait(smem_u32(&S.ctfull[acc]), accphase, verr)) break;
       tc_fence_after();
-      // counts of the warp's group(s): FP32 integers straight from TMEM
-      uint32_t r[kGpw][32];
-#pragma unroll
-      for (int gi = 0; gi < kGpw; gi++) {
-        const int grp = wq + gi * kPerQuad;
-        tmem_ld32(tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)(acc * kTN + grp * 32), r[gi]);
-      }
-      tmem_ld_wait();
-      tc_fence_before();
-      mbar_arrive(smem_u32(&S.accempty[acc]));
-      if (++acc == 2) {
-        acc = 0;
-        accphase ^= 1u;
-      }
+      const float *ctile =
+          reinterpret_cast<const float *>(base + kStages * kStageBytes + kCtOff + acc * kCtBytes);
       const int u = mb * kTM + row;
       const bool valid = u < B;
       // tables the quick filter cannot settle are queued (counts, class,
@@ -293,33 +358,58 @@ __global__ void __launch_bounds__(32 * (2 + kEpi), kMinBlocks)
         }
         nq += __popc(bal);
       };
+      // one pair: class-1 counts cv (FP32 integers from TMEM), class 2 =
+      // full-sample table - class 1
+      auto do_pair = [&](const uint32_t *cv, int grp, int q) {
+        const int p = tn * kPairsPerTile + grp * kPairsPerGroup + q;
+        if (p >= sd.c) return;
+        const float4 *cf =
+            reinterpret_cast<const float4 *>(ctile + (grp * kPairsPerGroup + q) * 12);
+        const float4 f0 = cf[0], f1 = cf[1], f2 = cf[2];
+        float oA[9], oB[9];
+#pragma unroll
+        for (int k = 0; k < 9; k++) oA[k] = __uint_as_float(cv[k]);
+        oB[0] = f0.x - oA[0]; oB[1] = f0.y - oA[1]; oB[2] = f0.z - oA[2];
+        oB[3] = f0.w - oA[3]; oB[4] = f1.x - oA[4]; oB[5] = f1.y - oA[5];
+        oB[6] = f1.z - oA[6]; oB[7] = f1.w - oA[7]; oB[8] = f2.x - oA[8];
+        const int prior = (f2.y != 0.f) ? 1 : 0;
+        const float chiA = prior ? thr1 : thr0;
+        const bool qa = quick_zero_f(oA, chiA), qb = quick_zero_f(oB, chiA);
+        enqueue(valid && !qa, oA, 0, prior, p);
+        enqueue(valid && !qb, oB, 1, prior, p);
+        if (valid) {
+          dmask[(size_t)u * sd.c + p] = 0u;
+          nfilt += (unsigned)qa + (unsigned)qb;
+          ntab += 2;
+        }
+      };
+      // each column group in two 16-column TMEM loads: pair 0 = columns 0-8,
+      // pair 1 = 9-17, pair 2 = 18-26
 #pragma unroll
       for (int gi = 0; gi < kGpw; gi++) {
         const int grp = wq + gi * kPerQuad;
+        const uint32_t ta = tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)(acc * kTN + grp * 32);
+        uint32_t lo[16], hi[16], cv[9];
+        tmem_ld16(ta, lo);
+        tmem_ld_wait();
 #pragma unroll
-        for (int q = 0; q < kPairsPerGroup; q++) {
-          const int p = tn * kPairsPerTile + grp * kPairsPerGroup + q;
-          if (p >= sd.c) continue;
-          // full-sample table (nine counts) and the prior flag of pair p
-          const float4 *cf = reinterpret_cast<const float4 *>(ctotf + (size_t)p * 12);
-          const float4 f0 = cf[0], f1 = cf[1], f2 = cf[2];
-          float oA[9], oB[9];
+        for (int k = 0; k < 9; k++) cv[k] = lo[k];
+        do_pair(cv, grp, 0);
+        tmem_ld16(ta + 16, hi);
+        tmem_ld_wait();
 #pragma unroll
-          for (int k = 0; k < 9; k++) oA[k] = __uint_as_float(r[gi][9 * q + k]);
-          oB[0] = f0.x - oA[0]; oB[1] = f0.y - oA[1]; oB[2] = f0.z - oA[2];
-          oB[3] = f0.w - oA[3]; oB[4] = f1.x - oA[4]; oB[5] = f1.y - oA[5];
-          oB[6] = f1.z - oA[6]; oB[7] = f1.w - oA[7]; oB[8] = f2.x - oA[8];
-          const int prior = (f2.y != 0.f) ? 1 : 0;
-          const float chiA = prior ? thr1 : thr0;
-          const bool qa = quick_zero_f(oA, chiA), qb = quick_zero_f(oB, chiA);
-          enqueue(valid && !qa, oA, 0, prior, p);
-          enqueue(valid && !qb, oB, 1, prior, p);
-          if (valid) {
-            dmask[(size_t)u * sd.c + p] = 0u;
-            nfilt += (unsigned)qa + (unsigned)qb;
-            ntab += 2;
-          }
-        }
+        for (int k = 0; k < 9; k++) cv[k] = (9 + k < 16) ? lo[9 + k] : hi[9 + k - 16];
+        do_pair(cv, grp, 1);
+#pragma unroll
+        for (int k = 0; k < 9; k++) cv[k] = hi[2 + k];
+        do_pair(cv, grp, 2);
+      }
+      // the slot (accumulator and table buffer) is free again
+      tc_fence_before();
+      mbar_arrive(smem_u32(&S.accempty[acc]));
+      if (++acc == 2) {
+        acc = 0;
+        accphase ^= 1u;
       }
       __syncwarp();
       for (int i = lane; i < nq; i += 32) {
@@ -354,26 +444,26 @@ __global__ void __launch_bounds__(32 * (2 + kEpi), kMinBlocks)
   __syncthreads();
   if (warp == 1) {
     tc_fence_after();
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 256;" ::"r"(tmem));
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
+                 "n"(kTmemCols));
   }
 }
 
 // -------------------------------------------------------------- operands
-// Y: row (tile*128 + h*32 + q*9 + 3a + b), h < 4, q < 3 = indicator over the
-// samples of pair tile*12 + h*3 + q having (x_row = a-1, x_col = b-1);
-// e4m3 1.0 = 0x38; columns 27..31 of each group and out-of-range pairs are
-// zero.
-__global__ void k_build_y(const uint64_t *planes, int g, int W, int c, int n_pad, int ntiles,
+// Y: row (group*32 + q*9 + 3a + b), q < 3 = indicator over the samples of
+// pair group*3 + q having (x_row = a-1, x_col = b-1); e4m3 1.0 = 0x38; rows
+// 27..31 of each group and out-of-range pairs are zero.  A tile of any
+// variant is a run of whole groups.
+__global__ void k_build_y(const uint64_t *planes, int g, int W, int c, int n_pad, int ngroups,
                           uint8_t *Y) {
   const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;  // 16-sample chunk
   const int chunks = n_pad / 16;
-  const long long rows = (long long)ntiles * kTN;
+  const long long rows = (long long)ngroups * 32;
   if (idx >= rows * chunks) return;
   const int rr = (int)(idx / chunks), ch = (int)(idx % chunks);
-  const int tile = rr / kTN, r = rr % kTN;
-  const int h = r / 32, r32 = r % 32;
+  const int grp = rr / 32, r32 = rr % 32;
   const int q = r32 / 9, cell = r32 % 9;
-  const int p = tile * kPairsPerTile + h * kPairsPerGroup + q;
+  const int p = grp * kPairsPerGroup + q;
   uint8_t v[16];
   uint32_t bits = 0;
   if (r32 < kPairsPerGroup * 9 && p < c) {
@@ -395,14 +485,15 @@ __global__ void k_build_y(const uint64_t *planes, int g, int W, int c, int n_pad
 }
 
 // Full-sample tables as FP32 for the epilogue: pair p -> 12 floats (nine
-// counts, the prior flag, two pad), 48 bytes, float4-aligned.
-__global__ void k_ctot_f(const uint16_t *ctot, const uint8_t *prior, int c, float *out) {
+// counts, the prior flag, two pad), 48 bytes, float4-aligned; pairs past c
+// up to whole tiles are zero.
+__global__ void k_ctot_f(const uint16_t *ctot, const uint8_t *prior, int c, int cpad, float *out) {
   const int p = blockIdx.x * blockDim.x + threadIdx.x;
-  if (p >= c) return;
+  if (p >= cpad) return;
   float v[12];
 #pragma unroll
-  for (int k = 0; k < 9; k++) v[k] = (float)ctot[(size_t)p * 9 + k];
-  v[9] = prior[p] ? 1.f : 0.f;
+  for (int k = 0; k < 9; k++) v[k] = p < c ? (float)ctot[(size_t)p * 9 + k] : 0.f;
+  v[9] = (p < c && prior[p]) ? 1.f : 0.f;
   v[10] = v[11] = 0.f;
   float4 *o = reinterpret_cast<float4 *>(out + (size_t)p * 12);
   o[0] = make_float4(v[0], v[1], v[2], v[3]);
@@ -446,72 +537,99 @@ static EncodeTiledFn encode_fn() {
   return fn;
 }
 
-static bool make_map(CUtensorMap *m, void *ptr, int cols, int rows) {
+static bool make_map(CUtensorMap *m, void *ptr, int cols, int rows, int box_rows) {
   EncodeTiledFn f = encode_fn();
   if (!f) return false;
   cuuint64_t dims[2] = {(cuuint64_t)cols, (cuuint64_t)rows};
   cuuint64_t strides[1] = {(cuuint64_t)cols};
-  cuuint32_t box[2] = {(cuuint32_t)kKC, 128u};
+  cuuint32_t box[2] = {(cuuint32_t)kKC, (cuuint32_t)box_rows};
   cuuint32_t es[2] = {1u, 1u};
   return f(m, CU_TENSOR_MAP_DATA_TYPE_UINT8, 2, ptr, dims, strides, box, es,
            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
            CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
-int mma_ntiles(int c) { return (c + kPairsPerTile - 1) / kPairsPerTile; }
+// pair groups of a set, and that count padded for every variant
+static int ngroups_of(int c) { return (c + kPairsPerGroup - 1) / kPairsPerGroup; }
+int mma_ngroups_pad(int c) {
+  const int g = ngroups_of(c);
+  return (g > 0 ? (g + kGroupPad - 1) / kGroupPad : 1) * kGroupPad;
+}
 int mma_npad(int n) { return (n + kKC - 1) / kKC * kKC; }
 // the operand Y, then the FP32 full-sample tables (a multiple of 128 bytes in)
-static size_t y_operand_bytes(int c, int n) { return (size_t)mma_ntiles(c) * kTN * mma_npad(n); }
-size_t mma_y_bytes(int c, int n) { return y_operand_bytes(c, n) + 48 * (size_t)(c > 0 ? c : 1); }
+static size_t y_operand_bytes(int c, int n) {
+  return (size_t)mma_ngroups_pad(c) * 32 * mma_npad(n);
+}
+size_t mma_y_bytes(int c, int n) {
+  return y_operand_bytes(c, n) + (size_t)kGroupCtBytes * mma_ngroups_pad(c);
+}
 int mma_bpad(int B) { return (B + kTM - 1) / kTM * kTM; }
+static size_t a_operand_bytes(int B, int n) { return (size_t)mma_bpad(B) * mma_npad(n); }
+// the A operand, then the general-path queues of up to `sms` CTAs (a CTA's
+// queues hold 32 units x 3 pairs x 2 classes per group and quadrant)
+size_t mma_a_bytes(int B, int n, int sms) {
+  return a_operand_bytes(B, n) + (size_t)sms * 4 * 32 * 2 * kPairsPerGroup * kMaxGroups *
+                                     kQWords * sizeof(uint32_t);
+}
 
 cudaError_t launch_build_y(const SetDev &sd, uint8_t *Y, cudaStream_t st) {
-  const int nt = mma_ntiles(sd.c), np = mma_npad(sd.n);
-  const long long work = (long long)nt * kTN * (np / 16);
-  k_build_y<<<(unsigned)((work + 255) / 256), 256, 0, st>>>(sd.planes, sd.g, sd.W, sd.c, np, nt, Y);
-  if (sd.c > 0)
-    k_ctot_f<<<(sd.c + 255) / 256, 256, 0, st>>>(sd.ctot, sd.prior, sd.c,
+  const int ng = mma_ngroups_pad(sd.c), np = mma_npad(sd.n);
+  const long long work = (long long)ng * 32 * (np / 16);
+  k_build_y<<<(unsigned)((work + 255) / 256), 256, 0, st>>>(sd.planes, sd.g, sd.W, sd.c, np, ng, Y);
+  if (sd.c > 0) {
+    const int cpad = ng * kPairsPerGroup;  // whole groups, the pad zero
+    k_ctot_f<<<(cpad + 255) / 256, 256, 0, st>>>(sd.ctot, sd.prior, sd.c, cpad,
                                                   (float *)(Y + y_operand_bytes(sd.c, sd.n)));
+  }
   return cudaGetLastError();
 }
 
-template <int kStages, int kEpi, int kMinBlocks>
-static cudaError_t launch_variant(const CUtensorMap &ma, const CUtensorMap &mb, const SetDev &sd,
-                                  const float *ctotf, int B, int np, int nt, int mblocks,
-                                  uint32_t *dmask,
+template <int kStages, int kEpi, int kGroups>
+static cudaError_t launch_variant(const SetDev &sd, const uint8_t *Afp8, const uint8_t *Y,
+                                  uint32_t *gqueue, int B, uint32_t *dmask,
                                   unsigned long long *stats, unsigned *err, int sms,
                                   cudaStream_t st) {
-  constexpr int kQCap = 32 * 2 * kPairsPerGroup * (kGroups / (kEpi / 4));
-  const size_t smem = 1024 + kStages * kStageBytes + kBarBytes +
-                      (size_t)kEpi * kQCap * kQWords * sizeof(uint32_t);
-  auto kern = k_pairs_mma<kStages, kEpi, kMinBlocks>;
+  constexpr int kTN = 32 * kGroups;
+  const int np = mma_npad(sd.n), Bp = mma_bpad(B);
+  const int ng = ngroups_of(sd.c), nt = (ng + kGroups - 1) / kGroups;
+  CUtensorMap ma, mb;
+  if (!make_map(&ma, (void *)Afp8, np, Bp, kTM) ||
+      !make_map(&mb, (void *)Y, np, mma_ngroups_pad(sd.c) * 32, kTN))
+    return cudaErrorNotSupported;
+  const int mblocks = Bp / kTM;
+  const float *ctotf = (const float *)(Y + y_operand_bytes(sd.c, sd.n));
+  const size_t smem = 1024 + (size_t)kStages * (kTM + kTN) * kKC + kBarBytes;
+  auto kern = k_pairs_mma<kStages, kEpi, kGroups>;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   const int ntot = nt * mblocks;
-  const int grid = ntot < sms * kMinBlocks ? ntot : sms * kMinBlocks;
+  const int grid = ntot < sms ? ntot : sms;
   kern<<<grid, 32 * (2 + kEpi), smem, st>>>(ma, mb, sd, ctotf, B, np / kKC, nt, mblocks, dmask,
-                                            stats, err);
+                                            stats, err, gqueue);
   return cudaGetLastError();
 }
 
-int mma_variants() { return 2; }
+// 0: N=128, 16 epilogue warps; 1: N=128, 8 warps; 2: N=192, 12 warps;
+// 3: N=256, 8 warps (ring depths fill the shared memory)
+int mma_variants() { return 4; }
 
 cudaError_t launch_pairs_mma(const SetDev &sd, const uint64_t *masks, int B, uint8_t *Afp8,
                              const uint8_t *Y, uint32_t *dmask, unsigned long long *stats,
                              unsigned *err, int sms, cudaStream_t st, int variant) {
-  const int np = mma_npad(sd.n), Bp = mma_bpad(B), nt = mma_ntiles(sd.c);
+  const int np = mma_npad(sd.n), Bp = mma_bpad(B);
   const long long work = (long long)Bp * (np / 16);
   k_masks_fp8<<<(unsigned)((work + 255) / 256), 256, 0, st>>>(masks, B, Bp, sd.W, np, Afp8);
-  CUtensorMap ma, mb;
-  if (!make_map(&ma, Afp8, np, Bp) || !make_map(&mb, (void *)Y, np, nt * kTN))
-    return cudaErrorNotSupported;
-  const int mblocks = Bp / kTM;
-  const float *ctotf = (const float *)(Y + y_operand_bytes(sd.c, sd.n));
-  if (variant == 1)
-    return launch_variant<4, 8, 1>(ma, mb, sd, ctotf, B, np, nt, mblocks, dmask, stats, err, sms,
-                                   st);
-  return launch_variant<4, 16, 1>(ma, mb, sd, ctotf, B, np, nt, mblocks, dmask, stats, err, sms,
-                                  st);
+  uint32_t *gqueue = reinterpret_cast<uint32_t *>(Afp8 + a_operand_bytes(B, sd.n));
+  switch (variant) {
+    case 1:
+      return launch_variant<6, 8, 4>(sd, Afp8, Y, gqueue, B, dmask, stats, err, sms, st);
+    case 2:
+      return launch_variant<5, 12, 6>(sd, Afp8, Y, gqueue, B, dmask, stats, err, sms, st);
+    case 3:
+      return launch_variant<4, 8, 8>(sd, Afp8, Y, gqueue, B, dmask, stats, err, sms, st);
+    default:
+      return launch_variant<6, 16, 4>(sd, Afp8, Y, gqueue, B, dmask, stats, err, sms, st);
+  }
 }
 
 }  // namespace eddy

@@ -7,17 +7,20 @@
 #include "eddy_internal.h"
 
 namespace eddy {
-int mma_ntiles(int c);
+// pair groups (3 pairs, 32 operand rows each) padded for every variant
+int mma_ngroups_pad(int c);
 int mma_npad(int n);
 int mma_bpad(int B);
+// bytes of the Afp8 scratch for a batch of B units (operand + queues)
+size_t mma_a_bytes(int B, int n, int sms);
 size_t mma_y_bytes(int c, int n);
 // Builds the pair-cell indicator operand Y of the current set and, after it,
 // the FP32 copy of the full-sample tables the epilogue reads.
 cudaError_t launch_build_y(const SetDev &sd, uint8_t *Y, cudaStream_t st);
-// Masks -> e4m3 operand (Afp8, mma_bpad(B) x mma_npad(n) bytes), then the
+// Masks -> e4m3 operand (Afp8, mma_a_bytes(B, n, sms) bytes), then the
 // GEMM + decision kernel; *err is set on a bounded-wait timeout.
-// variant 0: 16 epilogue warps (one column group each); variant 1: 8
-// epilogue warps (two groups each); both a 4-stage ring, one CTA per SM.
+// variants (mma_variants()): tile widths N = 128 / 192 / 256 with 16, 8, 12
+// or 8 epilogue warps, one CTA per SM.
 int mma_variants();
 cudaError_t launch_pairs_mma(const SetDev &sd, const uint64_t *masks, int B, uint8_t *Afp8,
                              const uint8_t *Y, uint32_t *dmask, unsigned long long *stats,

@@ -171,11 +171,13 @@ def test_glibc_stream_matches_reference_sampler(eddy_lib, oracle_lib):
         assert js_close(js, ojs)
 
 
+@pytest.mark.parametrize("variant", [0, 1, 2, 3], ids=["n128e16", "n128e8", "n192e12", "n256e8"])
 @pytest.mark.parametrize("case", [CASES[2], CASES[4], CASES[5], CASES[6]],
                          ids=["g20", "g50", "invalid", "g40prior"])
-def test_tensor_core_and_popcount_paths_agree(case, eddy_lib, monkeypatch):
-    """The tcgen05 contingency GEMM and the popcount kernel give the same
-    edge decisions for every network (bit for bit)."""
+def test_tensor_core_and_popcount_paths_agree(case, variant, eddy_lib, monkeypatch):
+    """Every tile shape of the tcgen05 contingency GEMM and the popcount
+    kernel give the same edge decisions for every network (bit for bit)."""
+    monkeypatch.setenv("EDDY_MMA_VARIANT", str(variant))
     g, n, nA, mp, bonf, pw, npr, inv = case
     rng = np.random.default_rng(g + 7 * n)
     data = planted(rng, g, n, nA=nA, invalid=inv)
