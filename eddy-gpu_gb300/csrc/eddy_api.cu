@@ -8,6 +8,7 @@
 #include <string.h>
 
 #include <algorithm>
+#include <map>
 #include <string>
 #include <vector>
 
@@ -24,13 +25,22 @@ namespace {
 struct DevBuf {
   void *p = nullptr;
   size_t n = 0;
+  // grows by at least half its size: sets of varying size do not pay a
+  // cudaFree (a device-wide synchronisation) for every small growth
   cudaError_t ensure(size_t bytes) {
     if (bytes <= n) return cudaSuccess;
+    const size_t want = std::max(bytes, n + n / 2);
     if (p) cudaFree(p);
     p = nullptr;
     n = 0;
-    cudaError_t e = cudaMalloc(&p, bytes);
-    if (e == cudaSuccess) n = bytes;
+    cudaError_t e = cudaMalloc(&p, want);
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      e = cudaMalloc(&p, bytes);  // no room for the margin: the exact size
+      if (e == cudaSuccess) n = bytes;
+      return e;
+    }
+    n = want;
     return e;
   }
   void release() {
@@ -82,9 +92,17 @@ struct eddy_ctx {
   DevBuf d_oids, d_ocnt, d_opar, d_odist, d_olval, d_orows, d_stats;
   DevBuf d_Y, d_afp8, d_err;  // tensor-core contingency operands
   int sms = 148;
-  // autotuned contingency-kernel variant per set shape (g, n); -1 = untuned
-  int tuned_g = -1, tuned_n = -1, tuned_variant = -1;
+  // autotuned contingency-kernel variant per (n, power of two of the pair
+  // count); tuned_variant: the last one used (-1 = none yet)
+  std::map<std::pair<int, int>, int> tuned;
+  int tuned_variant = -1;
   float tuned_ms[4] = {0, 0, 0, 0};
+  // decision thresholds per gene-set size (the Bonferroni factor)
+  struct ThrSet {
+    Thr t[2][kDofSlots];
+    bool exact_all;
+  };
+  std::map<int, ThrSet> thr_cache;
   int lg_shift = 0;
   bool lg_ready = false;
   int lg_n = -1;  // sample count the fixed-point lgamma table was built for
@@ -188,7 +206,16 @@ int prepare_set(eddy_ctx *ctx, int set_id, SetRun &sr) {
   sd.bonf = ctx->o.bonferroni ? 1 : 0;
   sd.alpha_edge = ctx->o.alpha_edge;
   sd.alpha_edge_prior = ctx->o.alpha_edge_prior;
-  sd.exact_all = compute_thresholds(sd.alpha_edge, sd.alpha_edge_prior, g, sd.bonf, sd.thr) ? 1 : 0;
+  {
+    auto it = ctx->thr_cache.find(g);
+    if (it == ctx->thr_cache.end()) {
+      eddy_ctx::ThrSet ts;
+      ts.exact_all = compute_thresholds(sd.alpha_edge, sd.alpha_edge_prior, g, sd.bonf, ts.t);
+      it = ctx->thr_cache.emplace(g, ts).first;
+    }
+    memcpy(sd.thr, it->second.t, sizeof sd.thr);
+    sd.exact_all = it->second.exact_all ? 1 : 0;
+  }
   {
     // EDDY_DECISIONS=fp64: the plain FP64 form -- every table of every pair
     // evaluated with the reference's FP64 formula, no FP32 fast path, no
@@ -233,6 +260,14 @@ bool use_popc() {
   return e && strcmp(e, "popc") == 0;
 }
 
+// autotuning key: samples and the power of two of the pair count (sets of
+// similar size share a tile shape)
+std::pair<int, int> tune_key(const SetDev &sd) {
+  int lc = 0;
+  while ((1 << lc) < sd.c) lc++;
+  return {sd.n, lc};
+}
+
 int launch_pairs_any(eddy_ctx *ctx, const SetDev &sd, const uint64_t *masks, int B, uint32_t *dmask,
                      unsigned long long *stats) {
   if (sd.c == 0) return EDDY_OK;
@@ -256,8 +291,8 @@ int launch_pairs_any(eddy_ctx *ctx, const SetDev &sd, const uint64_t *masks, int
   const char *ev = getenv("EDDY_MMA_VARIANT");
   if (ev) {
     variant = atoi(ev) % mma_variants();
-  } else if (ctx->tuned_g == sd.g && ctx->tuned_n == sd.n && ctx->tuned_variant >= 0) {
-    variant = ctx->tuned_variant;
+  } else if (ctx->tuned.count(tune_key(sd))) {
+    variant = ctx->tuned[tune_key(sd)];
   } else if (B >= 512) {
     // autotune on this batch: time every variant once (same results), keep
     // the fastest for this (g, n); the last run leaves dmask filled
@@ -278,11 +313,10 @@ int launch_pairs_any(eddy_ctx *ctx, const SetDev &sd, const uint64_t *masks, int
       }
       ctx->launches += 2;
     }
-    ctx->tuned_g = sd.g;
-    ctx->tuned_n = sd.n;
-    ctx->tuned_variant = bi;
+    ctx->tuned[tune_key(sd)] = bi;
     variant = bi;
   }
+  ctx->tuned_variant = variant;
   CK(launch_pairs_mma(sd, masks, B, ctx->d_afp8.as<uint8_t>(), ctx->d_Y.as<uint8_t>(), dmask, stats,
                       ctx->d_err.as<unsigned>(), ctx->sms, ctx->stream, variant));
   ctx->launches += 2;
@@ -310,7 +344,6 @@ int run_units(eddy_ctx *ctx, SetRun &sr, int nunits, const uint64_t *masks_host,
   size_t per_unit = unit_scratch_bytes(c, S, kmax) + sizeof(uint32_t) * (size_t)c + 8 * W + 64;
   int Bmax = (int)std::max<size_t>(1, ((size_t)3 << 30) / std::max<size_t>(per_unit, 1));
   Bmax = std::min(Bmax, 4096);
-  if (keeping) Bmax = 1;
   std::vector<uint32_t> status;
   std::vector<int32_t> uset, uperm;
   const int mpk = std::max(1, mpk_req);
@@ -360,8 +393,14 @@ int run_units(eddy_ctx *ctx, SetRun &sr, int nunits, const uint64_t *masks_host,
                                 ctx->d_masks.as<uint64_t>(), Bt, ctx->stream));
         ctx->launches++;
       }
+      // the kept unit (the first of the call) writes its detailed outputs
       std::vector<int32_t> ks(Bt, -1);
-      if (keeping) ks[0] = 0;
+      int i0 = -1;
+      for (int i = 0; i < Bt && keeping; i++)
+        if (b0 + todo[i] == 0) {
+          ks[i] = 0;
+          i0 = i;
+        }
       CK(cudaMemcpyAsync(ctx->d_keep.p, ks.data(), 4 * Bt, cudaMemcpyHostToDevice, ctx->stream));
       BatchDev bd{};
       bd.B = Bt;
@@ -397,11 +436,13 @@ int run_units(eddy_ctx *ctx, SetRun &sr, int nunits, const uint64_t *masks_host,
       CK(cudaMemcpyAsync(jsb.data(), ctx->d_js.p, 8 * Bt, cudaMemcpyDeviceToHost, ctx->stream));
       CK(cudaMemcpyAsync(Ub.data(), ctx->d_U.p, 4 * Bt, cudaMemcpyDeviceToHost, ctx->stream));
       CK(cudaMemcpyAsync(status.data(), ctx->d_status.p, 4 * Bt, cudaMemcpyDeviceToHost, ctx->stream));
+      // the tensor-core kernel's timeout word, read with the results
+      unsigned errw = 0;
+      const bool mma_used = !use_popc() && ctx->d_err.p != nullptr && c > 0;
+      if (mma_used)
+        CK(cudaMemcpyAsync(&errw, ctx->d_err.p, sizeof errw, cudaMemcpyDeviceToHost, ctx->stream));
       CK(cudaStreamSynchronize(ctx->stream));
-      {
-        int rc = check_mma_error(ctx);
-        if (rc) return rc;
-      }
+      if (errw) return fail(ctx, EDDY_ERR_INTERNAL, "tensor-core pipeline wait timed out");
       float a = 0, bms = 0;
       cudaEventElapsedTime(&a, ctx->ev[0], ctx->ev[1]);
       cudaEventElapsedTime(&bms, ctx->ev[1], ctx->ev[2]);
@@ -422,10 +463,10 @@ int run_units(eddy_ctx *ctx, SetRun &sr, int nunits, const uint64_t *masks_host,
           U[u] = Ub[i];
         }
       }
-      if (keeping && again.empty()) {
+      if (i0 >= 0 && !(status[i0] & (kUnitKmaxOverflow | kUnitHashCollision))) {
         keep->mpk = mpk;
-        keep->U = Ub[0];
-        const int Uk = Ub[0];
+        keep->U = Ub[i0];
+        const int Uk = Ub[i0];
         keep->ids.resize(Uk);
         keep->cnt.resize((size_t)Uk * g);
         keep->par.resize((size_t)Uk * g * mpk);
@@ -651,54 +692,80 @@ static int run_set(eddy_ctx *ctx, int set_id) {
   SetRun sr;
   int rc = prepare_set(ctx, set_id, sr);
   if (rc) return rc;
-  // iteration 0 (kept: networks and likelihoods for the output files)
-  std::vector<uint64_t> masks((size_t)W);
-  std::vector<uint8_t> lab(ctx->labels0);
-  if (ctx->o.rng == EDDY_RNG_EXTERNAL) lab.assign(S.labels.begin(), S.labels.begin() + n);
-  if (ctx->o.rng == EDDY_RNG_GLIBC)
-    glibc_permutation(ctx->rng, n, ctx->nA, false, lab.data(), ctx->seen, ctx->order);
-  labels_to_mask(lab.data(), n, W, masks.data());
-  KeepOut K;
-  const int mpk = std::min(ctx->o.max_parents, std::max(g - 1, 1));
-  rc = run_units(ctx, sr, 1, masks.data(), nullptr, S.js.data(), S.U.data(),
-                 ctx->o.keep_networks ? &K : nullptr, mpk);
-  if (rc) return rc;
-  if (ctx->o.keep_networks) store_keep(ctx, S, K, g);
-  else S.U0 = S.U[0];
-  S.iterations = 1;
-  if (!finite_js(S.js[0])) {
-    S.failed = 1;
-    S.done = true;
-    return EDDY_OK;  // main.cu:1431-1435: break after iteration 0
-  }
-  if (R > 1) {
-    const int nu = R - 1;
-    std::vector<int32_t> perms(nu);
-    for (int i = 0; i < nu; i++) perms[i] = i + 1;
-    const bool device_counter = ctx->o.rng == EDDY_RNG_COUNTER && n <= 4096;
-    std::vector<uint64_t> mh;
-    if (!device_counter) {
-      mh.assign((size_t)nu * W, 0);
-      std::vector<uint8_t> cur(ctx->labels0);
-      for (int i = 0; i < nu; i++) {
-        if (ctx->o.rng == EDDY_RNG_GLIBC) {
-          glibc_permutation(ctx->rng, n, ctx->nA, true, cur.data(), ctx->seen, ctx->order);
-        } else if (ctx->o.rng == EDDY_RNG_COUNTER) {
-          counter_labels(ctx->o.seed, set_id, i + 1, n, ctx->nA, cur.data());
-        } else {
-          memcpy(cur.data(), S.labels.data() + (size_t)(i + 1) * n, n);
-          int a = 0;
-          for (int s = 0; s < n; s++) a += cur[s] == 0;
-          if (a != ctx->nA) return fail(ctx, EDDY_ERR_ARG, "labelling %d changes the class sizes", i + 1);
-        }
-        labels_to_mask(cur.data(), n, W, mh.data() + (size_t)i * W);
-      }
-    }
-    rc = run_units(ctx, sr, nu, device_counter ? nullptr : mh.data(), perms.data(), S.js.data() + 1,
-                   S.U.data() + 1, nullptr, 1);
+  const int mpk0 = std::min(ctx->o.max_parents, std::max(g - 1, 1));
+  if (ctx->o.rng == EDDY_RNG_COUNTER && n <= 4096) {
+    // counter stream: iteration 0 (the unpermuted labelling, kept) and the
+    // permutations in one pass, labellings generated on the device.  A
+    // non-finite JS at iteration 0 ends the set there (main.cu:1431-1435):
+    // the permutations' results are then discarded.
+    std::vector<int32_t> perms(R);
+    for (int i = 0; i < R; i++) perms[i] = i;
+    KeepOut K;
+    rc = run_units(ctx, sr, R, nullptr, perms.data(), S.js.data(), S.U.data(),
+                   ctx->o.keep_networks ? &K : nullptr, mpk0);
     if (rc) return rc;
+    if (ctx->o.keep_networks) store_keep(ctx, S, K, g);
+    else S.U0 = S.U[0];
+    if (!finite_js(S.js[0])) {
+      for (int i = 1; i < R; i++) {
+        S.js[i] = NAN;
+        S.U[i] = 0;
+      }
+      S.iterations = 1;
+      S.failed = 1;
+      S.done = true;
+      return EDDY_OK;
+    }
+    S.iterations = R;
+  } else {
+    // iteration 0 (kept: networks and likelihoods for the output files)
+    std::vector<uint64_t> masks((size_t)W);
+    std::vector<uint8_t> lab(ctx->labels0);
+    if (ctx->o.rng == EDDY_RNG_EXTERNAL) lab.assign(S.labels.begin(), S.labels.begin() + n);
+    if (ctx->o.rng == EDDY_RNG_GLIBC)
+      glibc_permutation(ctx->rng, n, ctx->nA, false, lab.data(), ctx->seen, ctx->order);
+    labels_to_mask(lab.data(), n, W, masks.data());
+    KeepOut K;
+    rc = run_units(ctx, sr, 1, masks.data(), nullptr, S.js.data(), S.U.data(),
+                   ctx->o.keep_networks ? &K : nullptr, mpk0);
+    if (rc) return rc;
+    if (ctx->o.keep_networks) store_keep(ctx, S, K, g);
+    else S.U0 = S.U[0];
+    S.iterations = 1;
+    if (!finite_js(S.js[0])) {
+      S.failed = 1;
+      S.done = true;
+      return EDDY_OK;  // main.cu:1431-1435: break after iteration 0
+    }
+    if (R > 1) {
+      const int nu = R - 1;
+      std::vector<int32_t> perms(nu);
+      for (int i = 0; i < nu; i++) perms[i] = i + 1;
+      const bool device_counter = ctx->o.rng == EDDY_RNG_COUNTER && n <= 4096;
+      std::vector<uint64_t> mh;
+      if (!device_counter) {
+        mh.assign((size_t)nu * W, 0);
+        std::vector<uint8_t> cur(ctx->labels0);
+        for (int i = 0; i < nu; i++) {
+          if (ctx->o.rng == EDDY_RNG_GLIBC) {
+            glibc_permutation(ctx->rng, n, ctx->nA, true, cur.data(), ctx->seen, ctx->order);
+          } else if (ctx->o.rng == EDDY_RNG_COUNTER) {
+            counter_labels(ctx->o.seed, set_id, i + 1, n, ctx->nA, cur.data());
+          } else {
+            memcpy(cur.data(), S.labels.data() + (size_t)(i + 1) * n, n);
+            int a = 0;
+            for (int s = 0; s < n; s++) a += cur[s] == 0;
+            if (a != ctx->nA) return fail(ctx, EDDY_ERR_ARG, "labelling %d changes the class sizes", i + 1);
+          }
+          labels_to_mask(cur.data(), n, W, mh.data() + (size_t)i * W);
+        }
+      }
+      rc = run_units(ctx, sr, nu, device_counter ? nullptr : mh.data(), perms.data(), S.js.data() + 1,
+                     S.U.data() + 1, nullptr, 1);
+      if (rc) return rc;
+    }
+    S.iterations = R;
   }
-  S.iterations = R;
   unsigned long long st[4];
   CK(cudaMemcpy(st, ctx->d_stats.p, sizeof st, cudaMemcpyDeviceToHost));
   S.exact += st[0];
