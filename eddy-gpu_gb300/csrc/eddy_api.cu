@@ -369,7 +369,9 @@ int run_units(eddy_ctx *ctx, SetRun &sr, int nunits, const uint64_t *masks_host,
       const int Bt = (int)todo.size();
       const size_t ub = unit_scratch_bytes(c, S, kmax_run);
       CK(ctx->d_masks.ensure(sizeof(uint64_t) * (size_t)Bt * W));
-      CK(ctx->d_dmask.ensure(sizeof(uint32_t) * (size_t)Bt * (c > 0 ? c : 1)));
+      CK(ctx->d_dmask.ensure(dmask_bytes(Bt, c)));
+      CK(cudaMemsetAsync(ctx->d_dmask.as<uint32_t>() + (size_t)Bt * (c > 0 ? c : 1), 0,
+                         sizeof(uint32_t) * (size_t)Bt * chunk_words(c > 0 ? c : 1), ctx->stream));
       CK(ctx->d_scratch.ensure(ub * Bt));
       CK(ctx->d_js.ensure(sizeof(double) * Bt));
       CK(ctx->d_U.ensure(sizeof(int32_t) * Bt));
@@ -878,7 +880,9 @@ int eddy_debug_edges(eddy_ctx *ctx, int set_id, const uint8_t *labels, uint8_t *
   std::vector<uint64_t> m(W);
   labels_to_mask(labels, n, W, m.data());
   CK(ctx->d_masks.ensure(8 * W));
-  CK(ctx->d_dmask.ensure(4 * (size_t)(c > 0 ? c : 1)));
+  CK(ctx->d_dmask.ensure(dmask_bytes(1, c)));
+  CK(cudaMemsetAsync(ctx->d_dmask.as<uint32_t>() + (c > 0 ? c : 1), 0,
+                     sizeof(uint32_t) * chunk_words(c > 0 ? c : 1), ctx->stream));
   CK(cudaMemcpyAsync(ctx->d_masks.p, m.data(), 8 * W, cudaMemcpyHostToDevice, ctx->stream));
   rc = launch_pairs_any(ctx, sd, ctx->d_masks.as<uint64_t>(), 1, ctx->d_dmask.as<uint32_t>(), nullptr);
   if (rc) return rc;

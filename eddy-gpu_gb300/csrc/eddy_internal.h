@@ -53,6 +53,29 @@ struct SetDev {
 };
 
 // Per-batch pointers for the unit kernel.
+// Decision masks of a batch: [B][c] u32, followed by a bitmap per unit of
+// the 32-pair chunks that hold a nonzero mask ([B][chunk_words(c)] u32);
+// the bitmap is zeroed before the decision kernel, which sets a chunk's bit
+// whenever it writes a nonzero mask into it.
+#ifdef __CUDACC__
+#define EDDY_HD __host__ __device__
+#else
+#define EDDY_HD
+#endif
+EDDY_HD constexpr int chunk_words(int c) { return ((c + 31) / 32 + 31) / 32; }
+EDDY_HD constexpr size_t dmask_bytes(int B, int c) {
+  const int cc = c > 0 ? c : 1;
+  return sizeof(uint32_t) * ((size_t)B * cc + (size_t)B * chunk_words(cc));
+}
+#ifdef __CUDACC__
+__device__ __forceinline__ uint32_t *chunk_bits(uint32_t *dmask, int B, int c, int u) {
+  return dmask + (size_t)B * c + (size_t)u * chunk_words(c);
+}
+__device__ __forceinline__ void mark_chunk(uint32_t *dmask, int B, int c, int u, int p) {
+  atomicOr(chunk_bits(dmask, B, c, u) + (p >> 10), 1u << ((p >> 5) & 31));
+}
+#endif
+
 struct BatchDev {
   int B;                       // units in the batch
   int kmax;                    // changed-node records per network

@@ -169,6 +169,7 @@ __global__ void __launch_bounds__(128) k_pairs(const __grid_constant__ SetDev sd
     uint32_t mA = pair_mask(tA, prior, sd, nexact, nfilt);
     uint32_t mB = pair_mask(tB, prior, sd, nexact, nfilt);
     dmask[(size_t)u * sd.c + p] = mA | (mB << 16);
+    if (mA | mB) mark_chunk(dmask, gridDim.y, sd.c, u, p);
     ntab = 2;
   }
   if (stats) {
@@ -487,7 +488,8 @@ __global__ void __launch_bounds__(256, 3) k_units(const __grid_constant__ SetDev
     P.mB[w] = sd.valid[w] & ~m;
   }
   for (int i = tid; i < 2 * g * GW; i += nt) P.rows[i] = 0;
-  for (int i = tid; i < 4 * g; i += nt) P.phs[i] = 0;  // phs and phe
+  // entry ranges of rows: start = INT_MAX, end = 0 until an entry lands
+  for (int i = tid; i < 4 * g; i += nt) P.phs[i] = (i < 2 * g) ? 0x7fffffff : 0;
   for (int i = tid; i < kMemo; i += nt) {
     P.mkey[i] = ~0ull;
     P.mval[2 * i] = LLONG_MIN;
@@ -543,12 +545,14 @@ __global__ void __launch_bounds__(256, 3) k_units(const __grid_constant__ SetDev
     else if ((b >> bit) & 1ull) sig[sd.nA + P.pcB[w] + __popcll(b & below64)] = i;
   }
 
-  // ---- P1: full-network rows and flip lists.  Warp w owns the rows whose
-  // pairs start in [w c/nw, (w+1) c/nw) and walks their pairs in 32-pair
-  // chunks (loads issued four chunks ahead).  Edge bits go into the row
-  // bitsets; the flip entries land, in pair order, in the warp's own segment
-  // of the list (which starts at its first pair); each row's entry range is
-  // marked by the lanes holding its first and last pair.
+  // ---- P1: full-network rows and flip lists, from the 32-pair chunks that
+  // hold a nonzero mask (the decision kernel's bitmap; the other chunks are
+  // all zero).  Warp w owns the rows whose pairs start in [w c/nw,
+  // (w+1) c/nw) and walks its flagged chunks in pair order, four loads at a
+  // time.  Edge bits go into the row bitsets; the flip entries land, in pair
+  // order, in the warp's own segment of the list (which starts at its first
+  // pair); a row's entry range is the min / max position of its entries
+  // (rows without entries keep start > end).
   {
     const long long p_lo = (long long)warp * c / nw, p_hi = (long long)(warp + 1) * c / nw;
     int r0, c0;
@@ -564,29 +568,14 @@ __global__ void __launch_bounds__(256, 3) k_units(const __grid_constant__ SetDev
     if (r0 < 1) r0 = 1;  // row 0 has no pairs
     const int pa = r0 * (r0 - 1) / 2, pb = r0 < r1 ? r1 * (r1 - 1) / 2 : pa;
     int wpos0 = pa, wpos1 = pa;
-    int t = 0, j = 0;
-    if (pa + lane < c) pair_rc(pa + lane, t, j);
-    constexpr int kAhead = 4;
-    uint32_t buf[kAhead];
-#pragma unroll
-    for (int d = 0; d < kAhead; d++) {
-      const int p = pa + 32 * d + lane;
-      buf[d] = (p < pb) ? dm[p] : 0u;
-    }
     const uint32_t below = (1u << lane) - 1u;
-    // unrolled by the prefetch depth: slot d is consumed and refilled with
-    // the chunk kAhead further on, so no register waits on a pending load
-    for (int base0 = pa; base0 < pb; base0 += 32 * kAhead)
-#pragma unroll
-    for (int d = 0; d < kAhead; d++) {
-      const int base = base0 + 32 * d;
-      if (base >= pb) break;
-      const uint32_t m = buf[d];
-      {
-        const int p = base + 32 * kAhead + lane;
-        buf[d] = (p < pb) ? dm[p] : 0u;
-      }
-      const bool in = base + lane < pb;
+    const uint32_t *cbits = chunk_bits(const_cast<uint32_t *>(bd.dmask), bd.B, c, u);
+    const int k0 = pa >> 5, k1 = (pb + 31) >> 5;  // chunks [k0, k1)
+    auto chunk = [&](int k, uint32_t m) {
+      const int p = 32 * k + lane;
+      const bool in = p >= pa && p < pb;
+      int t = 0, j = 0;
+      if (in) pair_rc(p, t, j);
       if (in && (m & 1u)) atomicOr(&P.rows[((size_t)0 * g + t) * GW + (j >> 5)], 1u << (j & 31));
       if (in && ((m >> 16) & 1u))
         atomicOr(&P.rows[((size_t)1 * g + t) * GW + (j >> 5)], 1u << (j & 31));
@@ -597,20 +586,39 @@ __global__ void __launch_bounds__(256, 3) k_units(const __grid_constant__ SetDev
         const bool flag = in && fb != 0u;
         const uint32_t bal = __ballot_sync(0xffffffffu, flag);
         const int wpos = cls ? wpos1 : wpos0;
-        const int before = wpos + __popc(bal & below);
+        const int pos = wpos + __popc(bal & below);
         if (flag) {
-          phi[cls][before] = ((uint32_t)(base + lane) << 9) | fb;
-          pcol[cls][before] = (uint16_t)j;
+          phi[cls][pos] = ((uint32_t)p << 9) | fb;
+          pcol[cls][pos] = (uint16_t)j;
+          atomicMin(&P.phs[cls * g + t], pos);
+          atomicMax(&P.phe[cls * g + t], pos + 1);
         }
-        if (in && j == 0) P.phs[cls * g + t] = before;
-        if (in && j == t - 1) P.phe[cls * g + t] = before + (flag ? 1 : 0);
         if (cls) wpos1 += __popc(bal); else wpos0 += __popc(bal);
       }
-      // this lane's next pair: 32 further on
-      j += 32;
-      while (t < g && j >= t) {
-        j -= t;
-        t++;
+    };
+    for (int kw = k0 >> 5; pa < pb && kw <= (k1 - 1) >> 5; kw++) {
+      uint32_t bits = cbits[kw];
+      if (kw == (k0 >> 5)) bits &= ~0u << (k0 & 31);
+      if (kw == ((k1 - 1) >> 5) && (k1 & 31)) bits &= ~0u >> (32 - (k1 & 31));
+      while (bits) {
+        int ks[4];
+        uint32_t mv[4];
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+          ks[q] = -1;
+          if (bits) {
+            ks[q] = 32 * kw + __ffs(bits) - 1;
+            bits &= bits - 1;
+          }
+        }
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+          const int p = 32 * ks[q] + lane;
+          mv[q] = (ks[q] >= 0 && p >= pa && p < pb) ? dm[p] : 0u;
+        }
+#pragma unroll
+        for (int q = 0; q < 4; q++)
+          if (ks[q] >= 0) chunk(ks[q], mv[q]);
       }
     }
   }

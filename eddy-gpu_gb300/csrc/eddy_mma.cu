@@ -421,7 +421,10 @@ __global__ void __maxnreg__(max_regs<kEpi>())
             (int)(it[2] & 0xFFFFu), (int)(it[2] >> 16), (int)(it[3] & 0xFFFFu), (int)(it[3] >> 16),
             (int)(it[4] & 0xFFFFu), prior, sd);
         const uint32_t m = (uint32_t)rr & 0x3FFu;
-        if (m) atomicOr(&dmask[(size_t)uu * sd.c + p], m << (16 * cls));
+        if (m) {
+          atomicOr(&dmask[(size_t)uu * sd.c + p], m << (16 * cls));
+          mark_chunk(dmask, B, sd.c, uu, p);
+        }
         nexact += (unsigned)(rr >> 32) & 0xFFFFu;
         nfilt += (unsigned)(rr >> 48) & 1u;
       }

@@ -51,7 +51,7 @@ constexpr size_t kOffPrior = kOffCtot + al256(2ull * 9 * kNAPairs);
 constexpr size_t kOffMask = kOffPrior + al256((size_t)kNAPairs);
 constexpr size_t kOffLg = kOffMask + al256(8ull * kNAW);
 constexpr size_t kOffDmask = kOffLg + al256(8ull * kDivisors * (kNAMaxSamples + 1));
-constexpr size_t kOffOut = kOffDmask + al256(4ull * kNAPairs);  // js, U, status
+constexpr size_t kOffOut = kOffDmask + al256(dmask_bytes(1, kNAPairs));  // js, U, status
 constexpr size_t kOffUnit = kOffOut + 256;
 
 }  // namespace
@@ -162,7 +162,10 @@ extern "C" int eddy_unit_noalloc(const eddy_opts *opts, const int8_t *vals, int 
   sd.lg_stride = n + 1;
   sd.lg_shift = shift;
 
-  if (launch_pairs(sd, (const uint64_t *)(base + kOffMask), (uint32_t *)(base + kOffDmask), 1,
+  // the chunk bitmap after the c masks is zeroed before the decision kernel
+  if (cudaMemsetAsync(base + kOffDmask + 4 * (size_t)c, 0, 4 * (size_t)chunk_words(c), st) !=
+          cudaSuccess ||
+      launch_pairs(sd, (const uint64_t *)(base + kOffMask), (uint32_t *)(base + kOffDmask), 1,
                    nullptr, st) != cudaSuccess)
     return EDDY_ERR_CUDA;
   double *d_js = (double *)(base + kOffOut);
