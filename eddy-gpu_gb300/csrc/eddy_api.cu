@@ -269,9 +269,9 @@ std::pair<int, int> tune_key(const SetDev &sd) {
 }
 
 int launch_pairs_any(eddy_ctx *ctx, const SetDev &sd, const uint64_t *masks, int B, uint32_t *dmask,
-                     unsigned long long *stats) {
+                     unsigned long long *stats, bool force_popc = false) {
   if (sd.c == 0) return EDDY_OK;
-  if (use_popc()) {
+  if (use_popc() || force_popc) {
     CK(launch_pairs(sd, masks, dmask, B, stats, ctx->stream));
     ctx->launches += 1;
     return EDDY_OK;
@@ -282,7 +282,7 @@ int launch_pairs_any(eddy_ctx *ctx, const SetDev &sd, const uint64_t *masks, int
     ctx->launches += 1;
     ctx->y_ready = true;
   }
-  CK(ctx->d_afp8.ensure(mma_a_bytes(B, sd.n, ctx->sms)));
+  CK(ctx->d_afp8.ensure(mma_a_bytes(B, sd.n, sd.c)));
   CK(ctx->d_err.ensure(sizeof(unsigned)));
   CK(cudaMemsetAsync(ctx->d_err.p, 0, sizeof(unsigned), ctx->stream));
   // untuned (batches below 512 units before the first tuning): the tile
@@ -311,7 +311,7 @@ int launch_pairs_any(eddy_ctx *ctx, const SetDev &sd, const uint64_t *masks, int
         best = ms;
         bi = v;
       }
-      ctx->launches += 2;
+      ctx->launches += 3;  // operand, GEMM + epilogue, general path
     }
     ctx->tuned[tune_key(sd)] = bi;
     variant = bi;
@@ -319,7 +319,7 @@ int launch_pairs_any(eddy_ctx *ctx, const SetDev &sd, const uint64_t *masks, int
   ctx->tuned_variant = variant;
   CK(launch_pairs_mma(sd, masks, B, ctx->d_afp8.as<uint8_t>(), ctx->d_Y.as<uint8_t>(), dmask, stats,
                       ctx->d_err.as<unsigned>(), ctx->sms, ctx->stream, variant));
-  ctx->launches += 2;
+  ctx->launches += 3;  // operand, GEMM + epilogue, general path
   return EDDY_OK;
 }
 
@@ -362,6 +362,7 @@ int run_units(eddy_ctx *ctx, SetRun &sr, int nunits, const uint64_t *masks_host,
   for (int b0 = 0; b0 < nunits; b0 += Bmax) {
     const int B = std::min(Bmax, nunits - b0);
     int kmax_run = kmax;
+    bool popc_batch = false;
     std::vector<int> todo(B);
     for (int i = 0; i < B; i++) todo[i] = i;
     // the batch is run once; units whose status asks for it are re-run
@@ -425,7 +426,8 @@ int run_units(eddy_ctx *ctx, SetRun &sr, int nunits, const uint64_t *masks_host,
       bd.stats = ctx->d_stats.as<unsigned long long>();
       CK(cudaEventRecord(ctx->ev[0], ctx->stream));
       {
-        int rc = launch_pairs_any(ctx, sd, bd.masks, Bt, ctx->d_dmask.as<uint32_t>(), bd.stats);
+        int rc = launch_pairs_any(ctx, sd, bd.masks, Bt, ctx->d_dmask.as<uint32_t>(), bd.stats,
+                                  popc_batch);
         if (rc) return rc;
       }
       CK(cudaEventRecord(ctx->ev[1], ctx->stream));
@@ -440,11 +442,17 @@ int run_units(eddy_ctx *ctx, SetRun &sr, int nunits, const uint64_t *masks_host,
       CK(cudaMemcpyAsync(status.data(), ctx->d_status.p, 4 * Bt, cudaMemcpyDeviceToHost, ctx->stream));
       // the tensor-core kernel's timeout word, read with the results
       unsigned errw = 0;
-      const bool mma_used = !use_popc() && ctx->d_err.p != nullptr && c > 0;
+      const bool mma_used = !use_popc() && !popc_batch && ctx->d_err.p != nullptr && c > 0;
       if (mma_used)
         CK(cudaMemcpyAsync(&errw, ctx->d_err.p, sizeof errw, cudaMemcpyDeviceToHost, ctx->stream));
       CK(cudaStreamSynchronize(ctx->stream));
-      if (errw) return fail(ctx, EDDY_ERR_INTERNAL, "tensor-core pipeline wait timed out");
+      if (errw & 1u) return fail(ctx, EDDY_ERR_INTERNAL, "tensor-core pipeline wait timed out");
+      if (errw & 2u) {
+        // the general-path queue overflowed (a large share of tables near a
+        // threshold): decide this batch with the popcount kernel
+        popc_batch = true;
+        continue;
+      }
       float a = 0, bms = 0;
       cudaEventElapsedTime(&a, ctx->ev[0], ctx->ev[1]);
       cudaEventElapsedTime(&bms, ctx->ev[1], ctx->ev[2]);

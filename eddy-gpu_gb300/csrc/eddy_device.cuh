@@ -265,28 +265,36 @@ __device__ __forceinline__ bool quick_zero(const TabInfo &ti, int prior, const S
 
 // quick_zero on the FP32 counts of the tensor-core epilogue: o = the nine
 // counts as exact floats.  Demands every marginal >= 2 (dof 4 in t and every
-// t', support unchanged), Yates off everywhere and N <= 4096 (every product
-// below an exact FP32 integer).  chi^2 = N (Q - 1), Q = sum o^2 / (R C), in
-// FP32 with |error| <= 1e-5 N (covered below); the leave-one-out bound as in
-// quick_zero.  chiA: the no-edge threshold of dof 4 (negative: never).
+// t', support unchanged), Yates off everywhere and N <= 4096, so that every
+// marginal product below is an exact FP32 integer.  The test of quick_zero,
+//   (N (rho - 1) + rho chi_hi) 1.0001 + 1e-3 < chiA,
+// chi_hi = N (Q - 1) + 1e-5 N, rho = rm cm / q, q = (rm - 1)(cm - 1),
+// multiplied through by q D with D = R0 R1 R2 C0 C1 C2 > 0, so no division
+// is left on the path:  Q D = sum_a PR_a sum_b o_ab^2 PC_b, PR_a / PC_b =
+// the products of the other two marginals.  FP32 error of Q D - D:
+// <= 6e-7 D (all products of marginals exact, o^2 exact), i.e. <= 6e-7 N in
+// chi^2, inside the 1e-5 N term; the other roundings are relative 1e-6,
+// inside the 1.0001 and 1e-3 terms.  chiA: the no-edge threshold of dof 4
+// (negative: never).
 __device__ __forceinline__ bool quick_zero_f(const float *o, float chiA) {
   const float R0 = o[0] + o[1] + o[2], R1 = o[3] + o[4] + o[5], R2 = o[6] + o[7] + o[8];
   const float C0 = o[0] + o[3] + o[6], C1 = o[1] + o[4] + o[7], C2 = o[2] + o[5] + o[8];
   const float N = R0 + R1 + R2;
   const float rm = fminf(R0, fminf(R1, R2)), cm = fminf(C0, fminf(C1, C2));
-  const float q = (rm - 1.f) * (cm - 1.f);
+  const float q = (rm - 1.f) * (cm - 1.f), rc = rm * cm;
   if (!(rm >= 2.f && cm >= 2.f && N >= 32.f && N <= 4096.f && q >= 5.f * (N - 1.f) &&
-        rm * cm >= 5.f * N))
+        rc >= 5.f * N))
     return false;
-  const float iC0 = rcp_approx(C0), iC1 = rcp_approx(C1), iC2 = rcp_approx(C2);
-  const float s0 = fmaf(o[0] * o[0], iC0, fmaf(o[1] * o[1], iC1, o[2] * o[2] * iC2));
-  const float s1 = fmaf(o[3] * o[3], iC0, fmaf(o[4] * o[4], iC1, o[5] * o[5] * iC2));
-  const float s2 = fmaf(o[6] * o[6], iC0, fmaf(o[7] * o[7], iC1, o[8] * o[8] * iC2));
-  const float Q = fmaf(s0, rcp_approx(R0), fmaf(s1, rcp_approx(R1), s2 * rcp_approx(R2)));
-  const float chi = N * (Q - 1.f) + 1e-5f * N;
-  const float r1 = (rm + cm - 1.f) * rcp_approx(q);  // rho - 1
-  const float bound = fmaf(N, r1, (1.f + r1) * chi) * 1.0001f + 1e-3f;
-  return bound < chiA;
+  const float PR0 = R1 * R2, PR1 = R0 * R2, PR2 = R0 * R1;
+  const float PC0 = C1 * C2, PC1 = C0 * C2, PC2 = C0 * C1;
+  const float D = (R0 * PR0) * (C0 * PC0);
+  const float s0 = fmaf(o[0] * o[0], PC0, fmaf(o[1] * o[1], PC1, o[2] * o[2] * PC2));
+  const float s1 = fmaf(o[3] * o[3], PC0, fmaf(o[4] * o[4], PC1, o[5] * o[5] * PC2));
+  const float s2 = fmaf(o[6] * o[6], PC0, fmaf(o[7] * o[7], PC1, o[8] * o[8] * PC2));
+  const float QD = fmaf(PR0, s0, fmaf(PR1, s1, PR2 * s2));
+  // q D bound = (N (rm + cm - 1) + rc (N (Q - 1) + 1e-5 N)) D
+  const float lhs = fmaf(N * (rm + cm - 1.f) + rc * (1e-5f * N), D, rc * N * (QD - D));
+  return fmaf(lhs, 1.0001f, 1e-3f * q * D) < chiA * q * D;
 }
 
 // The general path: full-table decision, the Minkowski leave-one-out filter

@@ -40,8 +40,9 @@ constexpr int kTM = 128, kPairsPerGroup = 3, kKC = 128;
 constexpr int kGroupPad = 24;
 constexpr int kMaxGroups = 8;
 constexpr unsigned long long kTimeoutNs = 2000000000ull;
-// general-path queue of an epilogue warp: room for every table of its tile
-// share (32 units x its pairs x 2 classes), 6 words each
+// tables the quick filter cannot settle go into one queue per launch (a
+// counter, then 6-word items) that k_general decides afterwards; a full
+// queue sets bit 2 of the error word and the batch is re-run elsewhere
 constexpr int kQWords = 6;
 // full-sample tables of one group: 3 pairs x 12 floats
 constexpr uint32_t kGroupCtBytes = kPairsPerGroup * 12 * sizeof(float);
@@ -199,7 +200,7 @@ __global__ void __maxnreg__(max_regs<kEpi>())
     k_pairs_mma(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
                 const __grid_constant__ SetDev sd, const float *__restrict__ ctotf, int B, int nk,
                 int ntiles, int mblocks, uint32_t *dmask, unsigned long long *stats,
-                unsigned *err, uint32_t *gqueue) {
+                unsigned *err, unsigned *gqueue, unsigned qcap) {
   constexpr int kTN = 32 * kGroups;
   constexpr int kPairsPerTile = kGroups * kPairsPerGroup;
   constexpr uint32_t kStageBytes = (kTM + kTN) * kKC;
@@ -208,7 +209,6 @@ __global__ void __maxnreg__(max_regs<kEpi>())
   constexpr uint32_t kIdesc = idesc_for(kTN);
   constexpr int kPerQuad = kEpi / 4, kGpw = kGroups / kPerQuad;
   static_assert(kEpi % 4 == 0 && kGroups % kPerQuad == 0 && kGroups <= kMaxGroups, "shape");
-  constexpr int kQCap = 32 * 2 * kPairsPerGroup * kGpw;
   extern __shared__ __align__(1024) uint8_t smraw[];
   // 1024-byte aligned stage ring, then barriers, then the epilogue buffer
   uint8_t *base = (uint8_t *)(((uintptr_t)smraw + 1023) & ~(uintptr_t)1023);
@@ -328,9 +328,7 @@ __global__ void __maxnreg__(max_regs<kEpi>())
     const float thr0 = sd.exact_all ? -1.f : sd.thr[0][2].chiA;
     const float thr1 = sd.exact_all ? -1.f : sd.thr[1][2].chiA;
     const uint32_t below = (1u << lane) - 1u;
-    // this warp's queue of tables for the general path (global memory: it
-    // is written for a small share of the tables)
-    uint32_t *gq = gqueue + ((size_t)blockIdx.x * kEpi + (warp - 2)) * kQCap * kQWords;
+    unsigned *qitems = gqueue + 4;
     for (int t = blockIdx.x; t < ntot && !*verr; t += gridDim.x) {
       const int tn = t / mblocks, mb = t % mblocks;
       if (!mbar_wait(smem_u32(&S.accfull[acc]), accphase, verr)) break;
@@ -340,23 +338,29 @@ __global__ void __maxnreg__(max_regs<kEpi>())
           reinterpret_cast<const float *>(base + kStages * kStageBytes + kCtOff + acc * kCtBytes);
       const int u = mb * kTM + row;
       const bool valid = u < B;
-      // tables the quick filter cannot settle are queued (counts, class,
-      // prior, pair, row) and decided after the loop, with the TMEM values
-      // no longer live
-      int nq = 0;
+      // tables the quick filter cannot settle: counts, unit, class, prior
+      // and pair into the launch's queue (one atomic per warp and call)
       auto enqueue = [&](bool flag, const float *o, int cls, int prior, int p) {
         const uint32_t bal = __ballot_sync(0xffffffffu, flag);
+        if (bal == 0u) return;
+        unsigned qbase = 0;
+        if (lane == 0) qbase = atomicAdd(gqueue, (unsigned)__popc(bal));
+        qbase = __shfl_sync(0xffffffffu, qbase, 0);
         if (flag) {
-          uint32_t *it = gq + (size_t)(nq + __popc(bal & below)) * kQWords;
-          it[0] = (uint32_t)o[0] | ((uint32_t)o[1] << 16);
-          it[1] = (uint32_t)o[2] | ((uint32_t)o[3] << 16);
-          it[2] = (uint32_t)o[4] | ((uint32_t)o[5] << 16);
-          it[3] = (uint32_t)o[6] | ((uint32_t)o[7] << 16);
-          it[4] = (uint32_t)o[8] | ((uint32_t)row << 16) | ((uint32_t)cls << 24) |
-                  ((uint32_t)prior << 25);
-          it[5] = (uint32_t)p;
+          const unsigned idx = qbase + (unsigned)__popc(bal & below);
+          if (idx < qcap) {
+            unsigned *it = qitems + (size_t)idx * kQWords;
+            it[0] = (uint32_t)o[0] | ((uint32_t)o[1] << 16);
+            it[1] = (uint32_t)o[2] | ((uint32_t)o[3] << 16);
+            it[2] = (uint32_t)o[4] | ((uint32_t)o[5] << 16);
+            it[3] = (uint32_t)o[6] | ((uint32_t)o[7] << 16);
+            it[4] = (uint32_t)o[8] | ((uint32_t)u << 16) | ((uint32_t)cls << 28) |
+                    ((uint32_t)prior << 29);
+            it[5] = (uint32_t)p;
+          } else {
+            atomicOr(err, 2u);
+          }
         }
-        nq += __popc(bal);
       };
       // one pair: class-1 counts cv (FP32 integers from TMEM), class 2 =
       // full-sample table - class 1
@@ -383,26 +387,20 @@ __global__ void __maxnreg__(max_regs<kEpi>())
           ntab += 2;
         }
       };
-      // each column group in two 16-column TMEM loads: pair 0 = columns 0-8,
-      // pair 1 = 9-17, pair 2 = 18-26
+      // the warp's column groups out of TMEM, every load issued before one
+      // wait; pair q of a group = columns 9q .. 9q+8
+      uint32_t r[kGpw][32];
 #pragma unroll
       for (int gi = 0; gi < kGpw; gi++) {
         const int grp = wq + gi * kPerQuad;
-        const uint32_t ta = tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)(acc * kTN + grp * 32);
-        uint32_t lo[16], hi[16], cv[9];
-        tmem_ld16(ta, lo);
-        tmem_ld_wait();
+        tmem_ld32(tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)(acc * kTN + grp * 32), r[gi]);
+      }
+      tmem_ld_wait();
 #pragma unroll
-        for (int k = 0; k < 9; k++) cv[k] = lo[k];
-        do_pair(cv, grp, 0);
-        tmem_ld16(ta + 16, hi);
-        tmem_ld_wait();
+      for (int gi = 0; gi < kGpw; gi++) {
+        const int grp = wq + gi * kPerQuad;
 #pragma unroll
-        for (int k = 0; k < 9; k++) cv[k] = (9 + k < 16) ? lo[9 + k] : hi[9 + k - 16];
-        do_pair(cv, grp, 1);
-#pragma unroll
-        for (int k = 0; k < 9; k++) cv[k] = hi[2 + k];
-        do_pair(cv, grp, 2);
+        for (int q = 0; q < kPairsPerGroup; q++) do_pair(&r[gi][9 * q], grp, q);
       }
       // the slot (accumulator and table buffer) is free again
       tc_fence_before();
@@ -411,24 +409,6 @@ __global__ void __maxnreg__(max_regs<kEpi>())
         acc = 0;
         accphase ^= 1u;
       }
-      __syncwarp();
-      for (int i = lane; i < nq; i += 32) {
-        const uint32_t *it = gq + (size_t)i * kQWords;
-        const int cls = (it[4] >> 24) & 1, prior = (it[4] >> 25) & 1;
-        const int uu = mb * kTM + (int)((it[4] >> 16) & 0xFFu), p = (int)it[5];
-        const uint64_t rr = pair_mask_general(
-            (int)(it[0] & 0xFFFFu), (int)(it[0] >> 16), (int)(it[1] & 0xFFFFu), (int)(it[1] >> 16),
-            (int)(it[2] & 0xFFFFu), (int)(it[2] >> 16), (int)(it[3] & 0xFFFFu), (int)(it[3] >> 16),
-            (int)(it[4] & 0xFFFFu), prior, sd);
-        const uint32_t m = (uint32_t)rr & 0x3FFu;
-        if (m) {
-          atomicOr(&dmask[(size_t)uu * sd.c + p], m << (16 * cls));
-          mark_chunk(dmask, B, sd.c, uu, p);
-        }
-        nexact += (unsigned)(rr >> 32) & 0xFFFFu;
-        nfilt += (unsigned)(rr >> 48) & 1u;
-      }
-      __syncwarp();
     }
     if (stats) {
       for (int o = 16; o > 0; o >>= 1) {
@@ -449,6 +429,43 @@ __global__ void __maxnreg__(max_regs<kEpi>())
     tc_fence_after();
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
                  "n"(kTmemCols));
+  }
+}
+
+// The general path for the queued tables of a launch: full-table decision,
+// the Minkowski leave-one-out filter, the cell-removed tables (FP32 with the
+// exact FP64 fallback); one thread per table, results OR-ed into the masks.
+__global__ void __launch_bounds__(256) k_general(const __grid_constant__ SetDev sd,
+                                                 const unsigned *queue, unsigned qcap, int B,
+                                                 uint32_t *dmask, unsigned long long *stats) {
+  const unsigned cnt = queue[0] < qcap ? queue[0] : qcap;
+  const unsigned *items = queue + 4;
+  unsigned nexact = 0, nfilt = 0;
+  for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < cnt; i += gridDim.x * blockDim.x) {
+    const unsigned *it = items + (size_t)i * kQWords;
+    const int u = (int)((it[4] >> 16) & 0xFFFu), cls = (it[4] >> 28) & 1,
+              prior = (it[4] >> 29) & 1, p = (int)it[5];
+    const uint64_t rr = pair_mask_general(
+        (int)(it[0] & 0xFFFFu), (int)(it[0] >> 16), (int)(it[1] & 0xFFFFu), (int)(it[1] >> 16),
+        (int)(it[2] & 0xFFFFu), (int)(it[2] >> 16), (int)(it[3] & 0xFFFFu), (int)(it[3] >> 16),
+        (int)(it[4] & 0xFFFFu), prior, sd);
+    const uint32_t m = (uint32_t)rr & 0x3FFu;
+    if (m) {
+      atomicOr(&dmask[(size_t)u * sd.c + p], m << (16 * cls));
+      mark_chunk(dmask, B, sd.c, u, p);
+    }
+    nexact += (unsigned)(rr >> 32) & 0xFFFFu;
+    nfilt += (unsigned)(rr >> 48) & 1u;
+  }
+  if (stats) {
+    for (int o = 16; o > 0; o >>= 1) {
+      nexact += __shfl_down_sync(0xffffffffu, nexact, o);
+      nfilt += __shfl_down_sync(0xffffffffu, nfilt, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+      if (nexact) atomicAdd(&stats[0], (unsigned long long)nexact);
+      if (nfilt) atomicAdd(&stats[2], (unsigned long long)nfilt);
+    }
   }
 }
 
@@ -568,11 +585,14 @@ size_t mma_y_bytes(int c, int n) {
 }
 int mma_bpad(int B) { return (B + kTM - 1) / kTM * kTM; }
 static size_t a_operand_bytes(int B, int n) { return (size_t)mma_bpad(B) * mma_npad(n); }
-// the A operand, then the general-path queues of up to `sms` CTAs (a CTA's
-// queues hold 32 units x 3 pairs x 2 classes per group and quadrant)
-size_t mma_a_bytes(int B, int n, int sms) {
-  return a_operand_bytes(B, n) + (size_t)sms * 4 * 32 * 2 * kPairsPerGroup * kMaxGroups *
-                                     kQWords * sizeof(uint32_t);
+// the A operand, then the general-path queue: a 16-byte counter and room
+// for 1/8 of the batch's tables (at least 65536)
+static unsigned queue_cap(int B, int c) {
+  const size_t t = (size_t)B * (c > 0 ? c : 1) * 2 / 8;
+  return (unsigned)(t < 65536 ? 65536 : t);
+}
+size_t mma_a_bytes(int B, int n, int c) {
+  return a_operand_bytes(B, n) + 16 + (size_t)queue_cap(B, c) * kQWords * sizeof(uint32_t);
 }
 
 cudaError_t launch_build_y(const SetDev &sd, uint8_t *Y, cudaStream_t st) {
@@ -589,7 +609,7 @@ cudaError_t launch_build_y(const SetDev &sd, uint8_t *Y, cudaStream_t st) {
 
 template <int kStages, int kEpi, int kGroups>
 static cudaError_t launch_variant(const SetDev &sd, const uint8_t *Afp8, const uint8_t *Y,
-                                  uint32_t *gqueue, int B, uint32_t *dmask,
+                                  unsigned *gqueue, unsigned qcap, int B, uint32_t *dmask,
                                   unsigned long long *stats, unsigned *err, int sms,
                                   cudaStream_t st) {
   constexpr int kTN = 32 * kGroups;
@@ -608,7 +628,10 @@ static cudaError_t launch_variant(const SetDev &sd, const uint8_t *Afp8, const u
   const int ntot = nt * mblocks;
   const int grid = ntot < sms ? ntot : sms;
   kern<<<grid, 32 * (2 + kEpi), smem, st>>>(ma, mb, sd, ctotf, B, np / kKC, nt, mblocks, dmask,
-                                            stats, err, gqueue);
+                                            stats, err, gqueue, qcap);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  k_general<<<sms * 4, 256, 0, st>>>(sd, gqueue, qcap, B, dmask, stats);
   return cudaGetLastError();
 }
 
@@ -622,16 +645,19 @@ cudaError_t launch_pairs_mma(const SetDev &sd, const uint64_t *masks, int B, uin
   const int np = mma_npad(sd.n), Bp = mma_bpad(B);
   const long long work = (long long)Bp * (np / 16);
   k_masks_fp8<<<(unsigned)((work + 255) / 256), 256, 0, st>>>(masks, B, Bp, sd.W, np, Afp8);
-  uint32_t *gqueue = reinterpret_cast<uint32_t *>(Afp8 + a_operand_bytes(B, sd.n));
+  unsigned *gqueue = reinterpret_cast<unsigned *>(Afp8 + a_operand_bytes(B, sd.n));
+  const unsigned qcap = queue_cap(B, sd.c);
+  cudaError_t e = cudaMemsetAsync(gqueue, 0, 16, st);
+  if (e != cudaSuccess) return e;
   switch (variant) {
     case 1:
-      return launch_variant<6, 8, 4>(sd, Afp8, Y, gqueue, B, dmask, stats, err, sms, st);
+      return launch_variant<6, 8, 4>(sd, Afp8, Y, gqueue, qcap, B, dmask, stats, err, sms, st);
     case 2:
-      return launch_variant<5, 12, 6>(sd, Afp8, Y, gqueue, B, dmask, stats, err, sms, st);
+      return launch_variant<5, 12, 6>(sd, Afp8, Y, gqueue, qcap, B, dmask, stats, err, sms, st);
     case 3:
-      return launch_variant<4, 8, 8>(sd, Afp8, Y, gqueue, B, dmask, stats, err, sms, st);
+      return launch_variant<4, 8, 8>(sd, Afp8, Y, gqueue, qcap, B, dmask, stats, err, sms, st);
     default:
-      return launch_variant<6, 16, 4>(sd, Afp8, Y, gqueue, B, dmask, stats, err, sms, st);
+      return launch_variant<6, 16, 4>(sd, Afp8, Y, gqueue, qcap, B, dmask, stats, err, sms, st);
   }
 }
 

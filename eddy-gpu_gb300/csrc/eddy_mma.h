@@ -11,14 +11,17 @@ namespace eddy {
 int mma_ngroups_pad(int c);
 int mma_npad(int n);
 int mma_bpad(int B);
-// bytes of the Afp8 scratch for a batch of B units (operand + queues)
-size_t mma_a_bytes(int B, int n, int sms);
+// bytes of the Afp8 scratch for a batch of B units of a set with c pairs
+// (operand + general-path queue)
+size_t mma_a_bytes(int B, int n, int c);
 size_t mma_y_bytes(int c, int n);
 // Builds the pair-cell indicator operand Y of the current set and, after it,
 // the FP32 copy of the full-sample tables the epilogue reads.
 cudaError_t launch_build_y(const SetDev &sd, uint8_t *Y, cudaStream_t st);
-// Masks -> e4m3 operand (Afp8, mma_a_bytes(B, n, sms) bytes), then the
-// GEMM + decision kernel; *err is set on a bounded-wait timeout.
+// Masks -> e4m3 operand (Afp8, mma_a_bytes(B, n, c) bytes), then the GEMM +
+// decision kernel and the general-path kernel for the tables its filter
+// could not settle.  *err: bit 0 = a bounded wait timed out, bit 1 = the
+// general-path queue overflowed (the batch must be decided another way).
 // variants (mma_variants()): tile widths N = 128 / 192 / 256 with 16, 8, 12
 // or 8 epilogue warps, one CTA per SM.
 int mma_variants();
