@@ -467,13 +467,28 @@ static __device__ int64_t bdeu_score(const SetDev &sd, int t, int np, const int 
   return score;
 }
 
-// Warp-cooperative form of bdeu_score for np >= 1: the lanes split the
-// 64-bit sample words, counts are summed with redux.sync, every lane returns
-// the score.  Same arithmetic and summation order of the fixed-point terms.
-static __device__ int64_t bdeu_score_warp(const SetDev &sd, int t, int np, const int *ps,
-                                          const uint64_t *m, const uint16_t *cnt3, int lane) {
+// Parent configurations of node t's score (np >= 1 parents) in one class:
+// q = product of the parents' observed-state counts (0: the score is 0).
+__device__ __forceinline__ int bdeu_q(const uint16_t *cnt3, int np, int p0, int p1, int p2) {
+  const int idx[3] = {p0, p1, p2};
+  int q = 1;
+  for (int k = 0; k < np; k++) {
+    const uint16_t *c = cnt3 + idx[k] * 3;
+    q *= (c[0] > 0) + (c[1] > 0) + (c[2] > 0);
+  }
+  return q;
+}
+
+// One parent configuration j of node t's score over class mask m (the
+// terms of kernel5.cu:30-218 for that j): sum_k LG(q r)[N_jk] - LG(q)[N_j].
+// Summing the terms of all j gives bdeu_score (fixed point, exact).
+// dmap: the divisor map in shared memory.
+static __device__ __noinline__ int64_t bdeu_config_term(const SetDev &sd, int t, int np, int p0,
+                                                        int p1, int p2, const uint64_t *m,
+                                                        const uint16_t *cnt3, int j,
+                                                        const int8_t *dmap) {
   int nstate[4], st[4][3];
-  int idx[4] = {t, np > 0 ? ps[0] : 0, np > 1 ? ps[1] : 0, np > 2 ? ps[2] : 0};
+  const int idx[4] = {t, p0, p1, p2};
   for (int k = 0; k <= np; k++) {
     int c = 0;
     for (int a = 0; a < 3; a++)
@@ -483,42 +498,35 @@ static __device__ int64_t bdeu_score_warp(const SetDev &sd, int t, int np, const
   const int r = nstate[0];
   int q = 1;
   for (int k = 1; k <= np; k++) q *= nstate[k];
-  if (q == 0) return 0;
-  const int64_t *LGq = sd.lg + (size_t)c_dmap[q] * sd.lg_stride;
-  const int64_t *LGqr = (r > 0) ? sd.lg + (size_t)c_dmap[q * r] * sd.lg_stride : nullptr;
   const int W = sd.W;
   const uint64_t *P = sd.planes;
+  const int64_t *LGq = sd.lg + (size_t)dmap[q] * sd.lg_stride;
+  const int64_t *LGqr = (r > 0) ? sd.lg + (size_t)dmap[q * r] * sd.lg_stride : LGq;
+  int rem = j;
+  const uint64_t *pp[3] = {P, P, P};
+  for (int k = 1; k <= np; k++) {
+    const int s = st[k][rem % nstate[k]];
+    rem /= nstate[k];
+    pp[k - 1] = P + ((size_t)idx[k] * 3 + s) * W;
+  }
   const uint64_t *pt0 = P + ((size_t)t * 3 + (r > 0 ? st[0][0] : 0)) * W;
   const uint64_t *pt1 = P + ((size_t)t * 3 + (r > 1 ? st[0][1] : 0)) * W;
   const uint64_t *pt2 = P + ((size_t)t * 3 + (r > 2 ? st[0][2] : 0)) * W;
-  int64_t score = 0;
-  for (int j = 0; j < q; j++) {
-    int rem = j;
-    const uint64_t *pp[3] = {P, P, P};
-    for (int k = 1; k <= np; k++) {
-      int s = st[k][rem % nstate[k]];
-      rem /= nstate[k];
-      pp[k - 1] = P + ((size_t)idx[k] * 3 + s) * W;
-    }
-    unsigned c0 = 0, c1 = 0, c2 = 0;
-    for (int w = lane; w < W; w += 32) {
-      uint64_t pm = m[w] & pp[0][w];
-      if (np > 1) pm &= pp[1][w];
-      if (np > 2) pm &= pp[2][w];
-      c0 += __popcll(pm & pt0[w]);
-      c1 += __popcll(pm & pt1[w]);
-      c2 += __popcll(pm & pt2[w]);
-    }
-    c0 = __reduce_add_sync(0xffffffffu, c0);
-    c1 = __reduce_add_sync(0xffffffffu, c1);
-    c2 = __reduce_add_sync(0xffffffffu, c2);
-    int nij = 0;
-    if (r > 0) { nij += (int)c0; score += LGqr[c0]; }
-    if (r > 1) { nij += (int)c1; score += LGqr[c1]; }
-    if (r > 2) { nij += (int)c2; score += LGqr[c2]; }
-    score -= LGq[nij];
+  int c0 = 0, c1 = 0, c2 = 0;
+  for (int w = 0; w < W; w++) {
+    uint64_t pm = m[w] & pp[0][w];
+    if (np > 1) pm &= pp[1][w];
+    if (np > 2) pm &= pp[2][w];
+    c0 += __popcll(pm & pt0[w]);
+    c1 += __popcll(pm & pt1[w]);
+    c2 += __popcll(pm & pt2[w]);
   }
-  return score;
+  int64_t term = 0;
+  int nij = 0;
+  if (r > 0) { nij += c0; term += LGqr[c0]; }
+  if (r > 1) { nij += c1; term += LGqr[c1]; }
+  if (r > 2) { nij += c2; term += LGqr[c2]; }
+  return term - LGq[nij];
 }
 
 }  // namespace eddy

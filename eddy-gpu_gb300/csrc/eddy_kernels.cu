@@ -283,7 +283,8 @@ struct UnitSmem {
   long long red_l[32];
 };
 
-constexpr int kMemo = 512;
+// BDeu work items (node scores) processed per round
+constexpr int kItems = 512;
 
 struct UnitPtrs {
   uint64_t *mA, *mB;      // [W]
@@ -297,8 +298,10 @@ struct UnitPtrs {
   uint16_t *dab;          // [g] nodes whose full lists differ between classes
   uint16_t *rphi;         // [2][g] rows that hold flip entries, per class
   int8_t *stsig;          // [nwarps][g] states at sigma
-  unsigned long long *mkey;  // [kMemo]
-  long long *mval;           // [kMemo][2]
+  unsigned long long *itk;   // [kItems] node-score items: t | np << 14 | parents
+  long long *acc;            // [kItems][2] their scores per class
+  int *tq;                   // [2 kItems + 1] task prefix per (item, class)
+  int8_t *dmap;              // [96] divisor map (copy of the constant one)
   long long *fsc;            // [2 full][2 data][g] base node scores
 };
 
@@ -316,8 +319,10 @@ __host__ __device__ inline size_t unit_smem_bytes(int g, int W, int GW, int nwar
   o = al(o) + sizeof(uint16_t) * g;
   o = al(o) + 2 * sizeof(uint16_t) * g;
   o = al(o) + (size_t)nwarps * g;
-  o = al(o) + sizeof(unsigned long long) * kMemo;
-  o = al(o) + 2 * sizeof(long long) * kMemo;
+  o = al(o) + sizeof(unsigned long long) * kItems;
+  o = al(o) + 2 * sizeof(long long) * kItems;
+  o = al(o) + sizeof(int) * (2 * kItems + 1);
+  o = al(o) + 96;
   o = al(o) + 4 * sizeof(long long) * g;
   return al(o);
 }
@@ -339,8 +344,10 @@ __device__ inline UnitPtrs carve(char *base, int g, int W, int GW, int nwarps) {
   o = al(o); P.dab = (uint16_t *)(base + o); o += sizeof(uint16_t) * g;
   o = al(o); P.rphi = (uint16_t *)(base + o); o += 2 * sizeof(uint16_t) * g;
   o = al(o); P.stsig = (int8_t *)(base + o); o += (size_t)nwarps * g;
-  o = al(o); P.mkey = (unsigned long long *)(base + o); o += sizeof(unsigned long long) * kMemo;
-  o = al(o); P.mval = (long long *)(base + o); o += 2 * sizeof(long long) * kMemo;
+  o = al(o); P.itk = (unsigned long long *)(base + o); o += sizeof(unsigned long long) * kItems;
+  o = al(o); P.acc = (long long *)(base + o); o += 2 * sizeof(long long) * kItems;
+  o = al(o); P.tq = (int *)(base + o); o += sizeof(int) * (2 * kItems + 1);
+  o = al(o); P.dmap = (int8_t *)(base + o); o += 96;
   o = al(o); P.fsc = (long long *)(base + o);
   return P;
 }
@@ -386,64 +393,62 @@ __device__ bool lists_equal(const SetDev &sd, const UnitPtrs &P, const uint32_t 
   return true;
 }
 
-__device__ __forceinline__ unsigned long long memo_key(int t, int np, const int *ps) {
-  unsigned long long k = (unsigned long long)t | ((unsigned long long)np << 14);
-  for (int i = 0; i < 3; i++)
-    k |= (unsigned long long)(i < np ? (ps[i] & 0xFFFF) : 0xFFFF) << (16 + 16 * i);
-  return k;
+
+// Node scores of `n` items, kItems per round, as a flat task list over the
+// block: task (item, class, parent configuration j).  get(i) -> the item's
+// key (t | np << 14 | p0 << 16 | p1 << 32 | p2 << 48; np = 0 or a key of ~0
+// = nothing to score); emit(i, class-1 score, class-2 score).  Fixed-point
+// terms are summed with atomics: exact, in any order.
+template <class Get, class Emit>
+__device__ void bdeu_items(const SetDev &sd, const UnitPtrs &P, int *scan, int n, Get get,
+                           Emit emit) {
+  const int tid = threadIdx.x, nt = blockDim.x, g = sd.g;
+  for (int b0 = 0; b0 < n; b0 += kItems) {
+    const int m = n - b0 < kItems ? n - b0 : kItems;
+    for (int i = tid; i < m; i += nt) {
+      const unsigned long long key = get(b0 + i);
+      P.itk[i] = key;
+      const int np = (key == ~0ull) ? 0 : (int)((key >> 14) & 3);
+      const int p0 = (int)((key >> 16) & 0xFFFF), p1 = (int)((key >> 32) & 0xFFFF),
+                p2 = (int)((key >> 48) & 0xFFFF);
+      for (int cls = 0; cls < 2; cls++) {
+        P.tq[2 * i + cls] = np ? bdeu_q(P.cnt3 + 3 * g * cls, np, p0, p1, p2) : 0;
+        P.acc[2 * i + cls] = 0;
+      }
+    }
+    __syncthreads();
+    int running = 0;
+    for (int c0 = 0; c0 < 2 * m; c0 += nt) {
+      const int e = c0 + tid;
+      const int v = e < 2 * m ? P.tq[e] : 0;
+      int total;
+      const int off = block_scan(v, total, scan);
+      if (e < 2 * m) P.tq[e] = running + off;
+      running += total;
+    }
+    __syncthreads();
+    for (int task = tid; task < running; task += nt) {
+      int lo = 0, hi = 2 * m - 1;
+      while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (P.tq[mid] <= task) lo = mid;
+        else hi = mid - 1;
+      }
+      const int i = lo >> 1, cls = lo & 1, j = task - P.tq[lo];
+      const unsigned long long key = P.itk[i];
+      const int t = (int)(key & 0x3FFF), np = (int)((key >> 14) & 3);
+      const long long term = bdeu_config_term(
+          sd, t, np, (int)((key >> 16) & 0xFFFF), (int)((key >> 32) & 0xFFFF),
+          (int)((key >> 48) & 0xFFFF), cls ? P.mB : P.mA, P.cnt3 + 3 * g * cls, j, P.dmap);
+      atomicAdd((unsigned long long *)&P.acc[2 * i + cls], (unsigned long long)term);
+    }
+    __syncthreads();
+    for (int i = tid; i < m; i += nt) emit(b0 + i, P.acc[2 * i], P.acc[2 * i + 1]);
+    __syncthreads();
+  }
 }
 
-// Memo of node scores per unit: open addressing over kMemo slots, 8 probes;
-// a slot whose values are not yet written counts as a miss.
-__device__ __forceinline__ bool memo_get(const UnitPtrs &P, unsigned h, unsigned long long key,
-                                         long long &a, long long &b) {
-  for (int probe = 0; probe < 8; probe++) {
-    unsigned slot = (h + probe) & (kMemo - 1);
-    unsigned long long kk = P.mkey[slot];
-    if (kk == key) {
-      __threadfence_block();
-      a = P.mval[2 * slot];
-      b = P.mval[2 * slot + 1];
-      return a != LLONG_MIN && b != LLONG_MIN;
-    }
-    if (kk == ~0ull) return false;
-  }
-  return false;
-}
-__device__ __forceinline__ void memo_put(const UnitPtrs &P, unsigned h, unsigned long long key,
-                                         const long long out[2]) {
-  for (int probe = 0; probe < 8; probe++) {
-    unsigned slot = (h + probe) & (kMemo - 1);
-    unsigned long long prev = atomicCAS(&P.mkey[slot], ~0ull, key);
-    if (prev == ~0ull) {
-      P.mval[2 * slot] = out[0];
-      P.mval[2 * slot + 1] = out[1];
-      return;
-    }
-    if (prev == key) return;
-  }
-}
 
-// Scores of (t, parents) for both data classes, memoised per unit, one warp
-// per node (np >= 1): lanes share the counting; every lane returns them.
-__device__ void scores_of_warp(const SetDev &sd, const UnitPtrs &P, int t, int np, const int *ps,
-                               long long out[2], int lane) {
-  const unsigned long long key = memo_key(t, np, ps);
-  const unsigned h = (unsigned)(mix64(key) & (kMemo - 1));
-  int hit = 0;
-  long long a = 0, b = 0;
-  if (lane == 0) hit = memo_get(P, h, key, a, b) ? 1 : 0;
-  hit = __shfl_sync(0xffffffffu, hit, 0);
-  if (hit) {
-    out[0] = __shfl_sync(0xffffffffu, a, 0);
-    out[1] = __shfl_sync(0xffffffffu, b, 0);
-    return;
-  }
-  out[0] = bdeu_score_warp(sd, t, np, ps, P.mA, P.cnt3, lane);
-  out[1] = bdeu_score_warp(sd, t, np, ps, P.mB, P.cnt3 + 3 * sd.g, lane);
-  if (lane == 0) memo_put(P, h, key, out);
-  __syncwarp();
-}
 
 __global__ void __launch_bounds__(256, 3) k_units(const __grid_constant__ SetDev sd,
                                                  const __grid_constant__ BatchDev bd) {
@@ -490,11 +495,7 @@ __global__ void __launch_bounds__(256, 3) k_units(const __grid_constant__ SetDev
   for (int i = tid; i < 2 * g * GW; i += nt) P.rows[i] = 0;
   // entry ranges of rows: start = INT_MAX, end = 0 until an entry lands
   for (int i = tid; i < 4 * g; i += nt) P.phs[i] = (i < 2 * g) ? 0x7fffffff : 0;
-  for (int i = tid; i < kMemo; i += nt) {
-    P.mkey[i] = ~0ull;
-    P.mval[2 * i] = LLONG_MIN;
-    P.mval[2 * i + 1] = LLONG_MIN;
-  }
+  for (int i = tid; i < 82; i += nt) P.dmap[i] = c_dmap[i];
   // hash tables, 16 bytes per store (HT is a power of two >= 8)
   for (int i = tid; i < L.HT / 2; i += nt) {
     reinterpret_cast<uint4 *>(htk)[i] = make_uint4(~0u, ~0u, ~0u, ~0u);
@@ -643,7 +644,9 @@ __global__ void __launch_bounds__(256, 3) k_units(const __grid_constant__ SetDev
   }
   __syncthreads();
 
-  // ---- P2: capped lists of the two full networks
+  // ---- P2: capped lists of the two full networks; their hashes summed per
+  // warp, then one atomic per warp and class
+  unsigned long long hsum[2] = {0ull, 0ull};
   for (int i = tid; i < 2 * g; i += nt) {
     const int k = i / g, t = i % g;
     ListGen G;
@@ -661,7 +664,15 @@ __global__ void __launch_bounds__(256, 3) k_units(const __grid_constant__ SetDev
     P.fcnt[i] = (uint16_t)cnt;
     for (int q = 0; q < 3; q++) P.fps[i * 3 + q] = (uint16_t)ps[q];
     P.fh[i] = h;
-    atomicAdd(&SM.HF[k], (unsigned long long)h);
+    hsum[k] += h;
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    hsum[0] += __shfl_xor_sync(0xffffffffu, hsum[0], o);
+    hsum[1] += __shfl_xor_sync(0xffffffffu, hsum[1], o);
+  }
+  if (lane == 0) {
+    atomicAdd(&SM.HF[0], hsum[0]);
+    atomicAdd(&SM.HF[1], hsum[1]);
   }
   __syncthreads();
   for (int t = tid; t < g; t += nt) {
@@ -1033,30 +1044,44 @@ __global__ void __launch_bounds__(256, 3) k_units(const __grid_constant__ SetDev
   if (bd.stats && tid == 0) atomicAdd(&bd.stats[3], (unsigned long long)(S - U));
 
   // ---- P5: BDeu.  Base node scores of the two full networks: nodes
-  // without parents thread by thread (from the state counts), the others
-  // warp by warp.
+  // without parents from the state counts, the others as flat tasks; a
+  // class-2 node whose capped parents equal the class-1 one copies its score.
+  auto same_as_class1 = [&](int t) -> bool {
+    const int a = P.fcnt[t] < 3 ? P.fcnt[t] : 3, b = P.fcnt[g + t] < 3 ? P.fcnt[g + t] : 3;
+    if (a != b) return false;
+    for (int q = 0; q < a; q++)
+      if (P.fps[t * 3 + q] != P.fps[(g + t) * 3 + q]) return false;
+    return true;
+  };
   for (int i = tid; i < 2 * g; i += nt) {
     if (P.fcnt[i] != 0) continue;
     const int k = i / g, t = i % g;
     int ps[3] = {0xFFFF, 0xFFFF, 0xFFFF};
-    long long sc[2];
-    sc[0] = bdeu_score(sd, t, 0, ps, P.mA, P.cnt3);
-    sc[1] = bdeu_score(sd, t, 0, ps, P.mB, P.cnt3 + 3 * g);
-    P.fsc[(k * 2 + 0) * g + t] = sc[0];
-    P.fsc[(k * 2 + 1) * g + t] = sc[1];
+    P.fsc[(k * 2 + 0) * g + t] = bdeu_score(sd, t, 0, ps, P.mA, P.cnt3);
+    P.fsc[(k * 2 + 1) * g + t] = bdeu_score(sd, t, 0, ps, P.mB, P.cnt3 + 3 * g);
   }
-  for (int i = warp; i < 2 * g; i += nw) {
-    if (P.fcnt[i] == 0) continue;
-    const int k = i / g, t = i % g;
-    int np = P.fcnt[i] < 3 ? P.fcnt[i] : 3;
-    int ps[3] = {P.fps[i * 3], P.fps[i * 3 + 1], P.fps[i * 3 + 2]};
-    long long sc[2];
-    scores_of_warp(sd, P, t, np, ps, sc, lane);
-    if (lane == 0) {
-      P.fsc[(k * 2 + 0) * g + t] = sc[0];
-      P.fsc[(k * 2 + 1) * g + t] = sc[1];
+  bdeu_items(
+      sd, P, SM.scan, 2 * g,
+      [&](int i) -> unsigned long long {
+        const int k = i / g, t = i % g;
+        if (P.fcnt[i] == 0 || (k == 1 && same_as_class1(t))) return ~0ull;
+        const int np = P.fcnt[i] < 3 ? P.fcnt[i] : 3;
+        return (unsigned long long)t | ((unsigned long long)np << 14) |
+               ((unsigned long long)P.fps[i * 3] << 16) |
+               ((unsigned long long)P.fps[i * 3 + 1] << 32) |
+               ((unsigned long long)P.fps[i * 3 + 2] << 48);
+      },
+      [&](int i, long long s1, long long s2) {
+        const int k = i / g, t = i % g;
+        if (P.fcnt[i] == 0 || (k == 1 && same_as_class1(t))) return;
+        P.fsc[(k * 2 + 0) * g + t] = s1;
+        P.fsc[(k * 2 + 1) * g + t] = s2;
+      });
+  for (int t = tid; t < g; t += nt)
+    if (P.fcnt[g + t] != 0 && same_as_class1(t)) {
+      P.fsc[(1 * 2 + 0) * g + t] = P.fsc[(0 * 2 + 0) * g + t];
+      P.fsc[(1 * 2 + 1) * g + t] = P.fsc[(0 * 2 + 1) * g + t];
     }
-  }
   __syncthreads();
   for (int i = tid; i < 4; i += nt) {
     const int k = i / 2, cls = i % 2;
@@ -1065,39 +1090,77 @@ __global__ void __launch_bounds__(256, 3) k_units(const __grid_constant__ SetDev
     SM.base[cls][k] = s;
   }
   __syncthreads();
-  // per unique network (warp by warp): base + deltas of its changed nodes
-  for (int uu = warp; uu < U; uu += nw) {
-    const int s = urep[uu];
+  // unique networks: base of their class + deltas of the changed nodes whose
+  // capped list (first three parents) differs from the full network's; the
+  // changed nodes of all unique networks form one flat item list
+  // (prefix over the networks in wl)
+  for (int uu = tid; uu < U; uu += nt) {
     int k, sigma;
-    net_of(s, sd, sig, k, sigma);
-    const unsigned long long *R = rec_of(s);
-    const int nchg = (int)R[1];
-    long long d0 = SM.base[0][k], d1 = SM.base[1][k];
-    for (int i = 0; i < nchg; i++) {
-      unsigned long long e = R[2 + i];
-      const int t = (int)(e & 0x3FFF);
-      const int np = (int)((e >> 14) & 3);
-      int ps[3] = {(int)((e >> 16) & 0xFFFF), (int)((e >> 32) & 0xFFFF), (int)((e >> 48) & 0xFFFF)};
-      int fnp = P.fcnt[k * g + t] < 3 ? P.fcnt[k * g + t] : 3;
-      bool same = (np == fnp);
-      for (int q = 0; same && q < np; q++) same = (ps[q] == (int)P.fps[(k * g + t) * 3 + q]);
-      if (same) continue;
-      long long sc[2];
-      if (np == 0) {
-        sc[0] = bdeu_score(sd, t, 0, ps, P.mA, P.cnt3);
-        sc[1] = bdeu_score(sd, t, 0, ps, P.mB, P.cnt3 + 3 * g);
-      } else {
-        scores_of_warp(sd, P, t, np, ps, sc, lane);
-      }
-      d0 += sc[0] - P.fsc[(k * 2 + 0) * g + t];
-      d1 += sc[1] - P.fsc[(k * 2 + 1) * g + t];
-    }
-    if (lane == 0) {
-      dist[uu] = d0;
-      dist[S + uu] = d1;
-    }
+    net_of(urep[uu], sd, sig, k, sigma);
+    dist[uu] = SM.base[0][k];
+    dist[S + uu] = SM.base[1][k];
   }
-  __syncthreads();
+  {
+    int running = 0;
+    for (int u0 = 0; u0 < U; u0 += nt) {
+      const int uu = u0 + tid;
+      const int v = uu < U ? (int)rec_of(urep[uu])[1] : 0;
+      int total;
+      const int off = block_scan(v, total, SM.scan);
+      if (uu < U) wl[uu] = running + off;
+      running += total;
+    }
+    if (tid == 0) SM.nwl = running;
+    __syncthreads();
+  }
+  const int nchg_all = SM.nwl;
+  // item e -> (unique network, changed-node record)
+  auto item_of = [&](int e, int &uu, int &k, unsigned long long &rec) {
+    int lo = 0, hi = U - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (wl[mid] <= e) lo = mid;
+      else hi = mid - 1;
+    }
+    uu = lo;
+    int sigma;
+    const int s = urep[uu];
+    net_of(s, sd, sig, k, sigma);
+    rec = rec_of(s)[2 + (e - wl[uu])];
+  };
+  auto differs = [&](int k, unsigned long long e) -> bool {
+    const int t = (int)(e & 0x3FFF), np = (int)((e >> 14) & 3);
+    const int fnp = P.fcnt[k * g + t] < 3 ? P.fcnt[k * g + t] : 3;
+    if (np != fnp) return true;
+    for (int q = 0; q < np; q++)
+      if ((int)((e >> (16 + 16 * q)) & 0xFFFF) != (int)P.fps[(k * g + t) * 3 + q]) return true;
+    return false;
+  };
+  bdeu_items(
+      sd, P, SM.scan, nchg_all,
+      [&](int e) -> unsigned long long {
+        int uu, k;
+        unsigned long long rec;
+        item_of(e, uu, k, rec);
+        if (!differs(k, rec)) return ~0ull;
+        return rec;  // t | np << 14 | parents: the item key format
+      },
+      [&](int e, long long s1, long long s2) {
+        int uu, k;
+        unsigned long long rec;
+        item_of(e, uu, k, rec);
+        if (!differs(k, rec)) return;
+        const int t = (int)(rec & 0x3FFF), np = (int)((rec >> 14) & 3);
+        if (np == 0) {
+          int ps[3] = {0xFFFF, 0xFFFF, 0xFFFF};
+          s1 = bdeu_score(sd, t, 0, ps, P.mA, P.cnt3);
+          s2 = bdeu_score(sd, t, 0, ps, P.mB, P.cnt3 + 3 * g);
+        }
+        atomicAdd((unsigned long long *)&dist[uu],
+                  (unsigned long long)(s1 - P.fsc[(k * 2 + 0) * g + t]));
+        atomicAdd((unsigned long long *)&dist[S + uu],
+                  (unsigned long long)(s2 - P.fsc[(k * 2 + 1) * g + t]));
+      });
 
   // ---- P6: normalisation (main.cu:1302-1404) and JS (main.cu:1406-1428),
   // both classes per reduction pass; one warp with shuffles when U <= 32
