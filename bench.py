@@ -192,7 +192,7 @@ def run_multiset(args, rank, world, local):
     R = args.perms or w.flags["r"]
     ctx = eddy_gpu.Context(max_parents=w.flags["mp"], prior_weight=w.flags["pw"], permutations=R,
                            rng=eddy_gpu.RNG_COUNTER, seed=77, device=local, keep_networks=False)
-    stream = torch.cuda.current_stream()
+    stream = torch.cuda.Stream()
     ctx.set_stream(stream.cuda_stream)
     ctx.load_matrix(w.data, w.labels)
     sids = [ctx.add_set(genes, prior) for _, genes, prior in w.sets]
@@ -242,7 +242,8 @@ def run_ours(args, rank, world, local):
     seed = 4242
     ctx = eddy_gpu.Context(max_parents=mp, prior_weight=pw, permutations=B,
                            rng=eddy_gpu.RNG_COUNTER, seed=seed, device=local, keep_networks=False)
-    stream = torch.cuda.current_stream()
+    # the library launches on this stream; the timing events are recorded on it
+    stream = torch.cuda.Stream()
     ctx.set_stream(stream.cuda_stream)
     ctx.load_matrix(w.data, w.labels)
     sid = ctx.add_set(genes)

@@ -112,6 +112,12 @@ struct eddy_ctx {
   long long launches = 0;
   uint64_t salt = 0x5EED5EEDull;
   cudaStream_t own_stream = nullptr;
+  // the steady-state batch as a CUDA graph: its parameters (key) and the
+  // instantiated graph; prep_gen counts rebuilds of the resident set
+  std::vector<uintptr_t> graph_key;
+  cudaGraphExec_t graph_exec = nullptr;
+  long long graph_launches = 0;  // kernels in one replay
+  unsigned prep_gen = 0;
   int prepared_set = -1;  // set whose data is resident in d_vals/d_planes/d_ctot
   bool set_all_valid = true;
   bool y_ready = false;
@@ -191,6 +197,7 @@ int prepare_set(eddy_ctx *ctx, int set_id, SetRun &sr) {
     ctx->set_all_valid = all_valid;
     ctx->prepared_set = set_id;
     ctx->y_ready = false;
+    ctx->prep_gen++;
   }
   SetDev &sd = sr.sd;
   sd = SetDev{};
@@ -268,14 +275,22 @@ std::pair<int, int> tune_key(const SetDev &sd) {
   return {sd.n, lc};
 }
 
-int launch_pairs_any(eddy_ctx *ctx, const SetDev &sd, const uint64_t *masks, int B, uint32_t *dmask,
-                     unsigned long long *stats, bool force_popc = false) {
-  if (sd.c == 0) return EDDY_OK;
-  if (use_popc() || force_popc) {
-    CK(launch_pairs(sd, masks, dmask, B, stats, ctx->stream));
-    ctx->launches += 1;
-    return EDDY_OK;
-  }
+// Tile variant for a batch of B units: pinned by EDDY_MMA_VARIANT, tuned
+// for the set's shape, or -1 when this batch is to tune (B >= 512).
+int pick_variant(eddy_ctx *ctx, const SetDev &sd, int B) {
+  const char *ev = getenv("EDDY_MMA_VARIANT");
+  if (ev) return atoi(ev) % mma_variants();
+  auto it = ctx->tuned.find(tune_key(sd));
+  if (it != ctx->tuned.end()) return it->second;
+  if (B >= 512) return -1;
+  // untuned small batch: the tile shape that measured fastest on 200 x 1000
+  // sets (N = 192, 12 epilogue warps)
+  return 2 % mma_variants();
+}
+
+// Buffers of the tensor-core path for a batch of B units (and the set's Y
+// operand, built once per resident set).
+int prepare_pairs(eddy_ctx *ctx, const SetDev &sd, int B) {
   if (!ctx->y_ready) {
     CK(ctx->d_Y.ensure(mma_y_bytes(sd.c, sd.n)));
     CK(launch_build_y(sd, ctx->d_Y.as<uint8_t>(), ctx->stream));
@@ -284,16 +299,24 @@ int launch_pairs_any(eddy_ctx *ctx, const SetDev &sd, const uint64_t *masks, int
   }
   CK(ctx->d_afp8.ensure(mma_a_bytes(B, sd.n, sd.c)));
   CK(ctx->d_err.ensure(sizeof(unsigned)));
+  return EDDY_OK;
+}
+
+int launch_pairs_any(eddy_ctx *ctx, const SetDev &sd, const uint64_t *masks, int B, uint32_t *dmask,
+                     unsigned long long *stats, bool force_popc = false) {
+  if (sd.c == 0) return EDDY_OK;
+  if (use_popc() || force_popc) {
+    CK(launch_pairs(sd, masks, dmask, B, stats, ctx->stream));
+    ctx->launches += 1;
+    return EDDY_OK;
+  }
+  {
+    int rc = prepare_pairs(ctx, sd, B);
+    if (rc) return rc;
+  }
   CK(cudaMemsetAsync(ctx->d_err.p, 0, sizeof(unsigned), ctx->stream));
-  // untuned (batches below 512 units before the first tuning): the tile
-  // shape that measured fastest on 200 x 1000 sets (N = 192, 12 warps)
-  int variant = 2 % mma_variants();
-  const char *ev = getenv("EDDY_MMA_VARIANT");
-  if (ev) {
-    variant = atoi(ev) % mma_variants();
-  } else if (ctx->tuned.count(tune_key(sd))) {
-    variant = ctx->tuned[tune_key(sd)];
-  } else if (B >= 512) {
+  int variant = pick_variant(ctx, sd, B);
+  if (variant < 0) {
     // autotune on this batch: time every variant once (same results), keep
     // the fastest for this (g, n); the last run leaves dmask filled
     float best = 1e30f;
@@ -378,6 +401,12 @@ int run_units(eddy_ctx *ctx, SetRun &sr, int nunits, const uint64_t *masks_host,
       CK(ctx->d_U.ensure(sizeof(int32_t) * Bt));
       CK(ctx->d_status.ensure(sizeof(uint32_t) * Bt));
       CK(ctx->d_keep.ensure(sizeof(int32_t) * Bt));
+      // steady state (device labellings, nothing kept, tile shape known, the
+      // set's operand built): the batch's launches as one CUDA graph,
+      // captured once per set / batch shape / buffers and replayed
+      const bool graphable = !masks_host && !keeping && !popc_batch && !use_popc() && c > 0 &&
+                             ctx->y_ready && ctx->stream != nullptr &&
+                             pick_variant(ctx, sd, Bt) >= 0;
       if (masks_host) {
         std::vector<uint64_t> mh((size_t)Bt * W);
         for (int i = 0; i < Bt; i++)
@@ -391,10 +420,6 @@ int run_units(eddy_ctx *ctx, SetRun &sr, int nunits, const uint64_t *masks_host,
         CK(ctx->d_uperm.ensure(sizeof(int32_t) * Bt));
         CK(cudaMemcpyAsync(ctx->d_uset.p, uset.data(), 4 * Bt, cudaMemcpyHostToDevice, ctx->stream));
         CK(cudaMemcpyAsync(ctx->d_uperm.p, uperm.data(), 4 * Bt, cudaMemcpyHostToDevice, ctx->stream));
-        CK(launch_counter_masks(sd.n, sd.nA, W, ctx->o.seed, ctx->d_uset.as<int32_t>(),
-                                ctx->d_uperm.as<int32_t>(), ctx->d_mask0.as<uint64_t>(),
-                                ctx->d_masks.as<uint64_t>(), Bt, ctx->stream));
-        ctx->launches++;
       }
       // the kept unit (the first of the call) writes its detailed outputs
       std::vector<int32_t> ks(Bt, -1);
@@ -424,16 +449,76 @@ int run_units(eddy_ctx *ctx, SetRun &sr, int nunits, const uint64_t *masks_host,
       bd.out_lval = ctx->d_olval.as<double>();
       bd.out_rows = ctx->d_orows.as<uint32_t>();
       bd.stats = ctx->d_stats.as<unsigned long long>();
-      CK(cudaEventRecord(ctx->ev[0], ctx->stream));
-      {
-        int rc = launch_pairs_any(ctx, sd, bd.masks, Bt, ctx->d_dmask.as<uint32_t>(), bd.stats,
-                                  popc_batch);
+      // the batch's device work: labellings, decisions, networks
+      // (events become record nodes when captured)
+      auto record = [&](cudaEvent_t e, bool capturing) -> cudaError_t {
+        return capturing ? cudaEventRecordWithFlags(e, ctx->stream, cudaEventRecordExternal)
+                         : cudaEventRecord(e, ctx->stream);
+      };
+      auto enqueue = [&](bool capturing) -> int {
+        if (!masks_host) {
+          CK(launch_counter_masks(sd.n, sd.nA, W, ctx->o.seed, ctx->d_uset.as<int32_t>(),
+                                  ctx->d_uperm.as<int32_t>(), ctx->d_mask0.as<uint64_t>(),
+                                  ctx->d_masks.as<uint64_t>(), Bt, ctx->stream));
+          ctx->launches++;
+        }
+        CK(record(ctx->ev[0], capturing));
+        {
+          int rc = launch_pairs_any(ctx, sd, bd.masks, Bt, ctx->d_dmask.as<uint32_t>(), bd.stats,
+                                    popc_batch);
+          if (rc) return rc;
+        }
+        CK(record(ctx->ev[1], capturing));
+        CK(launch_units(sd, bd, ctx->stream));
+        CK(record(ctx->ev[2], capturing));
+        ctx->launches += 1;
+        return EDDY_OK;
+      };
+      if (graphable) {
+        {
+          int rc = prepare_pairs(ctx, sd, Bt);
+          if (rc) return rc;
+        }
+        // everything a replay bakes in: the set, its state, the batch shape
+        // and every buffer address
+        std::vector<uintptr_t> key = {
+            (uintptr_t)sr.set_id, (uintptr_t)ctx->prep_gen, (uintptr_t)sd.salt,
+            (uintptr_t)sd.exact_all, (uintptr_t)Bt, (uintptr_t)kmax_run, (uintptr_t)ub,
+            (uintptr_t)pick_variant(ctx, sd, Bt), (uintptr_t)ctx->o.seed,
+            (uintptr_t)ctx->d_masks.p, (uintptr_t)ctx->d_dmask.p, (uintptr_t)ctx->d_scratch.p,
+            (uintptr_t)ctx->d_js.p, (uintptr_t)ctx->d_U.p, (uintptr_t)ctx->d_status.p,
+            (uintptr_t)ctx->d_keep.p, (uintptr_t)ctx->d_uset.p, (uintptr_t)ctx->d_uperm.p,
+            (uintptr_t)ctx->d_stats.p, (uintptr_t)ctx->d_afp8.p, (uintptr_t)ctx->d_Y.p,
+            (uintptr_t)ctx->d_err.p, (uintptr_t)ctx->d_mask0.p, (uintptr_t)ctx->stream};
+        if (key != ctx->graph_key || !ctx->graph_exec) {
+          if (ctx->graph_exec) {
+            cudaGraphExecDestroy(ctx->graph_exec);
+            ctx->graph_exec = nullptr;
+          }
+          ctx->graph_key.clear();
+          const long long l0 = ctx->launches;
+          CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+          const int rc = enqueue(true);
+          cudaGraph_t graph = nullptr;
+          const cudaError_t ce = cudaStreamEndCapture(ctx->stream, &graph);
+          if (rc) {
+            if (graph) cudaGraphDestroy(graph);
+            return rc;
+          }
+          CK(ce);
+          const cudaError_t ie = cudaGraphInstantiate(&ctx->graph_exec, graph, 0);
+          cudaGraphDestroy(graph);
+          CK(ie);
+          ctx->graph_key = key;
+          ctx->graph_launches = ctx->launches - l0;
+          ctx->launches = l0;
+        }
+        CK(cudaGraphLaunch(ctx->graph_exec, ctx->stream));
+        ctx->launches += ctx->graph_launches;
+      } else {
+        int rc = enqueue(false);
         if (rc) return rc;
       }
-      CK(cudaEventRecord(ctx->ev[1], ctx->stream));
-      CK(launch_units(sd, bd, ctx->stream));
-      CK(cudaEventRecord(ctx->ev[2], ctx->stream));
-      ctx->launches += 1;
       std::vector<double> jsb(Bt);
       std::vector<int32_t> Ub(Bt);
       status.assign(Bt, 0);
@@ -605,6 +690,7 @@ int eddy_ctx_destroy(eddy_ctx *ctx) {
   for (DevBuf *b : bufs) b->release();
   for (auto &ev : ctx->ev)
     if (ev) cudaEventDestroy(ev);
+  if (ctx->graph_exec) cudaGraphExecDestroy(ctx->graph_exec);
   if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
   delete ctx;
   return EDDY_OK;

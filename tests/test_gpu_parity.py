@@ -145,6 +145,31 @@ def test_counter_stream_matches_oracle(eddy_lib, oracle_lib):
         np.testing.assert_allclose(s["pddn"], p, rtol=1e-4, atol=1e-9)
 
 
+def test_graph_replays_match_oracle(eddy_lib, oracle_lib, monkeypatch):
+    """Repeated batches of one set run as a captured CUDA graph (after the
+    first batch builds the operand); replays with new permutation indices,
+    a switch to another set and back (re-capture) all match the oracle."""
+    monkeypatch.setenv("EDDY_MMA_VARIANT", "2")  # a known tile shape: no tuning batch
+    rng = np.random.default_rng(21)
+    g, n, nA = 24, 180, 80
+    data = planted(rng, g, n, nA=nA)
+    labels0 = np.concatenate([np.zeros(nA, np.uint8), np.ones(n - nA, np.uint8)])
+    seed = 77
+    ctx = eddy_lib.Context(max_parents=3, permutations=64, rng=eddy_lib.RNG_COUNTER, seed=seed)
+    ctx.load_matrix(data, labels0)
+    sa = ctx.add_set(np.arange(g))
+    sb = ctx.add_set(np.arange(0, g, 2))
+    B = 48
+    prm = oracle_lib.params(mp=3)
+    for sid, first in [(sa, 1), (sa, 1 + B), (sa, 1 + 2 * B), (sb, 1), (sb, 1 + B), (sa, 1 + 3 * B)]:
+        js, U = ctx.run_permutations(sid, first, B)
+        genes = np.arange(g) if sid == sa else np.arange(0, g, 2)
+        lab = oracle_lib.counter_labels(seed, sid, labels0, first + B)[first:first + B]
+        ojs, oU = oracle_lib.units(data[genes], lab, None, prm)
+        assert np.array_equal(U, oU), (sid, first)
+        assert js_close(js, ojs), (sid, first)
+
+
 def test_glibc_stream_matches_reference_sampler(eddy_lib, oracle_lib):
     """GLIBC mode: the permutation stream of main.cu:538-573 across two sets."""
     rng = np.random.default_rng(3)
