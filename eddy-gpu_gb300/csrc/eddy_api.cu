@@ -22,6 +22,32 @@ using namespace eddy;
 
 namespace {
 
+// Page-locked host staging for the small per-batch transfers (indices in,
+// results out): asynchronous copies without the driver's pageable path.
+struct PinnedBuf {
+  void *p = nullptr;
+  size_t n = 0;
+  cudaError_t ensure(size_t bytes) {
+    if (bytes <= n) return cudaSuccess;
+    if (p) cudaFreeHost(p);
+    p = nullptr;
+    n = 0;
+    const size_t want = std::max(bytes, (size_t)64 << 10);
+    cudaError_t e = cudaHostAlloc(&p, want, cudaHostAllocDefault);
+    if (e == cudaSuccess) n = want;
+    return e;
+  }
+  void release() {
+    if (p) cudaFreeHost(p);
+    p = nullptr;
+    n = 0;
+  }
+  template <class T>
+  T *as(size_t byte_off = 0) const {
+    return reinterpret_cast<T *>(reinterpret_cast<char *>(p) + byte_off);
+  }
+};
+
 struct DevBuf {
   void *p = nullptr;
   size_t n = 0;
@@ -91,6 +117,7 @@ struct eddy_ctx {
   DevBuf d_masks, d_dmask, d_scratch, d_js, d_U, d_status, d_keep, d_uset, d_uperm;
   DevBuf d_oids, d_ocnt, d_opar, d_odist, d_olval, d_orows, d_stats;
   DevBuf d_Y, d_afp8, d_err;  // tensor-core contingency operands
+  PinnedBuf h_stage;          // per-batch indices and results
   int sms = 148;
   // autotuned contingency-kernel variant per (n, power of two of the pair
   // count); tuned_variant: the last one used (-1 = none yet)
@@ -368,7 +395,6 @@ int run_units(eddy_ctx *ctx, SetRun &sr, int nunits, const uint64_t *masks_host,
   int Bmax = (int)std::max<size_t>(1, ((size_t)3 << 30) / std::max<size_t>(per_unit, 1));
   Bmax = std::min(Bmax, 4096);
   std::vector<uint32_t> status;
-  std::vector<int32_t> uset, uperm;
   const int mpk = std::max(1, mpk_req);
   if (keeping) {
     CK(ctx->d_oids.ensure(sizeof(int32_t) * S));
@@ -401,6 +427,9 @@ int run_units(eddy_ctx *ctx, SetRun &sr, int nunits, const uint64_t *masks_host,
       CK(ctx->d_U.ensure(sizeof(int32_t) * Bt));
       CK(ctx->d_status.ensure(sizeof(uint32_t) * Bt));
       CK(ctx->d_keep.ensure(sizeof(int32_t) * Bt));
+      // pinned staging for this attempt's indices and results (grown here,
+      // before any copy uses it)
+      CK(ctx->h_stage.ensure(16 * (size_t)Bt + 64));
       // steady state (device labellings, nothing kept, tile shape known, the
       // set's operand built): the batch's launches as one CUDA graph,
       // captured once per set / batch shape / buffers and replayed
@@ -413,23 +442,25 @@ int run_units(eddy_ctx *ctx, SetRun &sr, int nunits, const uint64_t *masks_host,
           memcpy(mh.data() + (size_t)i * W, masks_host + (size_t)(b0 + todo[i]) * W, 8 * W);
         CK(cudaMemcpyAsync(ctx->d_masks.p, mh.data(), 8 * mh.size(), cudaMemcpyHostToDevice, ctx->stream));
       } else {
-        uset.assign(Bt, sr.set_id);
-        uperm.resize(Bt);
-        for (int i = 0; i < Bt; i++) uperm[i] = perms[b0 + todo[i]];
+        // (staging: set ids, then permutation indices; the previous batch's
+        // copies out of it completed at its synchronisation)
+        int32_t *hs = ctx->h_stage.as<int32_t>(), *hp = hs + Bt;
+        for (int i = 0; i < Bt; i++) {
+          hs[i] = sr.set_id;
+          hp[i] = perms[b0 + todo[i]];
+        }
         CK(ctx->d_uset.ensure(sizeof(int32_t) * Bt));
         CK(ctx->d_uperm.ensure(sizeof(int32_t) * Bt));
-        CK(cudaMemcpyAsync(ctx->d_uset.p, uset.data(), 4 * Bt, cudaMemcpyHostToDevice, ctx->stream));
-        CK(cudaMemcpyAsync(ctx->d_uperm.p, uperm.data(), 4 * Bt, cudaMemcpyHostToDevice, ctx->stream));
+        CK(cudaMemcpyAsync(ctx->d_uset.p, hs, 4 * Bt, cudaMemcpyHostToDevice, ctx->stream));
+        CK(cudaMemcpyAsync(ctx->d_uperm.p, hp, 4 * Bt, cudaMemcpyHostToDevice, ctx->stream));
       }
-      // the kept unit (the first of the call) writes its detailed outputs
-      std::vector<int32_t> ks(Bt, -1);
+      // the kept unit (the first of the call) writes its detailed outputs;
+      // slot -1 (every byte 0xFF) for the others
       int i0 = -1;
       for (int i = 0; i < Bt && keeping; i++)
-        if (b0 + todo[i] == 0) {
-          ks[i] = 0;
-          i0 = i;
-        }
-      CK(cudaMemcpyAsync(ctx->d_keep.p, ks.data(), 4 * Bt, cudaMemcpyHostToDevice, ctx->stream));
+        if (b0 + todo[i] == 0) i0 = i;
+      CK(cudaMemsetAsync(ctx->d_keep.p, 0xFF, 4 * (size_t)Bt, ctx->stream));
+      if (i0 >= 0) CK(cudaMemsetAsync(ctx->d_keep.as<int32_t>() + i0, 0, 4, ctx->stream));
       BatchDev bd{};
       bd.B = Bt;
       bd.kmax = kmax_run;
@@ -519,18 +550,24 @@ int run_units(eddy_ctx *ctx, SetRun &sr, int nunits, const uint64_t *masks_host,
         int rc = enqueue(false);
         if (rc) return rc;
       }
-      std::vector<double> jsb(Bt);
-      std::vector<int32_t> Ub(Bt);
-      status.assign(Bt, 0);
-      CK(cudaMemcpyAsync(jsb.data(), ctx->d_js.p, 8 * Bt, cudaMemcpyDeviceToHost, ctx->stream));
-      CK(cudaMemcpyAsync(Ub.data(), ctx->d_U.p, 4 * Bt, cudaMemcpyDeviceToHost, ctx->stream));
-      CK(cudaMemcpyAsync(status.data(), ctx->d_status.p, 4 * Bt, cudaMemcpyDeviceToHost, ctx->stream));
-      // the tensor-core kernel's timeout word, read with the results
-      unsigned errw = 0;
+      // results (and the tensor-core kernel's timeout word) through the
+      // pinned staging: JS, U, status, error word
+      double *hjs = ctx->h_stage.as<double>();
+      int32_t *hU = ctx->h_stage.as<int32_t>(8 * (size_t)Bt);
+      uint32_t *hst = ctx->h_stage.as<uint32_t>(12 * (size_t)Bt);
+      unsigned *herr = ctx->h_stage.as<unsigned>(16 * (size_t)Bt);
+      *herr = 0;
+      CK(cudaMemcpyAsync(hjs, ctx->d_js.p, 8 * Bt, cudaMemcpyDeviceToHost, ctx->stream));
+      CK(cudaMemcpyAsync(hU, ctx->d_U.p, 4 * Bt, cudaMemcpyDeviceToHost, ctx->stream));
+      CK(cudaMemcpyAsync(hst, ctx->d_status.p, 4 * Bt, cudaMemcpyDeviceToHost, ctx->stream));
       const bool mma_used = !use_popc() && !popc_batch && ctx->d_err.p != nullptr && c > 0;
       if (mma_used)
-        CK(cudaMemcpyAsync(&errw, ctx->d_err.p, sizeof errw, cudaMemcpyDeviceToHost, ctx->stream));
+        CK(cudaMemcpyAsync(herr, ctx->d_err.p, sizeof(unsigned), cudaMemcpyDeviceToHost, ctx->stream));
       CK(cudaStreamSynchronize(ctx->stream));
+      const unsigned errw = *herr;
+      std::vector<double> jsb(hjs, hjs + Bt);
+      std::vector<int32_t> Ub(hU, hU + Bt);
+      status.assign(hst, hst + Bt);
       if (errw & 1u) return fail(ctx, EDDY_ERR_INTERNAL, "tensor-core pipeline wait timed out");
       if (errw & 2u) {
         // the general-path queue overflowed (a large share of tables near a
@@ -691,6 +728,7 @@ int eddy_ctx_destroy(eddy_ctx *ctx) {
   for (auto &ev : ctx->ev)
     if (ev) cudaEventDestroy(ev);
   if (ctx->graph_exec) cudaGraphExecDestroy(ctx->graph_exec);
+  ctx->h_stage.release();
   if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
   delete ctx;
   return EDDY_OK;
