@@ -118,6 +118,7 @@ struct eddy_ctx {
   DevBuf d_oids, d_ocnt, d_opar, d_odist, d_olval, d_orows, d_stats;
   DevBuf d_Y, d_afp8, d_err;  // tensor-core contingency operands
   PinnedBuf h_stage;          // per-batch indices and results
+  PinnedBuf h_vals;           // the resident set's values on their way in
   int sms = 148;
   // autotuned contingency-kernel variant per (n, power of two of the pair
   // count); tuned_variant: the last one used (-1 = none yet)
@@ -146,7 +147,6 @@ struct eddy_ctx {
   long long graph_launches = 0;  // kernels in one replay
   unsigned prep_gen = 0;
   int prepared_set = -1;  // set whose data is resident in d_vals/d_planes/d_ctot
-  bool set_all_valid = true;
   bool y_ready = false;
 };
 
@@ -193,13 +193,14 @@ int prepare_set(eddy_ctx *ctx, int set_id, SetRun &sr) {
     ctx->lg_n = n;
   }
   const bool resident = (ctx->prepared_set == set_id);
-  std::vector<int8_t> vals(resident ? 0 : (size_t)g * n);
-  bool all_valid = true;
-  for (int i = 0; i < g && !resident; i++) {
-    const int8_t *src = ctx->data.data() + (size_t)S.genes[i] * n;
-    memcpy(vals.data() + (size_t)i * n, src, n);
-    for (int s = 0; s < n; s++)
-      if (src[s] < -1 || src[s] > 1) all_valid = false;
+  int8_t *vals = nullptr;
+  if (!resident) {
+    // the previous set's copy out of this staging finished at that set's
+    // first synchronisation
+    CK(ctx->h_vals.ensure((size_t)g * n + 16));
+    vals = ctx->h_vals.as<int8_t>();
+    for (int i = 0; i < g; i++)
+      memcpy(vals + (size_t)i * n, ctx->data.data() + (size_t)S.genes[i] * n, n);
   }
   std::vector<uint8_t> pbits(c > 0 ? c : 1, 0);
   if (!S.prior.empty() && !resident) {
@@ -209,19 +210,18 @@ int prepare_set(eddy_ctx *ctx, int set_id, SetRun &sr) {
   }
   if (!resident) {
     ctx->prepared_set = -1;
-    CK(ctx->d_vals.ensure(vals.size() + 16));
-    CK(ctx->d_valsT.ensure(vals.size() + 16));
+    CK(ctx->d_vals.ensure((size_t)g * n + 16));
+    CK(ctx->d_valsT.ensure((size_t)g * n + 16));
     CK(ctx->d_planes.ensure(sizeof(uint64_t) * (size_t)g * 3 * W));
     CK(ctx->d_valid.ensure(sizeof(uint64_t) * W));
     CK(ctx->d_ctot.ensure(sizeof(uint16_t) * 9 * (size_t)(c > 0 ? c : 1)));
     CK(ctx->d_prior.ensure(pbits.size()));
-    CK(cudaMemcpyAsync(ctx->d_vals.p, vals.data(), vals.size(), cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(ctx->d_vals.p, vals, (size_t)g * n, cudaMemcpyHostToDevice, ctx->stream));
     CK(cudaMemcpyAsync(ctx->d_prior.p, pbits.data(), pbits.size(), cudaMemcpyHostToDevice, ctx->stream));
     CK(launch_prep(ctx->d_vals.as<int8_t>(), g, n, W, c, ctx->d_planes.as<uint64_t>(),
                    ctx->d_valid.as<uint64_t>(), ctx->d_ctot.as<uint16_t>(),
                    ctx->d_valsT.as<int8_t>(), ctx->stream));
     ctx->launches += 2 + (c > 0);
-    ctx->set_all_valid = all_valid;
     ctx->prepared_set = set_id;
     ctx->y_ready = false;
     ctx->prep_gen++;
@@ -257,7 +257,6 @@ int prepare_set(eddy_ctx *ctx, int set_id, SetRun &sr) {
     const char *dm = getenv("EDDY_DECISIONS");
     if (dm && strcmp(dm, "fp64") == 0) sd.exact_all = 1;
   }
-  sd.all_valid = ctx->set_all_valid ? 1 : 0;
   sd.planes = ctx->d_planes.as<uint64_t>();
   sd.valid = ctx->d_valid.as<uint64_t>();
   sd.vals = ctx->d_vals.as<int8_t>();
@@ -605,12 +604,28 @@ int run_units(eddy_ctx *ctx, SetRun &sr, int nunits, const uint64_t *masks_host,
         keep->dist.resize(2 * (size_t)S);
         keep->lval.resize(2 * (size_t)S);
         keep->rows.resize(2 * (size_t)g * sd.GW);
-        CK(cudaMemcpy(keep->ids.data(), ctx->d_oids.p, 4 * Uk, cudaMemcpyDeviceToHost));
-        CK(cudaMemcpy(keep->cnt.data(), ctx->d_ocnt.p, 4 * (size_t)Uk * g, cudaMemcpyDeviceToHost));
-        CK(cudaMemcpy(keep->par.data(), ctx->d_opar.p, 4 * (size_t)Uk * g * mpk, cudaMemcpyDeviceToHost));
-        CK(cudaMemcpy(keep->dist.data(), ctx->d_odist.p, 16 * (size_t)S, cudaMemcpyDeviceToHost));
-        CK(cudaMemcpy(keep->lval.data(), ctx->d_olval.p, 16 * (size_t)S, cudaMemcpyDeviceToHost));
-        CK(cudaMemcpy(keep->rows.data(), ctx->d_orows.p, 4 * keep->rows.size(), cudaMemcpyDeviceToHost));
+        // through the pinned staging: six asynchronous copies, one wait
+        const size_t b_ids = 4 * (size_t)Uk, b_cnt = 4 * (size_t)Uk * g,
+                     b_par = 4 * (size_t)Uk * g * mpk, b_dist = 16 * (size_t)S,
+                     b_rows = 4 * keep->rows.size();
+        const size_t o_cnt = (b_ids + 15) & ~(size_t)15, o_par = o_cnt + ((b_cnt + 15) & ~(size_t)15),
+                     o_dist = o_par + ((b_par + 15) & ~(size_t)15), o_lval = o_dist + b_dist,
+                     o_rows = o_lval + b_dist;
+        CK(ctx->h_stage.ensure(o_rows + b_rows));
+        char *hk = ctx->h_stage.as<char>();
+        CK(cudaMemcpyAsync(hk, ctx->d_oids.p, b_ids, cudaMemcpyDeviceToHost, ctx->stream));
+        CK(cudaMemcpyAsync(hk + o_cnt, ctx->d_ocnt.p, b_cnt, cudaMemcpyDeviceToHost, ctx->stream));
+        CK(cudaMemcpyAsync(hk + o_par, ctx->d_opar.p, b_par, cudaMemcpyDeviceToHost, ctx->stream));
+        CK(cudaMemcpyAsync(hk + o_dist, ctx->d_odist.p, b_dist, cudaMemcpyDeviceToHost, ctx->stream));
+        CK(cudaMemcpyAsync(hk + o_lval, ctx->d_olval.p, b_dist, cudaMemcpyDeviceToHost, ctx->stream));
+        CK(cudaMemcpyAsync(hk + o_rows, ctx->d_orows.p, b_rows, cudaMemcpyDeviceToHost, ctx->stream));
+        CK(cudaStreamSynchronize(ctx->stream));
+        memcpy(keep->ids.data(), hk, b_ids);
+        memcpy(keep->cnt.data(), hk + o_cnt, b_cnt);
+        memcpy(keep->par.data(), hk + o_par, b_par);
+        memcpy(keep->dist.data(), hk + o_dist, b_dist);
+        memcpy(keep->lval.data(), hk + o_lval, b_dist);
+        memcpy(keep->rows.data(), hk + o_rows, b_rows);
       }
       if (overflow) kmax_run = g + 1;
       if (collision) {
@@ -729,6 +744,7 @@ int eddy_ctx_destroy(eddy_ctx *ctx) {
     if (ev) cudaEventDestroy(ev);
   if (ctx->graph_exec) cudaGraphExecDestroy(ctx->graph_exec);
   ctx->h_stage.release();
+  ctx->h_vals.release();
   if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
   delete ctx;
   return EDDY_OK;
