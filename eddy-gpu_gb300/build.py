@@ -76,8 +76,8 @@ def build(verbose: bool = False) -> str:
         _run([nvcc] + ARCH + ["-shared", "-o", LIB] + objs + ["-lcudart_static", "-lrt", "-ldl", "-lpthread"])
     cli_src = os.path.join(CSRC, "eddy_cli.cpp")
     if os.path.exists(cli_src) and _stale(CLI, [cli_src, LIB] + headers):
-        _run(["g++", "-O2", "-std=c++17", "-I", os.path.join(ROOT, "include"), cli_src, "-o", CLI,
-              "-L", LIBDIR, "-leddy_gpu", "-Wl,-rpath,$ORIGIN/../lib"])
+        _run(["g++", "-O2", "-std=c++17", "-pthread", "-I", os.path.join(ROOT, "include"), cli_src,
+              "-o", CLI, "-L", LIBDIR, "-leddy_gpu", "-Wl,-rpath,$ORIGIN/../lib"])
     return LIB
 
 

@@ -15,7 +15,9 @@
 #include <string.h>
 #include <sys/time.h>
 
+#include <algorithm>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "eddy_gpu.h"
@@ -37,6 +39,57 @@ bool read_line(FILE *f, std::string &out) {
     if (ch == '\n') break;
   }
   return !out.empty();
+}
+
+// The whole file in memory (the expression matrix is read once, in one go).
+bool read_file(const char *path, std::vector<char> &buf) {
+  FILE *f = fopen(path, "rb");
+  if (!f) return false;
+  buf.clear();
+  char tmp[1 << 16];
+  size_t got;
+  while ((got = fread(tmp, 1, sizeof tmp, f)) > 0) buf.insert(buf.end(), tmp, tmp + got);
+  fclose(f);
+  return true;
+}
+
+// sscanf(token, "%d") on a token that ends at `end`: leading white space,
+// an optional sign, then the digits (none: not a number).
+bool scan_int(const char *p, const char *end, int &v) {
+  while (p < end && (*p == ' ' || *p == '\n' || *p == '\r' || *p == '\v' || *p == '\f')) p++;
+  bool neg = false;
+  if (p < end && (*p == '+' || *p == '-')) neg = (*p++ == '-');
+  if (p >= end || *p < '0' || *p > '9') return false;
+  long long x = 0;
+  while (p < end && *p >= '0' && *p <= '9') {
+    if (x < 1000000000ll) x = x * 10 + (*p - '0');
+    p++;
+  }
+  v = (int)(neg ? -x : x);
+  return true;
+}
+
+// One matrix row as strtok(row, "\t") sees it (empty fields skipped): the
+// gene name, then up to n values; returns the number of value tokens.
+int parse_row(const char *p, const char *end, int n, std::string &name, int8_t *out) {
+  auto next = [&](const char *&b, const char *&e) -> bool {
+    while (p < end && *p == '\t') p++;
+    if (p >= end) return false;
+    b = p;
+    while (p < end && *p != '\t') p++;
+    e = p;
+    return true;
+  };
+  const char *b, *e;
+  if (!next(b, e)) return -1;
+  name.assign(b, e);
+  int k = 0;
+  while (k < n && next(b, e)) {
+    int v = 2;
+    if (!scan_int(b, e, v)) v = 2;
+    out[k++] = (int8_t)((v >= -1 && v <= 1) ? v : 2);
+  }
+  return k;
 }
 
 // strtok(s, delims) over a std::string copy.
@@ -119,37 +172,53 @@ int main(int argc, char *argv[]) {
   if (!fpResults) { printf("results file is NULL: %s [%d]\n", strerror(errno), errno); exit(EXIT_FAILURE); }
 
   // ---- expression matrix, main.cu:255-301 (quirks kept: 1-character sample
-  // names leave the count, the last row is dropped)
+  // names leave the count, the last row is dropped).  The file is read in
+  // one go; the rows are parsed in parallel.
   std::string line;
-  read_line(fpExpr, line);
+  fclose(fpExpr);
+  std::vector<char> text;
+  if (!read_file(inputFile, text)) {
+    printf("Expression file is NULL: %s [%d]\n", strerror(errno), errno);
+    exit(EXIT_FAILURE);
+  }
+  std::vector<size_t> ls;  // line starts (each line keeps its '\n')
+  for (size_t pos = 0; pos < text.size();) {
+    ls.push_back(pos);
+    const void *nl = memchr(text.data() + pos, '\n', text.size() - pos);
+    pos = nl ? (size_t)((const char *)nl - text.data()) + 1 : text.size();
+  }
+  ls.push_back(text.size());
+  const int nlines = (int)ls.size() - 1;
+  line = nlines > 0 ? std::string(text.data() + ls[0], text.data() + ls[1]) : std::string();
   std::vector<std::string> sampleNames = tokens(line, "\t");
   if (!sampleNames.empty()) sampleNames.erase(sampleNames.begin());
   int numSamples = (int)sampleNames.size();
   for (int i = 0; i < numSamples; i++)
     if (sampleNames[i].size() == 1) numSamples--;
   printf("%d samples\n", numSamples);
-  std::vector<std::string> rows;
-  while (read_line(fpExpr, line)) rows.push_back(line);
-  int numGenes = (int)rows.size() - 1;
+  int numGenes = nlines - 2;  // rows after the header, the last one dropped
   if (numGenes < 0) numGenes = 0;
   printf("%d genes\n", numGenes);
   std::vector<std::string> geneNames(numGenes);
   std::vector<int8_t> data((size_t)numGenes * numSamples);
-  for (int i = 0; i < numGenes; i++) {
-    std::vector<std::string> tk = tokens(rows[i], "\t");
-    if ((int)tk.size() < numSamples + 1) {
-      fprintf(stderr, "eddy: row %d of %s has %d values, %d expected\n", i + 2, inputFile,
-              (int)tk.size() - 1, numSamples);
-      exit(EXIT_FAILURE);
-    }
-    geneNames[i] = tk[0];
-    for (int j = 0; j < numSamples; j++) {
-      int v = 2;
-      if (sscanf(tk[j + 1].c_str(), "%d", &v) != 1) v = 2;
-      data[(size_t)i * numSamples + j] = (int8_t)((v >= -1 && v <= 1) ? v : 2);
-    }
+  {
+    std::vector<int> got(numGenes, 0);
+    const int nth = std::max(1, std::min((int)std::thread::hardware_concurrency(), 32));
+    std::vector<std::thread> pool;
+    for (int t = 0; t < nth; t++)
+      pool.emplace_back([&, t]() {
+        for (int i = t; i < numGenes; i += nth)
+          got[i] = parse_row(text.data() + ls[1 + i], text.data() + ls[2 + i], numSamples,
+                             geneNames[i], data.data() + (size_t)i * numSamples);
+      });
+    for (auto &th : pool) th.join();
+    for (int i = 0; i < numGenes; i++)
+      if (got[i] < numSamples) {
+        fprintf(stderr, "eddy: row %d of %s has %d values, %d expected\n", i + 2, inputFile,
+                got[i] < 0 ? 0 : got[i], numSamples);
+        exit(EXIT_FAILURE);
+      }
   }
-  fclose(fpExpr);
 
   // ---- class labels, main.cu:303-352
   read_line(fpClass, line);
