@@ -432,30 +432,51 @@ __global__ void __maxnreg__(max_regs<kEpi>())
   }
 }
 
-// The general path for the queued tables of a launch: full-table decision,
-// the Minkowski leave-one-out filter, the cell-removed tables (FP32 with the
-// exact FP64 fallback); one thread per table, results OR-ed into the masks.
+// The general path for the queued tables of a launch, one thread per
+// (table, decision): decision 0 = the full table, decision 1 + 3a + b = the
+// table with one sample of cell (a, b) removed.  A thread decides the full
+// table (FP32, exact FP64 in the guard bands) and, when the Minkowski
+// leave-one-out window cannot settle the cells, its own cell-removed table;
+// so a table's ten decisions, some of them exact FP64 series, run in
+// parallel.  Set bits are OR-ed into the masks.
 __global__ void __launch_bounds__(256) k_general(const __grid_constant__ SetDev sd,
                                                  const unsigned *queue, unsigned qcap, int B,
                                                  uint32_t *dmask, unsigned long long *stats) {
   const unsigned cnt = queue[0] < qcap ? queue[0] : qcap;
   const unsigned *items = queue + 4;
   unsigned nexact = 0, nfilt = 0;
-  for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < cnt; i += gridDim.x * blockDim.x) {
+  const unsigned long long ntask = 10ull * cnt;
+  for (unsigned long long task = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x;
+       task < ntask; task += (unsigned long long)gridDim.x * blockDim.x) {
+    const unsigned i = (unsigned)(task / 10);
+    const int slot = (int)(task % 10);
     const unsigned *it = items + (size_t)i * kQWords;
     const int u = (int)((it[4] >> 16) & 0xFFFu), cls = (it[4] >> 28) & 1,
               prior = (it[4] >> 29) & 1, p = (int)it[5];
-    const uint64_t rr = pair_mask_general(
-        (int)(it[0] & 0xFFFFu), (int)(it[0] >> 16), (int)(it[1] & 0xFFFFu), (int)(it[1] >> 16),
-        (int)(it[2] & 0xFFFFu), (int)(it[2] >> 16), (int)(it[3] & 0xFFFFu), (int)(it[3] >> 16),
-        (int)(it[4] & 0xFFFFu), prior, sd);
-    const uint32_t m = (uint32_t)rr & 0x3FFu;
-    if (m) {
-      atomicOr(&dmask[(size_t)u * sd.c + p], m << (16 * cls));
+    int t[9] = {(int)(it[0] & 0xFFFFu), (int)(it[0] >> 16), (int)(it[1] & 0xFFFFu),
+                (int)(it[1] >> 16),     (int)(it[2] & 0xFFFFu), (int)(it[2] >> 16),
+                (int)(it[3] & 0xFFFFu), (int)(it[3] >> 16),     (int)(it[4] & 0xFFFFu)};
+    TabInfo ti;
+    unsigned nx = 0;
+    const int bit0 = decide(t, prior, sd, ti, nx);
+    int bit = bit0;
+    if (slot == 0) {
+      nexact += nx;
+      if (loo_safe(ti, prior, sd)) nfilt++;
+    } else if (!loo_safe(ti, prior, sd)) {
+      const int cell = slot - 1;
+      if (t[cell] > 0) {
+        t[cell]--;
+        TabInfo tj;
+        unsigned ny = 0;
+        bit = decide(t, prior, sd, tj, ny);
+        nexact += ny;
+      }
+    }
+    if (bit) {
+      atomicOr(&dmask[(size_t)u * sd.c + p], 1u << (slot + 16 * cls));
       mark_chunk(dmask, B, sd.c, u, p);
     }
-    nexact += (unsigned)(rr >> 32) & 0xFFFFu;
-    nfilt += (unsigned)(rr >> 48) & 1u;
   }
   if (stats) {
     for (int o = 16; o > 0; o >>= 1) {
@@ -631,7 +652,7 @@ static cudaError_t launch_variant(const SetDev &sd, const uint8_t *Afp8, const u
                                             stats, err, gqueue, qcap);
   e = cudaGetLastError();
   if (e != cudaSuccess) return e;
-  k_general<<<sms * 4, 256, 0, st>>>(sd, gqueue, qcap, B, dmask, stats);
+  k_general<<<sms * 8, 256, 0, st>>>(sd, gqueue, qcap, B, dmask, stats);
   return cudaGetLastError();
 }
 
