@@ -26,6 +26,7 @@
 #include <cuda.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
+#include <stdlib.h>
 
 #include "eddy_device.cuh"
 #include "eddy_kernels.h"
@@ -612,6 +613,15 @@ static unsigned queue_cap(int B, int c) {
   const size_t t = (size_t)B * (c > 0 ? c : 1) * 2 / 8;
   return (unsigned)(t < 65536 ? 65536 : t);
 }
+// EDDY_GENERAL_QUEUE_CAP lowers the queue's capacity (tests of the
+// overflow path: the batch is then decided by the popcount kernel)
+static unsigned queue_cap_used(int B, int c) {
+  const unsigned cap = queue_cap(B, c);
+  const char *e = getenv("EDDY_GENERAL_QUEUE_CAP");
+  if (!e) return cap;
+  const long v = atol(e);
+  return (v >= 1 && (unsigned long)v < cap) ? (unsigned)v : cap;
+}
 size_t mma_a_bytes(int B, int n, int c) {
   return a_operand_bytes(B, n) + 16 + (size_t)queue_cap(B, c) * kQWords * sizeof(uint32_t);
 }
@@ -667,7 +677,7 @@ cudaError_t launch_pairs_mma(const SetDev &sd, const uint64_t *masks, int B, uin
   const long long work = (long long)Bp * (np / 16);
   k_masks_fp8<<<(unsigned)((work + 255) / 256), 256, 0, st>>>(masks, B, Bp, sd.W, np, Afp8);
   unsigned *gqueue = reinterpret_cast<unsigned *>(Afp8 + a_operand_bytes(B, sd.n));
-  const unsigned qcap = queue_cap(B, sd.c);
+  const unsigned qcap = queue_cap_used(B, sd.c);
   cudaError_t e = cudaMemsetAsync(gqueue, 0, 16, st);
   if (e != cudaSuccess) return e;
   switch (variant) {
