@@ -124,7 +124,7 @@ struct eddy_ctx {
   // count); tuned_variant: the last one used (-1 = none yet)
   std::map<std::pair<int, int>, int> tuned;
   int tuned_variant = -1;
-  float tuned_ms[4] = {0, 0, 0, 0};
+  float tuned_ms[8] = {0, 0, 0, 0, 0, 0, 0, 0};
   // decision thresholds per gene-set size (the Bonferroni factor)
   struct ThrSet {
     Thr t[2][kDofSlots];
@@ -310,8 +310,8 @@ int pick_variant(eddy_ctx *ctx, const SetDev &sd, int B) {
   if (it != ctx->tuned.end()) return it->second;
   if (B >= 512) return -1;
   // untuned small batch: the tile shape that measured fastest on 200 x 1000
-  // sets (N = 192, 12 epilogue warps)
-  return 2 % mma_variants();
+  // sets (N = 256, 16 epilogue warps)
+  return 4 % mma_variants();
 }
 
 // Buffers of the tensor-core path for a batch of B units (and the set's Y

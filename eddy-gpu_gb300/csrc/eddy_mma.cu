@@ -667,8 +667,8 @@ static cudaError_t launch_variant(const SetDev &sd, const uint8_t *Afp8, const u
 }
 
 // 0: N=128, 16 epilogue warps; 1: N=128, 8 warps; 2: N=192, 12 warps;
-// 3: N=256, 8 warps (ring depths fill the shared memory)
-int mma_variants() { return 4; }
+// 3: N=256, 8 warps; 4: N=256, 16 warps (ring depths fill the shared memory)
+int mma_variants() { return 5; }
 
 cudaError_t launch_pairs_mma(const SetDev &sd, const uint64_t *masks, int B, uint8_t *Afp8,
                              const uint8_t *Y, uint32_t *dmask, unsigned long long *stats,
@@ -687,6 +687,8 @@ cudaError_t launch_pairs_mma(const SetDev &sd, const uint64_t *masks, int B, uin
       return launch_variant<5, 12, 6>(sd, Afp8, Y, gqueue, qcap, B, dmask, stats, err, sms, st);
     case 3:
       return launch_variant<4, 8, 8>(sd, Afp8, Y, gqueue, qcap, B, dmask, stats, err, sms, st);
+    case 4:
+      return launch_variant<4, 16, 8>(sd, Afp8, Y, gqueue, qcap, B, dmask, stats, err, sms, st);
     default:
       return launch_variant<6, 16, 4>(sd, Afp8, Y, gqueue, qcap, B, dmask, stats, err, sms, st);
   }

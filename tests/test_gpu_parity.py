@@ -196,7 +196,8 @@ def test_glibc_stream_matches_reference_sampler(eddy_lib, oracle_lib):
         assert js_close(js, ojs)
 
 
-@pytest.mark.parametrize("variant", [0, 1, 2, 3], ids=["n128e16", "n128e8", "n192e12", "n256e8"])
+@pytest.mark.parametrize("variant", [0, 1, 2, 3, 4],
+                         ids=["n128e16", "n128e8", "n192e12", "n256e8", "n256e16"])
 @pytest.mark.parametrize("case", [CASES[2], CASES[4], CASES[5], CASES[6]],
                          ids=["g20", "g50", "invalid", "g40prior"])
 def test_tensor_core_and_popcount_paths_agree(case, variant, eddy_lib, monkeypatch):
