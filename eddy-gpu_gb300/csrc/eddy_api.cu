@@ -504,7 +504,7 @@ int run_units(eddy_ctx *ctx, SetRun &sr, int nunits, const uint64_t *masks_host,
         CK(record(ctx->ev[1], capturing));
         CK(launch_units(sd, bd, ctx->stream));
         CK(record(ctx->ev[2], capturing));
-        ctx->launches += 1;
+        ctx->launches += 2;  // networks, then normalisation and JS
         return EDDY_OK;
       };
       if (graphable) {

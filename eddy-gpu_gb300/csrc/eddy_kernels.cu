@@ -1162,179 +1162,12 @@ __global__ void __launch_bounds__(256, 3) k_units(const __grid_constant__ SetDev
                   (unsigned long long)(s2 - P.fsc[(k * 2 + 1) * g + t]));
       });
 
-  // ---- P6: normalisation (main.cu:1302-1404) and JS (main.cu:1406-1428),
-  // both classes per reduction pass; one warp with shuffles when U <= 32
+  // ---- P6: unique count and status; the normalisation and JS follow in
+  // k_js (one warp per unit) from the fixed-point scores in dist
   const int keep = bd.keep_slot ? bd.keep_slot[u] : -1;
-  if (U <= 32) {
-    if (warp == 0) {
-      const bool on = lane < U;
-      const long long a = on ? dist[lane] : 0, b = on ? dist[S + lane] : 0;
-      long long l0 = on ? a : LLONG_MAX, h0 = on ? a : LLONG_MIN;
-      long long l1 = on ? b : LLONG_MAX, h1 = on ? b : LLONG_MIN;
-      for (int o = 16; o > 0; o >>= 1) {
-        long long x;
-        x = __shfl_xor_sync(0xffffffffu, l0, o); l0 = x < l0 ? x : l0;
-        x = __shfl_xor_sync(0xffffffffu, h0, o); h0 = x > h0 ? x : h0;
-        x = __shfl_xor_sync(0xffffffffu, l1, o); l1 = x < l1 ? x : l1;
-        x = __shfl_xor_sync(0xffffffffu, h1, o); h1 = x > h1 ? x : h1;
-      }
-      const double da = on ? (double)(a - l0) : 0.0, db = on ? (double)(b - l1) : 0.0;
-      double s0 = da, s1 = db;
-      for (int o = 16; o > 0; o >>= 1) {
-        s0 += __shfl_xor_sync(0xffffffffu, s0, o);
-        s1 += __shfl_xor_sync(0xffffffffu, s1, o);
-      }
-      const double m0 = s0 / (double)U, m1 = s1 / (double)U;
-      const double sA = 10.0 / (double)(h0 - l0), sB = 10.0 / (double)(h1 - l1);
-      const double xa = on ? exp((da - m0) * sA) : 0.0, xb = on ? exp((db - m1) * sB) : 0.0;
-      double e0 = xa, e1 = xb;
-      for (int o = 16; o > 0; o >>= 1) {
-        e0 += __shfl_xor_sync(0xffffffffu, e0, o);
-        e1 += __shfl_xor_sync(0xffffffffu, e1, o);
-      }
-      double ls = 0.0;
-      if (on) {
-        const double Pu = xa / e0, Qu = xb / e1;
-        const double M = (Pu + Qu) / 2;
-        if (M != 0) {
-          if (Pu != 0) ls += 0.5 * (Pu * log(Pu / M));
-          if (Qu != 0) ls += 0.5 * (Qu * log(Qu / M));
-        }
-        if (keep >= 0) {
-          bd.out_lval[((size_t)keep * 2 + 0) * S + lane] = Pu;
-          bd.out_lval[((size_t)keep * 2 + 1) * S + lane] = Qu;
-        }
-      }
-      for (int o = 16; o > 0; o >>= 1) ls += __shfl_xor_sync(0xffffffffu, ls, o);
-      if (lane == 0) {
-        double js = ls / log(2.0);
-        if (h0 == l0 || h1 == l1) js = __longlong_as_double(0x7ff8000000000000ll);
-        bd.js[u] = js;
-        bd.U[u] = U;
-        bd.status[u] = SM.status;
-      }
-    }
-  } else {
-
-  double js = 0.0;
-  long long mn[2], mx[2];
-  double mean[2], esum[2];
-  {
-    long long l0 = LLONG_MAX, h0 = LLONG_MIN, l1 = LLONG_MAX, h1 = LLONG_MIN;
-    for (int uu = tid; uu < U; uu += nt) {
-      const long long a = dist[uu], b = dist[S + uu];
-      l0 = a < l0 ? a : l0;
-      h0 = a > h0 ? a : h0;
-      l1 = b < l1 ? b : l1;
-      h1 = b > h1 ? b : h1;
-    }
-    for (int o = 16; o > 0; o >>= 1) {
-      long long x;
-      x = __shfl_down_sync(0xffffffffu, l0, o); l0 = x < l0 ? x : l0;
-      x = __shfl_down_sync(0xffffffffu, h0, o); h0 = x > h0 ? x : h0;
-      x = __shfl_down_sync(0xffffffffu, l1, o); l1 = x < l1 ? x : l1;
-      x = __shfl_down_sync(0xffffffffu, h1, o); h1 = x > h1 ? x : h1;
-    }
-    if (lane == 0) {
-      SM.red_l[warp] = l0;
-      SM.red_l[8 + warp] = h0;
-      SM.red_l[16 + warp] = l1;
-      SM.red_l[24 + warp] = h1;
-    }
-    __syncthreads();
-    l0 = SM.red_l[0], h0 = SM.red_l[8], l1 = SM.red_l[16], h1 = SM.red_l[24];
-    for (int w = 1; w < nw; w++) {
-      l0 = SM.red_l[w] < l0 ? SM.red_l[w] : l0;
-      h0 = SM.red_l[8 + w] > h0 ? SM.red_l[8 + w] : h0;
-      l1 = SM.red_l[16 + w] < l1 ? SM.red_l[16 + w] : l1;
-      h1 = SM.red_l[24 + w] > h1 ? SM.red_l[24 + w] : h1;
-    }
-    mn[0] = l0, mx[0] = h0, mn[1] = l1, mx[1] = h1;
-  }
-  {
-    double s0 = 0.0, s1 = 0.0;
-    for (int uu = tid; uu < U; uu += nt) {
-      s0 += (double)(dist[uu] - mn[0]);
-      s1 += (double)(dist[S + uu] - mn[1]);
-    }
-    for (int o = 16; o > 0; o >>= 1) {
-      s0 += __shfl_down_sync(0xffffffffu, s0, o);
-      s1 += __shfl_down_sync(0xffffffffu, s1, o);
-    }
-    __syncthreads();  // red_l readers done
-    if (lane == 0) {
-      SM.red_d[warp] = s0;
-      SM.red_d[8 + warp] = s1;
-    }
-    __syncthreads();
-    s0 = 0.0;
-    s1 = 0.0;
-    for (int w = 0; w < nw; w++) {
-      s0 += SM.red_d[w];
-      s1 += SM.red_d[8 + w];
-    }
-    mean[0] = s0 / (double)U;
-    mean[1] = s1 / (double)U;
-  }
-  // likelihoods exp((d - mean) * 10 / (max - min)) (FP64: U values per class)
-  const double sA = 10.0 / (double)(mx[0] - mn[0]), sB = 10.0 / (double)(mx[1] - mn[1]);
-  {
-    double e0 = 0.0, e1 = 0.0;
-    for (int uu = tid; uu < U; uu += nt) {
-      e0 += exp(((double)(dist[uu] - mn[0]) - mean[0]) * sA);
-      e1 += exp(((double)(dist[S + uu] - mn[1]) - mean[1]) * sB);
-    }
-    for (int o = 16; o > 0; o >>= 1) {
-      e0 += __shfl_down_sync(0xffffffffu, e0, o);
-      e1 += __shfl_down_sync(0xffffffffu, e1, o);
-    }
-    __syncthreads();
-    if (lane == 0) {
-      SM.red_d[16 + warp] = e0;
-      SM.red_d[24 + warp] = e1;
-    }
-    __syncthreads();
-    e0 = 0.0;
-    e1 = 0.0;
-    for (int w = 0; w < nw; w++) {
-      e0 += SM.red_d[16 + w];
-      e1 += SM.red_d[24 + w];
-    }
-    esum[0] = e0;
-    esum[1] = e1;
-  }
-  {
-    double ls = 0.0;
-    for (int uu = tid; uu < U; uu += nt) {
-      // likelihoods (main.cu:1360-1394) and the two KL terms of kool()
-      // (routines.cu:42-60): P log(P/M), Q log(Q/M), zeros skipped
-      const double Pu = exp(((double)(dist[uu] - mn[0]) - mean[0]) * sA) / esum[0];
-      const double Qu = exp(((double)(dist[S + uu] - mn[1]) - mean[1]) * sB) / esum[1];
-      const double M = (Pu + Qu) / 2;
-      if (M != 0) {
-        if (Pu != 0) ls += 0.5 * (Pu * log(Pu / M));
-        if (Qu != 0) ls += 0.5 * (Qu * log(Qu / M));
-      }
-      if (keep >= 0) {
-        bd.out_lval[((size_t)keep * 2 + 0) * S + uu] = Pu;
-        bd.out_lval[((size_t)keep * 2 + 1) * S + uu] = Qu;
-      }
-    }
-    for (int o = 16; o > 0; o >>= 1) ls += __shfl_down_sync(0xffffffffu, ls, o);
-    __syncthreads();
-    if (lane == 0) SM.red_d[warp] = ls;
-    __syncthreads();
-    if (tid == 0) {
-      double a = 0;
-      for (int w = 0; w < nw; w++) a += SM.red_d[w];
-      js = a / log(2.0);
-      bool degenerate = (mx[0] == mn[0]) || (mx[1] == mn[1]);
-      if (degenerate) js = __longlong_as_double(0x7ff8000000000000ll);
-      bd.js[u] = js;
-      bd.U[u] = U;
-      bd.status[u] = SM.status;
-    }
-  }
+  if (tid == 0) {
+    bd.U[u] = U;
+    bd.status[u] = SM.status;
   }
 
   // ---- P7: detailed outputs of kept units
@@ -1368,6 +1201,80 @@ __global__ void __launch_bounds__(256, 3) k_units(const __grid_constant__ SetDev
       }
       __syncwarp();
     }
+  }
+}
+
+// Normalisation (main.cu:1302-1404) and JS (main.cu:1406-1428) of every
+// unit of a batch, one warp per unit, from the node-summed fixed-point
+// scores k_units left in the unit's scratch: per class min, max and mean of
+// the scores, likelihoods exp((d - mean) 10 / (max - min)) normalised to
+// sum 1, then the two KL terms of kool() (routines.cu:42-60), zeros
+// skipped, in FP64.  A unit k_units gave up on (U < 0) is left as it is.
+__global__ void __launch_bounds__(256) k_js(const __grid_constant__ SetDev sd,
+                                            const __grid_constant__ BatchDev bd) {
+  const int u = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+  const int lane = threadIdx.x & 31;
+  if (u >= bd.B) return;
+  const int U = bd.U[u];
+  if (U < 0) return;
+  const int S = sd.S;
+  const UnitLayout L = unit_layout(sd.c, S, bd.kmax);
+  const long long *dist = (const long long *)(bd.scratch + (size_t)u * bd.unit_bytes + L.dist);
+  long long l0 = LLONG_MAX, h0 = LLONG_MIN, l1 = LLONG_MAX, h1 = LLONG_MIN;
+  for (int uu = lane; uu < U; uu += 32) {
+    const long long a = dist[uu], b = dist[S + uu];
+    l0 = a < l0 ? a : l0;
+    h0 = a > h0 ? a : h0;
+    l1 = b < l1 ? b : l1;
+    h1 = b > h1 ? b : h1;
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    long long x;
+    x = __shfl_xor_sync(0xffffffffu, l0, o); l0 = x < l0 ? x : l0;
+    x = __shfl_xor_sync(0xffffffffu, h0, o); h0 = x > h0 ? x : h0;
+    x = __shfl_xor_sync(0xffffffffu, l1, o); l1 = x < l1 ? x : l1;
+    x = __shfl_xor_sync(0xffffffffu, h1, o); h1 = x > h1 ? x : h1;
+  }
+  double s0 = 0.0, s1 = 0.0;
+  for (int uu = lane; uu < U; uu += 32) {
+    s0 += (double)(dist[uu] - l0);
+    s1 += (double)(dist[S + uu] - l1);
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    s0 += __shfl_xor_sync(0xffffffffu, s0, o);
+    s1 += __shfl_xor_sync(0xffffffffu, s1, o);
+  }
+  const double m0 = s0 / (double)U, m1 = s1 / (double)U;
+  const double sA = 10.0 / (double)(h0 - l0), sB = 10.0 / (double)(h1 - l1);
+  double e0 = 0.0, e1 = 0.0;
+  for (int uu = lane; uu < U; uu += 32) {
+    e0 += exp(((double)(dist[uu] - l0) - m0) * sA);
+    e1 += exp(((double)(dist[S + uu] - l1) - m1) * sB);
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    e0 += __shfl_xor_sync(0xffffffffu, e0, o);
+    e1 += __shfl_xor_sync(0xffffffffu, e1, o);
+  }
+  const int keep = bd.keep_slot ? bd.keep_slot[u] : -1;
+  double ls = 0.0;
+  for (int uu = lane; uu < U; uu += 32) {
+    const double Pu = exp(((double)(dist[uu] - l0) - m0) * sA) / e0;
+    const double Qu = exp(((double)(dist[S + uu] - l1) - m1) * sB) / e1;
+    const double M = (Pu + Qu) / 2;
+    if (M != 0) {
+      if (Pu != 0) ls += 0.5 * (Pu * log(Pu / M));
+      if (Qu != 0) ls += 0.5 * (Qu * log(Qu / M));
+    }
+    if (keep >= 0) {
+      bd.out_lval[((size_t)keep * 2 + 0) * S + uu] = Pu;
+      bd.out_lval[((size_t)keep * 2 + 1) * S + uu] = Qu;
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) ls += __shfl_xor_sync(0xffffffffu, ls, o);
+  if (lane == 0) {
+    double js = ls / log(2.0);
+    if (h0 == l0 || h1 == l1) js = __longlong_as_double(0x7ff8000000000000ll);
+    bd.js[u] = js;
   }
 }
 
@@ -1408,6 +1315,9 @@ cudaError_t launch_units(const SetDev &sd, const BatchDev &bd, cudaStream_t st) 
   cudaError_t e = cudaFuncSetAttribute(k_units, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   k_units<<<bd.B, threads, smem, st>>>(sd, bd);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  k_js<<<(bd.B + 7) / 8, 256, 0, st>>>(sd, bd);
   return cudaGetLastError();
 }
 
