@@ -388,14 +388,16 @@ int run_units(eddy_ctx *ctx, SetRun &sr, int nunits, const uint64_t *masks_host,
   SetDev &sd = sr.sd;
   const int W = sd.W, c = sd.c, S = sd.S, g = sd.g;
   const bool keeping = keep != nullptr;
-  // batch size: bounded by memory (~3 GB for masks, decisions and scratch);
+  // batch size: bounded by memory (masks, decisions and scratch);
   // kmax: changed-node records per network (EDDY_KMAX lowers it, to test the
   // re-run of the units that overflow it)
   int kmax = 16;
   if (const char *ek = getenv("EDDY_KMAX")) kmax = std::max(1, std::min(16, atoi(ek)));
   size_t per_unit = unit_scratch_bytes(c, S, kmax) + sizeof(uint32_t) * (size_t)c + 8 * W + 64;
-  int Bmax = (int)std::max<size_t>(1, ((size_t)3 << 30) / std::max<size_t>(per_unit, 1));
-  Bmax = std::min(Bmax, 4096);
+  // (up to 16 GB and 16384 units per batch: the general-path queue holds
+  // unit indices below 2^15)
+  int Bmax = (int)std::max<size_t>(1, ((size_t)16 << 30) / std::max<size_t>(per_unit, 1));
+  Bmax = std::min(Bmax, 16384);
   std::vector<uint32_t> status;
   const int mpk = std::max(1, mpk_req);
   if (keeping) {

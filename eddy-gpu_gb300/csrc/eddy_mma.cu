@@ -355,9 +355,8 @@ __global__ void __maxnreg__(max_regs<kEpi>())
             it[1] = (uint32_t)o[2] | ((uint32_t)o[3] << 16);
             it[2] = (uint32_t)o[4] | ((uint32_t)o[5] << 16);
             it[3] = (uint32_t)o[6] | ((uint32_t)o[7] << 16);
-            it[4] = (uint32_t)o[8] | ((uint32_t)u << 16) | ((uint32_t)cls << 28) |
-                    ((uint32_t)prior << 29);
-            it[5] = (uint32_t)p;
+            it[4] = (uint32_t)o[8] | ((uint32_t)cls << 16) | ((uint32_t)prior << 17);
+            it[5] = (uint32_t)p | ((uint32_t)u << 17);  // pair < 2^17, unit < 2^15
           } else {
             atomicOr(err, 2u);
           }
@@ -452,8 +451,8 @@ __global__ void __launch_bounds__(256) k_general(const __grid_constant__ SetDev 
     const unsigned i = (unsigned)(task / 10);
     const int slot = (int)(task % 10);
     const unsigned *it = items + (size_t)i * kQWords;
-    const int u = (int)((it[4] >> 16) & 0xFFFu), cls = (it[4] >> 28) & 1,
-              prior = (it[4] >> 29) & 1, p = (int)it[5];
+    const int cls = (it[4] >> 16) & 1, prior = (it[4] >> 17) & 1;
+    const int p = (int)(it[5] & 0x1FFFFu), u = (int)(it[5] >> 17);
     int t[9] = {(int)(it[0] & 0xFFFFu), (int)(it[0] >> 16), (int)(it[1] & 0xFFFFu),
                 (int)(it[1] >> 16),     (int)(it[2] & 0xFFFFu), (int)(it[2] >> 16),
                 (int)(it[3] & 0xFFFFu), (int)(it[3] >> 16),     (int)(it[4] & 0xFFFFu)};
