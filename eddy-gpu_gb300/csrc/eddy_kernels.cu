@@ -188,6 +188,37 @@ __global__ void __launch_bounds__(128) k_pairs(const __grid_constant__ SetDev sd
 }
 
 // ------------------------------------------------------------ k_units
+// Open-addressing table: key -> smallest value inserted with it.  `empty`
+// marks a free slot (no real key equals it); probing stops after `probes`
+// slots (an insert that finds no place returns false).
+struct MinTable {
+  unsigned long long *key;
+  int *val;
+  unsigned mask;
+  unsigned long long empty;
+  unsigned probes;
+  __device__ bool insert_min(unsigned long long k, int v) const {
+    unsigned slot = (unsigned)(mix64(k) & mask);
+    for (unsigned i = 0; i < probes; i++, slot = (slot + 1) & mask) {
+      const unsigned long long prev = atomicCAS(&key[slot], empty, k);
+      if (prev == empty || prev == k) {
+        atomicMin(&val[slot], v);
+        return true;
+      }
+    }
+    return false;
+  }
+  // value of a key that was inserted
+  __device__ int get(unsigned long long k) const {
+    unsigned slot = (unsigned)(mix64(k) & mask);
+    while (key[slot] != k) slot = (slot + 1) & mask;
+    return val[slot];
+  }
+};
+// slots of the shared-memory tables (in the BDeu work region, idle then)
+constexpr int kSmSlots = 512;
+constexpr unsigned kSmProbes = 64;
+
 struct UnitLayout {
   size_t phi[2], pcol[2], rec, htk, htv, dist, uid, urep, sig;
   size_t skey, sbits, srep, hsk, hsv, wl, total;
@@ -272,6 +303,7 @@ struct UnitSmem {
   int nphi[2];
   int ndab;
   int nrphi[2];
+  int tfull;    // a shared-memory table ran out of probes
   int nent[2];  // flip entries per class
   int nwl;      // work-list length
   int firstB0;  // first class-2 network equal to the class-2 full network
@@ -496,15 +528,6 @@ __global__ void __launch_bounds__(256, 3) k_units(const __grid_constant__ SetDev
   // entry ranges of rows: start = INT_MAX, end = 0 until an entry lands
   for (int i = tid; i < 4 * g; i += nt) P.phs[i] = (i < 2 * g) ? 0x7fffffff : 0;
   for (int i = tid; i < 82; i += nt) P.dmap[i] = c_dmap[i];
-  // hash tables, 16 bytes per store (HT is a power of two >= 8)
-  for (int i = tid; i < L.HT / 2; i += nt) {
-    reinterpret_cast<uint4 *>(htk)[i] = make_uint4(~0u, ~0u, ~0u, ~0u);
-    reinterpret_cast<uint4 *>(hsk)[i] = make_uint4(0u, 0u, 0u, 0u);
-  }
-  for (int i = tid; i < L.HT / 4; i += nt) {
-    reinterpret_cast<uint4 *>(htv)[i] = make_uint4(0x7fffffffu, 0x7fffffffu, 0x7fffffffu, 0x7fffffffu);
-    reinterpret_cast<uint4 *>(hsv)[i] = make_uint4(0x7fffffffu, 0x7fffffffu, 0x7fffffffu, 0x7fffffffu);
-  }
   __syncthreads();
   for (int i = tid; i < g * 3; i += nt) {
     const uint64_t *pl = sd.planes + (size_t)i * W;
@@ -725,40 +748,53 @@ __global__ void __launch_bounds__(256, 3) k_units(const __grid_constant__ SetDev
     }
     return any ? (key | 1ull) : 0ull;
   };
+  // Tables (key -> smallest network index) in shared memory first; a unit
+  // whose keys do not fit there within kSmProbes probes uses its global
+  // table of HT slots instead (initialised only then).
+  unsigned long long *smk = P.itk;
+  int *smv = (int *)P.acc;
+  auto table_init = [&](unsigned long long *k, int *v, int slots, unsigned long long empty) {
+    for (int i = tid; i < slots; i += nt) {
+      k[i] = empty;
+      v[i] = 0x7fffffff;
+    }
+  };
+  const MinTable sig_sm{smk, smv, kSmSlots - 1, 0ull, kSmProbes};
+  const MinTable sig_gl{hsk, hsv, (unsigned)HTs - 1, 0ull, (unsigned)HTs};
+  table_init(smk, smv, kSmSlots, 0ull);
   if (tid == 0) {
     skey[0] = skey[S - 1] = 0ull;
     sbits[0] = sbits[S - 1] = 0ull;
     srep[0] = 0;
     srep[S - 1] = S - 1;
+    SM.tfull = 0;
   }
+  __syncthreads();
   for (int s = 1 + tid; s < S - 1; s += nt) {
     unsigned long long bits;
     const unsigned long long key = signature(class_of(s), sig[s - 1], bits);
     skey[s] = key;
     sbits[s] = bits;
-    if (key) {
-      unsigned slot = (unsigned)(mix64(key) & (HTs - 1));
-      while (true) {
-        const unsigned long long prev = atomicCAS(&hsk[slot], 0ull, key);
-        if (prev == 0ull || prev == key) {
-          atomicMin(&hsv[slot], s);
-          break;
-        }
-        slot = (slot + 1) & (HTs - 1);
-      }
-    }
+    if (key && !sig_sm.insert_min(key, s)) SM.tfull = 1;
   }
   if (tid == 0) SM.nwl = 0;
   __syncthreads();
+  const bool sig_global = SM.tfull != 0;
+  if (sig_global) {
+    table_init(hsk, hsv, HTs, 0ull);
+    __syncthreads();
+    for (int s = 1 + tid; s < S - 1; s += nt)
+      if (skey[s]) sig_gl.insert_min(skey[s], s);
+    __syncthreads();
+  }
+  const MinTable &sig_tab = sig_global ? sig_gl : sig_sm;
   // representatives, the work list of distinct signatures, and an exact check
   // that every network shares its representative's triggered entries
   for (int s = 1 + tid; s < S - 1; s += nt) {
     const unsigned long long key = skey[s];
     int rep = s;
     if (key) {
-      unsigned slot = (unsigned)(mix64(key) & (HTs - 1));
-      while (hsk[slot] != key) slot = (slot + 1) & (HTs - 1);
-      rep = hsv[slot];
+      rep = sig_tab.get(key);
       if (rep == s) {
         wl[atomicAdd(&SM.nwl, 1)] = s;
       } else {
@@ -896,30 +932,31 @@ __global__ void __launch_bounds__(256, 3) k_units(const __grid_constant__ SetDev
     return s == 0 || s == firstB0 ||
            (s != S - 1 && skey[s] != 0 && srep[s] == s && rec[(size_t)s * L.rec_words + 1] != 0);
   };
-  auto slot_of = [&](unsigned long long key) -> unsigned {
-    unsigned slot = (unsigned)(mix64(key) & (HT - 1));
-    while (htk[slot] != key) slot = (slot + 1) & (HT - 1);
-    return slot;
-  };
-  for (int s = tid; s < S; s += nt) {
-    if (!inserted(s)) continue;
+  // network table: shared memory first (the signature table is done with),
+  // the global one when the inserted networks do not fit
+  const MinTable net_sm{smk, smv, kSmSlots - 1, ~0ull, kSmProbes};
+  const MinTable net_gl{htk, htv, (unsigned)HT - 1, ~0ull, (unsigned)HT};
+  auto net_key = [&](int s) -> unsigned long long {
     unsigned long long key = rec_of(s)[0];
-    if (key == ~0ull) key ^= 1ull;
-    unsigned slot = (unsigned)(mix64(key) & (HT - 1));
-    while (true) {
-      unsigned long long prev = atomicCAS(&htk[slot], ~0ull, key);
-      if (prev == ~0ull || prev == key) {
-        atomicMin(&htv[slot], s);
-        break;
-      }
-      slot = (slot + 1) & (HT - 1);
-    }
-  }
+    return key == ~0ull ? key ^ 1ull : key;
+  };
+  table_init(smk, smv, kSmSlots, ~0ull);
+  if (tid == 0) SM.tfull = 0;
   __syncthreads();
+  for (int s = tid; s < S; s += nt)
+    if (inserted(s) && !net_sm.insert_min(net_key(s), s)) SM.tfull = 1;
+  __syncthreads();
+  const bool net_global = SM.tfull != 0;
+  if (net_global) {
+    table_init(htk, htv, HT, ~0ull);
+    __syncthreads();
+    for (int s = tid; s < S; s += nt)
+      if (inserted(s)) net_gl.insert_min(net_key(s), s);
+    __syncthreads();
+  }
+  const MinTable &net_tab = net_global ? net_gl : net_sm;
   if (tid == 0) {
-    unsigned long long kb = rec_of(firstB0)[0];
-    if (kb == ~0ull) kb ^= 1ull;
-    SM.repB = htv[slot_of(kb)];
+    SM.repB = net_tab.get(net_key(firstB0));
     SM.nwl = 0;
   }
   __syncthreads();
@@ -934,9 +971,7 @@ __global__ void __launch_bounds__(256, 3) k_units(const __grid_constant__ SetDev
       if (Rs[1] == 0) {
         rep = (class_of(s) == 0) ? 0 : repB;
       } else {
-        unsigned long long key = Rs[0];
-        if (key == ~0ull) key ^= 1ull;
-        rep = htv[slot_of(key)];
+        rep = net_tab.get(net_key(s));
       }
       uq = (rep == s) ? 1 : 0;
       // inserted networks merged by hash are checked list by list below
