@@ -117,6 +117,12 @@ struct eddy_ctx {
   DevBuf d_masks, d_dmask, d_scratch, d_js, d_U, d_status, d_keep, d_uset, d_uperm;
   DevBuf d_oids, d_ocnt, d_opar, d_odist, d_olval, d_orows, d_stats;
   DevBuf d_Y, d_afp8, d_err;  // tensor-core contingency operands
+  // d_dmask is all zero between batches (decisions only set bits, the unit
+  // kernel clears what it reads) while this equals d_dmask.p; null = unknown
+  void *dmask_clean = nullptr;
+  // the JS values of an eddy_run call, every set's R in a row, for the
+  // beta fit on the device; positions of a batch's units in it; fit results
+  DevBuf d_jsall, d_jpos, d_fit;
   PinnedBuf h_stage;          // per-batch indices and results
   PinnedBuf h_vals;           // the resident set's values on their way in
   int sms = 148;
@@ -328,6 +334,17 @@ int prepare_pairs(eddy_ctx *ctx, const SetDev &sd, int B) {
   return EDDY_OK;
 }
 
+// A decision buffer for B units of c pairs that holds only zeros: cleared
+// in full after an allocation or a batch that did not finish.
+int dmask_ready(eddy_ctx *ctx, int B, int c) {
+  CK(ctx->d_dmask.ensure(dmask_bytes(B, c)));
+  if (ctx->dmask_clean != ctx->d_dmask.p) {
+    CK(cudaMemsetAsync(ctx->d_dmask.p, 0, ctx->d_dmask.n, ctx->stream));
+    ctx->dmask_clean = ctx->d_dmask.p;
+  }
+  return EDDY_OK;
+}
+
 int launch_pairs_any(eddy_ctx *ctx, const SetDev &sd, const uint64_t *masks, int B, uint32_t *dmask,
                      unsigned long long *stats, bool force_popc = false) {
   if (sd.c == 0) return EDDY_OK;
@@ -383,8 +400,10 @@ int check_mma_error(eddy_ctx *ctx) {
 
 // Runs units of one set.  masks_host: B x W host masks, or null to
 // generate counter-mode masks for perms[] on the device.
+// js_dev >= 0: unit i's JS also goes to d_jsall[js_dev + i].
 int run_units(eddy_ctx *ctx, SetRun &sr, int nunits, const uint64_t *masks_host,
-              const int32_t *perms, double *js, int32_t *U, KeepOut *keep, int mpk_req) {
+              const int32_t *perms, double *js, int32_t *U, KeepOut *keep, int mpk_req,
+              long long js_dev = -1) {
   SetDev &sd = sr.sd;
   const int W = sd.W, c = sd.c, S = sd.S, g = sd.g;
   const bool keeping = keep != nullptr;
@@ -423,9 +442,10 @@ int run_units(eddy_ctx *ctx, SetRun &sr, int nunits, const uint64_t *masks_host,
       const int Bt = (int)todo.size();
       const size_t ub = unit_scratch_bytes(c, S, kmax_run);
       CK(ctx->d_masks.ensure(sizeof(uint64_t) * (size_t)Bt * W));
-      CK(ctx->d_dmask.ensure(dmask_bytes(Bt, c)));
-      CK(cudaMemsetAsync(ctx->d_dmask.as<uint32_t>() + (size_t)Bt * (c > 0 ? c : 1), 0,
-                         sizeof(uint32_t) * (size_t)Bt * chunk_words(c > 0 ? c : 1), ctx->stream));
+      {
+        int rc = dmask_ready(ctx, Bt, c);
+        if (rc) return rc;
+      }
       CK(ctx->d_scratch.ensure(ub * Bt));
       CK(ctx->d_js.ensure(sizeof(double) * Bt));
       CK(ctx->d_U.ensure(sizeof(int32_t) * Bt));
@@ -460,6 +480,13 @@ int run_units(eddy_ctx *ctx, SetRun &sr, int nunits, const uint64_t *masks_host,
       }
       // the kept unit (the first of the call) writes its detailed outputs;
       // slot -1 (every byte 0xFF) for the others
+      if (js_dev >= 0) {
+        // (staging: after the set ids and permutation indices)
+        int32_t *hq = ctx->h_stage.as<int32_t>() + 2 * (size_t)Bt;
+        for (int i = 0; i < Bt; i++) hq[i] = (int32_t)(js_dev + b0 + todo[i]);
+        CK(ctx->d_jpos.ensure(sizeof(int32_t) * Bt));
+        CK(cudaMemcpyAsync(ctx->d_jpos.p, hq, 4 * (size_t)Bt, cudaMemcpyHostToDevice, ctx->stream));
+      }
       int i0 = -1;
       for (int i = 0; i < Bt && keeping; i++)
         if (b0 + todo[i] == 0) i0 = i;
@@ -473,6 +500,8 @@ int run_units(eddy_ctx *ctx, SetRun &sr, int nunits, const uint64_t *masks_host,
       bd.scratch = ctx->d_scratch.as<uint8_t>();
       bd.unit_bytes = ub;
       bd.js = ctx->d_js.as<double>();
+      bd.js_all = js_dev >= 0 ? ctx->d_jsall.as<double>() : nullptr;
+      bd.js_pos = js_dev >= 0 ? ctx->d_jpos.as<int32_t>() : nullptr;
       bd.U = ctx->d_U.as<int32_t>();
       bd.status = ctx->d_status.as<uint32_t>();
       bd.keep_slot = ctx->d_keep.as<int32_t>();
@@ -509,6 +538,7 @@ int run_units(eddy_ctx *ctx, SetRun &sr, int nunits, const uint64_t *masks_host,
         ctx->launches += 2;  // networks, then normalisation and JS
         return EDDY_OK;
       };
+      ctx->dmask_clean = nullptr;  // until the batch is seen to finish
       if (graphable) {
         {
           int rc = prepare_pairs(ctx, sd, Bt);
@@ -524,7 +554,8 @@ int run_units(eddy_ctx *ctx, SetRun &sr, int nunits, const uint64_t *masks_host,
             (uintptr_t)ctx->d_js.p, (uintptr_t)ctx->d_U.p, (uintptr_t)ctx->d_status.p,
             (uintptr_t)ctx->d_keep.p, (uintptr_t)ctx->d_uset.p, (uintptr_t)ctx->d_uperm.p,
             (uintptr_t)ctx->d_stats.p, (uintptr_t)ctx->d_afp8.p, (uintptr_t)ctx->d_Y.p,
-            (uintptr_t)ctx->d_err.p, (uintptr_t)ctx->d_mask0.p, (uintptr_t)ctx->stream};
+            (uintptr_t)ctx->d_err.p, (uintptr_t)ctx->d_mask0.p, (uintptr_t)ctx->stream,
+            (uintptr_t)bd.js_all, (uintptr_t)bd.js_pos};
         if (key != ctx->graph_key || !ctx->graph_exec) {
           if (ctx->graph_exec) {
             cudaGraphExecDestroy(ctx->graph_exec);
@@ -573,6 +604,7 @@ int run_units(eddy_ctx *ctx, SetRun &sr, int nunits, const uint64_t *masks_host,
       std::vector<int32_t> Ub(hU, hU + Bt);
       status.assign(hst, hst + Bt);
       if (errw & 1u) return fail(ctx, EDDY_ERR_INTERNAL, "tensor-core pipeline wait timed out");
+      ctx->dmask_clean = ctx->d_dmask.p;  // the unit kernel cleared every bit set
       if (errw & 2u) {
         // the general-path queue overflowed (a large share of tables near a
         // threshold): decide this batch with the popcount kernel
@@ -815,15 +847,18 @@ int eddy_set_labellings(eddy_ctx *ctx, int set_id, const uint8_t *labels, int R)
   return EDDY_OK;
 }
 
-static int run_set(eddy_ctx *ctx, int set_id) {
+// Iterations of a set in eddy_run (0: EXTERNAL labellings missing).
+static int set_iterations(const eddy_ctx *ctx, const SetHost &S) {
+  return ctx->o.rng == EDDY_RNG_EXTERNAL ? std::max(S.R_ext, 0) : ctx->o.permutations;
+}
+
+// Runs one set; its JS values also go to d_jsall[js_off ..] for the fit.
+static int run_set(eddy_ctx *ctx, int set_id, long long js_off) {
   SetHost &S = ctx->sets[set_id];
   const int n = ctx->samples, W = ctx->W;
   const int g = (int)S.genes.size();
-  int R = ctx->o.permutations;
-  if (ctx->o.rng == EDDY_RNG_EXTERNAL) {
-    if (S.R_ext < 1) return fail(ctx, EDDY_ERR_STATE, "set %d has no labellings", set_id);
-    R = S.R_ext;
-  }
+  const int R = set_iterations(ctx, S);
+  if (R < 1) return fail(ctx, EDDY_ERR_STATE, "set %d has no labellings", set_id);
   S.js.assign(R, NAN);
   S.U.assign(R, 0);
   S.iterations = 0;
@@ -857,7 +892,7 @@ static int run_set(eddy_ctx *ctx, int set_id) {
     for (int i = 0; i < R; i++) perms[i] = i;
     KeepOut K;
     rc = run_units(ctx, sr, R, nullptr, perms.data(), S.js.data(), S.U.data(),
-                   ctx->o.keep_networks ? &K : nullptr, mpk0);
+                   ctx->o.keep_networks ? &K : nullptr, mpk0, js_off);
     if (rc) return rc;
     if (ctx->o.keep_networks) store_keep(ctx, S, K, g);
     else S.U0 = S.U[0];
@@ -882,7 +917,7 @@ static int run_set(eddy_ctx *ctx, int set_id) {
     labels_to_mask(lab.data(), n, W, masks.data());
     KeepOut K;
     rc = run_units(ctx, sr, 1, masks.data(), nullptr, S.js.data(), S.U.data(),
-                   ctx->o.keep_networks ? &K : nullptr, mpk0);
+                   ctx->o.keep_networks ? &K : nullptr, mpk0, js_off);
     if (rc) return rc;
     if (ctx->o.keep_networks) store_keep(ctx, S, K, g);
     else S.U0 = S.U[0];
@@ -916,7 +951,7 @@ static int run_set(eddy_ctx *ctx, int set_id) {
         }
       }
       rc = run_units(ctx, sr, nu, device_counter ? nullptr : mh.data(), perms.data(), S.js.data() + 1,
-                     S.U.data() + 1, nullptr, 1);
+                     S.U.data() + 1, nullptr, 1, js_off + 1);
       if (rc) return rc;
     }
     S.iterations = R;
@@ -927,8 +962,43 @@ static int run_set(eddy_ctx *ctx, int set_id) {
   S.tables += st[1];
   for (int i = 0; i < R; i++)
     if (!finite_js(S.js[i])) S.failed = 1;
-  if (!S.failed) S.betafit_ok = beta_pddn(S.js.data(), R, S.alpha, S.beta, S.pddn) ? 1 : 0;
-  S.done = true;
+  S.done = true;  // the beta fit follows in eddy_run, on the device
+  return EDDY_OK;
+}
+
+// Beta fit and pDDN (main.cu:1488-1502) of the sets of one eddy_run call
+// whose JS values are all finite (main.cu:1465-1479), in one launch over
+// d_jsall; offsets and counts in and four doubles per set out through the
+// pinned staging.
+static int fit_sets(eddy_ctx *ctx, const std::vector<int> &run, const std::vector<long long> &off) {
+  std::vector<int> fit;
+  for (size_t k = 0; k < run.size(); k++)
+    if (!ctx->sets[run[k]].failed) fit.push_back((int)k);
+  const size_t m = fit.size();
+  if (m == 0) return EDDY_OK;
+  CK(ctx->h_stage.ensure(48 * m + 64));
+  CK(ctx->d_fit.ensure(48 * m));
+  long long *ho = ctx->h_stage.as<long long>();
+  int32_t *hr = ctx->h_stage.as<int32_t>(8 * m);
+  double *hout = ctx->h_stage.as<double>(16 * m);
+  for (size_t i = 0; i < m; i++) {
+    ho[i] = off[fit[i]];
+    hr[i] = ctx->sets[run[fit[i]]].iterations;
+  }
+  char *d = ctx->d_fit.as<char>();
+  CK(cudaMemcpyAsync(d, ho, 12 * m, cudaMemcpyHostToDevice, ctx->stream));
+  CK(launch_beta_fit(ctx->d_jsall.as<double>(), (const long long *)d, (const int *)(d + 8 * m),
+                     (int)m, (double *)(d + 16 * m), ctx->stream));
+  ctx->launches++;
+  CK(cudaMemcpyAsync(hout, d + 16 * m, 32 * m, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  for (size_t i = 0; i < m; i++) {
+    SetHost &S = ctx->sets[run[fit[i]]];
+    S.alpha = hout[4 * i];
+    S.beta = hout[4 * i + 1];
+    S.pddn = hout[4 * i + 2];
+    S.betafit_ok = hout[4 * i + 3] != 0.0 ? 1 : 0;
+  }
   return EDDY_OK;
 }
 
@@ -937,12 +1007,23 @@ int eddy_run(eddy_ctx *ctx) {
   if (ctx->samples == 0) return fail(ctx, EDDY_ERR_STATE, "no matrix loaded");
   ctx->ms_total = ctx->ms_pairs = ctx->ms_units = 0;
   ctx->launches = 0;
+  // the JS values of every pending set in one device array (R per set)
+  std::vector<int> run;
+  std::vector<long long> off;
+  long long total = 0;
   for (int s = 0; s < (int)ctx->sets.size(); s++) {
     if (ctx->sets[s].done) continue;
-    int rc = run_set(ctx, s);
+    run.push_back(s);
+    off.push_back(total);
+    total += std::max(1, set_iterations(ctx, ctx->sets[s]));
+  }
+  if (total > INT32_MAX) return fail(ctx, EDDY_ERR_CAPACITY, "over 2^31 iterations in one run");
+  if (total > 0) CK(ctx->d_jsall.ensure(sizeof(double) * (size_t)total));
+  for (size_t k = 0; k < run.size(); k++) {
+    int rc = run_set(ctx, run[k], off[k]);
     if (rc) return rc;
   }
-  return EDDY_OK;
+  return fit_sets(ctx, run, off);
 }
 
 int eddy_get_set_summary(const eddy_ctx *ctx, int set_id, eddy_set_summary *out) {
@@ -1033,9 +1114,9 @@ int eddy_debug_edges(eddy_ctx *ctx, int set_id, const uint8_t *labels, uint8_t *
   std::vector<uint64_t> m(W);
   labels_to_mask(labels, n, W, m.data());
   CK(ctx->d_masks.ensure(8 * W));
-  CK(ctx->d_dmask.ensure(dmask_bytes(1, c)));
-  CK(cudaMemsetAsync(ctx->d_dmask.as<uint32_t>() + (c > 0 ? c : 1), 0,
-                     sizeof(uint32_t) * chunk_words(c > 0 ? c : 1), ctx->stream));
+  rc = dmask_ready(ctx, 1, c);
+  if (rc) return rc;
+  ctx->dmask_clean = nullptr;  // no unit kernel reads (and clears) these masks
   CK(cudaMemcpyAsync(ctx->d_masks.p, m.data(), 8 * W, cudaMemcpyHostToDevice, ctx->stream));
   rc = launch_pairs_any(ctx, sd, ctx->d_masks.as<uint64_t>(), 1, ctx->d_dmask.as<uint32_t>(), nullptr);
   if (rc) return rc;

@@ -53,9 +53,10 @@ struct SetDev {
 
 // Per-batch pointers for the unit kernel.
 // Decision masks of a batch: [B][c] u32, followed by a bitmap per unit of
-// the 32-pair chunks that hold a nonzero mask ([B][chunk_words(c)] u32);
-// the bitmap is zeroed before the decision kernel, which sets a chunk's bit
-// whenever it writes a nonzero mask into it.
+// the 32-pair chunks that hold a nonzero mask ([B][chunk_words(c)] u32).
+// Between batches the whole buffer is zero: the decision kernels only set
+// bits (and a chunk's bit with every nonzero mask in it), and the unit
+// kernel clears each mask word and chunk bit it reads.
 #ifdef __CUDACC__
 #define EDDY_HD __host__ __device__
 #else
@@ -79,10 +80,12 @@ struct BatchDev {
   int B;                       // units in the batch
   int kmax;                    // changed-node records per network
   const uint64_t *masks;       // [B][W] class-1 sample mask per unit
-  const uint32_t *dmask;       // [B][c] decision masks (class 1 bits 0-9, class 2 bits 16-25)
+  uint32_t *dmask;             // [B][c] decision masks (class 1 bits 0-9, class 2 bits 16-25)
   uint8_t *scratch;            // per-unit scratch, unit_bytes each
   size_t unit_bytes;
   double *js;                  // [B]
+  double *js_all;              // null, or the run's JS array, where unit u's
+  const int32_t *js_pos;       //   JS also goes, at index js_pos[u]
   int32_t *U;                  // [B]
   uint32_t *status;            // [B]
   int32_t *keep_slot;          // [B] -1 or slot of detailed output

@@ -507,7 +507,7 @@ __global__ void __launch_bounds__(256, 3) k_units(const __grid_constant__ SetDev
   unsigned long long *hsk = (unsigned long long *)(scr + L.hsk);
   int *hsv = (int *)(scr + L.hsv);
   int *wl = (int *)(scr + L.wl);
-  const uint32_t *dm = bd.dmask + (size_t)u * c;
+  uint32_t *dm = bd.dmask + (size_t)u * c;
   const int tid = threadIdx.x, nt = blockDim.x;
 
   // ---- P0: masks, state counts, selection prefixes, init
@@ -571,9 +571,10 @@ __global__ void __launch_bounds__(256, 3) k_units(const __grid_constant__ SetDev
 
   // ---- P1: full-network rows and flip lists, from the 32-pair chunks that
   // hold a nonzero mask (the decision kernel's bitmap; the other chunks are
-  // all zero).  Warp w owns the rows whose pairs start in [w c/nw,
-  // (w+1) c/nw) and walks its flagged chunks in pair order, four loads at a
-  // time.  Edge bits go into the row bitsets; the flip entries land, in pair
+  // all zero).  Each nonzero mask word read is set back to zero.  Warp w
+  // owns the rows whose pairs start in [w c/nw, (w+1) c/nw) and walks its
+  // flagged chunks in pair order, four loads at a time.  Edge bits go into
+  // the row bitsets; the flip entries land, in pair
   // order, in the warp's own segment of the list (which starts at its first
   // pair); a row's entry range is the min / max position of its entries
   // (rows without entries keep start > end).
@@ -593,7 +594,7 @@ __global__ void __launch_bounds__(256, 3) k_units(const __grid_constant__ SetDev
     const int pa = r0 * (r0 - 1) / 2, pb = r0 < r1 ? r1 * (r1 - 1) / 2 : pa;
     int wpos0 = pa, wpos1 = pa;
     const uint32_t below = (1u << lane) - 1u;
-    const uint32_t *cbits = chunk_bits(const_cast<uint32_t *>(bd.dmask), bd.B, c, u);
+    const uint32_t *cbits = chunk_bits(bd.dmask, bd.B, c, u);
     const int k0 = pa >> 5, k1 = (pb + 31) >> 5;  // chunks [k0, k1)
     auto chunk = [&](int k, uint32_t m) {
       const int p = 32 * k + lane;
@@ -642,11 +643,19 @@ __global__ void __launch_bounds__(256, 3) k_units(const __grid_constant__ SetDev
         }
 #pragma unroll
         for (int q = 0; q < 4; q++)
-          if (ks[q] >= 0) chunk(ks[q], mv[q]);
+          if (ks[q] >= 0) {
+            chunk(ks[q], mv[q]);
+            if (mv[q]) dm[32 * ks[q] + lane] = 0u;  // read once: left zero
+          }
       }
     }
   }
   __syncthreads();
+  // every warp has read the unit's chunk bitmap: zero it for the next batch
+  {
+    uint32_t *cb = chunk_bits(bd.dmask, bd.B, c, u);
+    for (int i = tid; i < chunk_words(c); i += nt) cb[i] = 0u;
+  }
 
   // rows holding flip entries, ascending, per class, and entry totals
   if (tid == 0) SM.nent[0] = SM.nent[1] = 0;
@@ -1310,6 +1319,7 @@ __global__ void __launch_bounds__(256) k_js(const __grid_constant__ SetDev sd,
     double js = ls / log(2.0);
     if (h0 == l0 || h1 == l1) js = __longlong_as_double(0x7ff8000000000000ll);
     bd.js[u] = js;
+    if (bd.js_all) bd.js_all[bd.js_pos[u]] = js;
   }
 }
 

@@ -8,8 +8,10 @@
 // accumulation in TMEM, exact for counts < 2^24.  This replaces the S x c x n
 // tally loops of the reference's run2/run2Scalable (kernel1.cu:76-336);
 // class 2 = full-sample table - class 1.  The epilogue reads the counts out
-// of TMEM and makes the 10-bit leave-one-out decision masks of both classes
-// (kernel1.cu:121-203, 419-431) in the same kernel.
+// of TMEM and settles, in the same kernel, every table whose ten
+// leave-one-out variants provably hold no edge; the others are queued for
+// k_general, which sets the bits of the 10-bit decision masks of both
+// classes (kernel1.cu:121-203, 419-431) in a buffer that starts at zero.
 //
 // Tile: 128 units (TMEM lanes) x kGroups column groups of 32 pair-cells
 // (3 pairs x 9 cells + 5 pad columns; N = 128, 192 or 256) x K in
@@ -200,7 +202,7 @@ template <int kStages, int kEpi, int kGroups>
 __global__ void __maxnreg__(max_regs<kEpi>())
     k_pairs_mma(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
                 const __grid_constant__ SetDev sd, const float *__restrict__ ctotf, int B, int nk,
-                int ntiles, int mblocks, uint32_t *dmask, unsigned long long *stats,
+                int ntiles, int mblocks, unsigned long long *stats,
                 unsigned *err, unsigned *gqueue, unsigned qcap) {
   constexpr int kTN = 32 * kGroups;
   constexpr int kPairsPerTile = kGroups * kPairsPerGroup;
@@ -210,6 +212,7 @@ __global__ void __maxnreg__(max_regs<kEpi>())
   constexpr uint32_t kIdesc = idesc_for(kTN);
   constexpr int kPerQuad = kEpi / 4, kGpw = kGroups / kPerQuad;
   static_assert(kEpi % 4 == 0 && kGroups % kPerQuad == 0 && kGroups <= kMaxGroups, "shape");
+  static_assert(2 * kGpw * kPairsPerGroup <= 32, "one bit per table of a thread");
   extern __shared__ __align__(1024) uint8_t smraw[];
   // 1024-byte aligned stage ring, then barriers, then the epilogue buffer
   uint8_t *base = (uint8_t *)(((uintptr_t)smraw + 1023) & ~(uintptr_t)1023);
@@ -248,10 +251,14 @@ __global__ void __maxnreg__(max_regs<kEpi>())
       int stage = 0;
       uint32_t phase = 0;
       long long nfill = 0;
-      for (int t = blockIdx.x; t < ntot && !*verr; t += gridDim.x) {
+      bool live = true;  // false after a wait gave up (the error word is set)
+      for (int t = blockIdx.x; t < ntot && live; t += gridDim.x) {
         const int tn = t / mblocks, mb = t % mblocks;
         for (int kc = 0; kc < nk; kc++) {
-          if (!mbar_wait(smem_u32(&S.empty[stage]), phase ^ 1u, verr)) break;
+          if (!mbar_wait(smem_u32(&S.empty[stage]), phase ^ 1u, verr)) {
+            live = false;
+            break;
+          }
           const uint32_t fb = smem_u32(&S.full[stage]);
           mbar_expect_tx(fb, kStageBytes);
           const uint32_t sa = smem_u32(base + stage * kStageBytes);
@@ -273,7 +280,7 @@ __global__ void __maxnreg__(max_regs<kEpi>())
       int stage = 0, acc = 0;
       uint32_t phase = 0, accphase = 0;
       long long nct = 0;
-      for (int t = blockIdx.x; t < ntot && !*verr; t += gridDim.x) {
+      for (int t = blockIdx.x; t < ntot; t += gridDim.x) {
         if (!mbar_wait(smem_u32(&S.accempty[acc]), accphase ^ 1u, verr)) break;
         tc_fence_after();
         {
@@ -328,9 +335,8 @@ __global__ void __maxnreg__(max_regs<kEpi>())
     // no-edge thresholds of dof 4 without / with a prior (quick_zero_f)
     const float thr0 = sd.exact_all ? -1.f : sd.thr[0][2].chiA;
     const float thr1 = sd.exact_all ? -1.f : sd.thr[1][2].chiA;
-    const uint32_t below = (1u << lane) - 1u;
     unsigned *qitems = gqueue + 4;
-    for (int t = blockIdx.x; t < ntot && !*verr; t += gridDim.x) {
+    for (int t = blockIdx.x; t < ntot; t += gridDim.x) {
       const int tn = t / mblocks, mb = t % mblocks;
       if (!mbar_wait(smem_u32(&S.accfull[acc]), accphase, verr)) break;
       if (!mbar_wait(smem_u32(&S.ctfull[acc]), accphase, verr)) break;
@@ -338,55 +344,8 @@ __global__ void __maxnreg__(max_regs<kEpi>())
       const float *ctile =
           reinterpret_cast<const float *>(base + kStages * kStageBytes + kCtOff + acc * kCtBytes);
       const int u = mb * kTM + row;
-      const bool valid = u < B;
-      // tables the quick filter cannot settle: counts, unit, class, prior
-      // and pair into the launch's queue (one atomic per warp and call)
-      auto enqueue = [&](bool flag, const float *o, int cls, int prior, int p) {
-        const uint32_t bal = __ballot_sync(0xffffffffu, flag);
-        if (bal == 0u) return;
-        unsigned qbase = 0;
-        if (lane == 0) qbase = atomicAdd(gqueue, (unsigned)__popc(bal));
-        qbase = __shfl_sync(0xffffffffu, qbase, 0);
-        if (flag) {
-          const unsigned idx = qbase + (unsigned)__popc(bal & below);
-          if (idx < qcap) {
-            unsigned *it = qitems + (size_t)idx * kQWords;
-            it[0] = (uint32_t)o[0] | ((uint32_t)o[1] << 16);
-            it[1] = (uint32_t)o[2] | ((uint32_t)o[3] << 16);
-            it[2] = (uint32_t)o[4] | ((uint32_t)o[5] << 16);
-            it[3] = (uint32_t)o[6] | ((uint32_t)o[7] << 16);
-            it[4] = (uint32_t)o[8] | ((uint32_t)cls << 16) | ((uint32_t)prior << 17);
-            it[5] = (uint32_t)p | ((uint32_t)u << 17);  // pair < 2^17, unit < 2^15
-          } else {
-            atomicOr(err, 2u);
-          }
-        }
-      };
-      // one pair: class-1 counts cv (FP32 integers from TMEM), class 2 =
-      // full-sample table - class 1
-      auto do_pair = [&](const uint32_t *cv, int grp, int q) {
-        const int p = tn * kPairsPerTile + grp * kPairsPerGroup + q;
-        if (p >= sd.c) return;
-        const float4 *cf =
-            reinterpret_cast<const float4 *>(ctile + (grp * kPairsPerGroup + q) * 12);
-        const float4 f0 = cf[0], f1 = cf[1], f2 = cf[2];
-        float oA[9], oB[9];
-#pragma unroll
-        for (int k = 0; k < 9; k++) oA[k] = __uint_as_float(cv[k]);
-        oB[0] = f0.x - oA[0]; oB[1] = f0.y - oA[1]; oB[2] = f0.z - oA[2];
-        oB[3] = f0.w - oA[3]; oB[4] = f1.x - oA[4]; oB[5] = f1.y - oA[5];
-        oB[6] = f1.z - oA[6]; oB[7] = f1.w - oA[7]; oB[8] = f2.x - oA[8];
-        const int prior = (f2.y != 0.f) ? 1 : 0;
-        const float chiA = prior ? thr1 : thr0;
-        const bool qa = quick_zero_f(oA, chiA), qb = quick_zero_f(oB, chiA);
-        enqueue(valid && !qa, oA, 0, prior, p);
-        enqueue(valid && !qb, oB, 1, prior, p);
-        if (valid) {
-          dmask[(size_t)u * sd.c + p] = 0u;
-          nfilt += (unsigned)qa + (unsigned)qb;
-          ntab += 2;
-        }
-      };
+      // pairs of the tile below c (the last tile's tail is padding)
+      const int lim = sd.c - tn * kPairsPerTile;
       // the warp's column groups out of TMEM, every load issued before one
       // wait; pair q of a group = columns 9q .. 9q+8
       uint32_t r[kGpw][32];
@@ -396,11 +355,82 @@ __global__ void __maxnreg__(max_regs<kEpi>())
         tmem_ld32(tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)(acc * kTN + grp * 32), r[gi]);
       }
       tmem_ld_wait();
+      // one pair's class-1 counts (FP32 integers from TMEM) and class-2
+      // counts (full-sample table - class 1), and its prior flag
+      auto tables = [&](int gi, int q, float *oA, float *oB) -> int {
+        const int lp = (wq + gi * kPerQuad) * kPairsPerGroup + q;
+        const float4 *cf = reinterpret_cast<const float4 *>(ctile + lp * 12);
+        const float4 f0 = cf[0], f1 = cf[1], f2 = cf[2];
+#pragma unroll
+        for (int k = 0; k < 9; k++) oA[k] = __uint_as_float(r[gi][9 * q + k]);
+        oB[0] = f0.x - oA[0]; oB[1] = f0.y - oA[1]; oB[2] = f0.z - oA[2];
+        oB[3] = f0.w - oA[3]; oB[4] = f1.x - oA[4]; oB[5] = f1.y - oA[5];
+        oB[6] = f1.z - oA[6]; oB[7] = f1.w - oA[7]; oB[8] = f2.x - oA[8];
+        return (f2.y != 0.f) ? 1 : 0;
+      };
+      // pass 1: the all-zero bound of every table of the thread, straight
+      // line; bit 2 j + class of qmask (j = pair slot gi * 3 + q) = the
+      // table goes to the general path
+      uint32_t qmask = 0u, vmask = 0u;
 #pragma unroll
       for (int gi = 0; gi < kGpw; gi++) {
-        const int grp = wq + gi * kPerQuad;
 #pragma unroll
-        for (int q = 0; q < kPairsPerGroup; q++) do_pair(&r[gi][9 * q], grp, q);
+        for (int q = 0; q < kPairsPerGroup; q++) {
+          float oA[9], oB[9];
+          const int prior = tables(gi, q, oA, oB);
+          const float chiA = prior ? thr1 : thr0;
+          const int j = gi * kPairsPerGroup + q;
+          const int lp = (wq + gi * kPerQuad) * kPairsPerGroup + q;
+          qmask |= (quick_zero_f(oA, chiA) ? 0u : 1u) << (2 * j);
+          qmask |= (quick_zero_f(oB, chiA) ? 0u : 1u) << (2 * j + 1);
+          vmask |= (lp < lim ? 3u : 0u) << (2 * j);
+        }
+      }
+      if (u >= B) vmask = 0u;
+      qmask &= vmask;
+      ntab += (unsigned)__popc(vmask);
+      nfilt += (unsigned)__popc(vmask & ~qmask);
+      // pass 2 (rare): the flagged tables into the launch's queue, one atomic
+      // per warp: counts, class, prior, pair and unit
+      if (__any_sync(0xffffffffu, qmask != 0u)) {
+        const unsigned cnt = (unsigned)__popc(qmask);
+        unsigned incl = cnt;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+          const unsigned y = __shfl_up_sync(0xffffffffu, incl, o);
+          if (lane >= o) incl += y;
+        }
+        unsigned qbase = 0;
+        if (lane == 31) qbase = atomicAdd(gqueue, incl);
+        unsigned idx = __shfl_sync(0xffffffffu, qbase, 31) + incl - cnt;
+#pragma unroll
+        for (int gi = 0; gi < kGpw; gi++) {
+#pragma unroll
+          for (int q = 0; q < kPairsPerGroup; q++) {
+            const int j = gi * kPairsPerGroup + q;
+            if (((qmask >> (2 * j)) & 3u) == 0u) continue;
+            float oA[9], oB[9];
+            const int prior = tables(gi, q, oA, oB);
+            const int p = tn * kPairsPerTile + (wq + gi * kPerQuad) * kPairsPerGroup + q;
+#pragma unroll
+            for (int cls = 0; cls < 2; cls++) {
+              if (!((qmask >> (2 * j + cls)) & 1u)) continue;
+              const float *o = cls ? oB : oA;
+              if (idx < qcap) {
+                unsigned *it = qitems + (size_t)idx * kQWords;
+                it[0] = (uint32_t)o[0] | ((uint32_t)o[1] << 16);
+                it[1] = (uint32_t)o[2] | ((uint32_t)o[3] << 16);
+                it[2] = (uint32_t)o[4] | ((uint32_t)o[5] << 16);
+                it[3] = (uint32_t)o[6] | ((uint32_t)o[7] << 16);
+                it[4] = (uint32_t)o[8] | ((uint32_t)cls << 16) | ((uint32_t)prior << 17);
+                it[5] = (uint32_t)p | ((uint32_t)u << 17);  // pair < 2^17, unit < 2^15
+              } else {
+                atomicOr(err, 2u);
+              }
+              idx++;
+            }
+          }
+        }
       }
       // the slot (accumulator and table buffer) is free again
       tc_fence_before();
@@ -657,7 +687,7 @@ static cudaError_t launch_variant(const SetDev &sd, const uint8_t *Afp8, const u
   if (e != cudaSuccess) return e;
   const int ntot = nt * mblocks;
   const int grid = ntot < sms ? ntot : sms;
-  kern<<<grid, 32 * (2 + kEpi), smem, st>>>(ma, mb, sd, ctotf, B, np / kKC, nt, mblocks, dmask,
+  kern<<<grid, 32 * (2 + kEpi), smem, st>>>(ma, mb, sd, ctotf, B, np / kKC, nt, mblocks,
                                             stats, err, gqueue, qcap);
   e = cudaGetLastError();
   if (e != cudaSuccess) return e;

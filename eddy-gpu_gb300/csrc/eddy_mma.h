@@ -20,10 +20,11 @@ size_t mma_y_bytes(int c, int n);
 cudaError_t launch_build_y(const SetDev &sd, uint8_t *Y, cudaStream_t st);
 // Masks -> e4m3 operand (Afp8, mma_a_bytes(B, n, c) bytes), then the GEMM +
 // decision kernel and the general-path kernel for the tables its filter
-// could not settle.  *err: bit 0 = a bounded wait timed out, bit 1 = the
-// general-path queue overflowed (the batch must be decided another way).
-// variants (mma_variants()): tile widths N = 128 / 192 / 256 with 16, 8, 12
-// or 8 epilogue warps, one CTA per SM.
+// could not settle.  Only bits of dmask are set: its masks and chunk bitmap
+// must be zero when the launch starts.  *err: bit 0 = a bounded wait timed
+// out, bit 1 = the general-path queue overflowed (the batch must be decided
+// another way).  Variants (mma_variants()): tile widths N = 128 / 192 / 256
+// with 16, 8, 12 or 16 epilogue warps, one CTA per SM.
 int mma_variants();
 cudaError_t launch_pairs_mma(const SetDev &sd, const uint64_t *masks, int B, uint8_t *Afp8,
                              const uint8_t *Y, uint32_t *dmask, unsigned long long *stats,

@@ -162,23 +162,23 @@ extern "C" int eddy_unit_noalloc(const eddy_opts *opts, const int8_t *vals, int 
   sd.lg_stride = n + 1;
   sd.lg_shift = shift;
 
-  // the chunk bitmap after the c masks is zeroed before the decision kernel
-  if (cudaMemsetAsync(base + kOffDmask + 4 * (size_t)c, 0, 4 * (size_t)chunk_words(c), st) !=
-          cudaSuccess ||
-      launch_pairs(sd, (const uint64_t *)(base + kOffMask), (uint32_t *)(base + kOffDmask), 1,
-                   nullptr, st) != cudaSuccess)
-    return EDDY_ERR_CUDA;
   double *d_js = (double *)(base + kOffOut);
   int32_t *d_U = (int32_t *)(base + kOffOut + 8);
   uint32_t *d_status = (uint32_t *)(base + kOffOut + 12);
   uint64_t salt = 0x5EED5EEDull;
   for (int attempt = 0; attempt < 4; attempt++) {
     sd.salt = salt;
+    // decisions (the unit kernel zeroes the masks it reads, so every attempt
+    // decides again), from masks and a chunk bitmap that start at zero
+    if (cudaMemsetAsync(base + kOffDmask, 0, dmask_bytes(1, c), st) != cudaSuccess ||
+        launch_pairs(sd, (const uint64_t *)(base + kOffMask), (uint32_t *)(base + kOffDmask), 1,
+                     nullptr, st) != cudaSuccess)
+      return EDDY_ERR_CUDA;
     BatchDev bd{};
     bd.B = 1;
     bd.kmax = kNAKmax;
     bd.masks = (const uint64_t *)(base + kOffMask);
-    bd.dmask = (const uint32_t *)(base + kOffDmask);
+    bd.dmask = (uint32_t *)(base + kOffDmask);
     bd.scratch = base + kOffUnit;
     bd.unit_bytes = unit_scratch_bytes(c, S, kNAKmax);
     bd.js = d_js;
