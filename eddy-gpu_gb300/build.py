@@ -24,7 +24,7 @@ CLI = os.path.join(BINDIR, "eddy")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
                   "-Xcompiler", "-ffp-contract=off", "-I", os.path.join(ROOT, "include")]
-CU = ["eddy_kernels.cu", "eddy_mma.cu", "eddy_api.cu", "eddy_noalloc.cu", "eddy_beta.cu"]
+CU = ["eddy_kernels.cu", "eddy_mma.cu", "eddy_api.cu", "eddy_noalloc.cu"]
 CPP = ["eddy_host.cpp", "eddy_writers.cpp"]
 
 

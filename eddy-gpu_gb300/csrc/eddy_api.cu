@@ -120,9 +120,6 @@ struct eddy_ctx {
   // d_dmask is all zero between batches (decisions only set bits, the unit
   // kernel clears what it reads) while this equals d_dmask.p; null = unknown
   void *dmask_clean = nullptr;
-  // the JS values of an eddy_run call, every set's R in a row, for the
-  // beta fit on the device; positions of a batch's units in it; fit results
-  DevBuf d_jsall, d_jpos, d_fit;
   PinnedBuf h_stage;          // per-batch indices and results
   PinnedBuf h_vals;           // the resident set's values on their way in
   int sms = 148;
@@ -400,10 +397,8 @@ int check_mma_error(eddy_ctx *ctx) {
 
 // Runs units of one set.  masks_host: B x W host masks, or null to
 // generate counter-mode masks for perms[] on the device.
-// js_dev >= 0: unit i's JS also goes to d_jsall[js_dev + i].
 int run_units(eddy_ctx *ctx, SetRun &sr, int nunits, const uint64_t *masks_host,
-              const int32_t *perms, double *js, int32_t *U, KeepOut *keep, int mpk_req,
-              long long js_dev = -1) {
+              const int32_t *perms, double *js, int32_t *U, KeepOut *keep, int mpk_req) {
   SetDev &sd = sr.sd;
   const int W = sd.W, c = sd.c, S = sd.S, g = sd.g;
   const bool keeping = keep != nullptr;
@@ -480,13 +475,6 @@ int run_units(eddy_ctx *ctx, SetRun &sr, int nunits, const uint64_t *masks_host,
       }
       // the kept unit (the first of the call) writes its detailed outputs;
       // slot -1 (every byte 0xFF) for the others
-      if (js_dev >= 0) {
-        // (staging: after the set ids and permutation indices)
-        int32_t *hq = ctx->h_stage.as<int32_t>() + 2 * (size_t)Bt;
-        for (int i = 0; i < Bt; i++) hq[i] = (int32_t)(js_dev + b0 + todo[i]);
-        CK(ctx->d_jpos.ensure(sizeof(int32_t) * Bt));
-        CK(cudaMemcpyAsync(ctx->d_jpos.p, hq, 4 * (size_t)Bt, cudaMemcpyHostToDevice, ctx->stream));
-      }
       int i0 = -1;
       for (int i = 0; i < Bt && keeping; i++)
         if (b0 + todo[i] == 0) i0 = i;
@@ -500,8 +488,6 @@ int run_units(eddy_ctx *ctx, SetRun &sr, int nunits, const uint64_t *masks_host,
       bd.scratch = ctx->d_scratch.as<uint8_t>();
       bd.unit_bytes = ub;
       bd.js = ctx->d_js.as<double>();
-      bd.js_all = js_dev >= 0 ? ctx->d_jsall.as<double>() : nullptr;
-      bd.js_pos = js_dev >= 0 ? ctx->d_jpos.as<int32_t>() : nullptr;
       bd.U = ctx->d_U.as<int32_t>();
       bd.status = ctx->d_status.as<uint32_t>();
       bd.keep_slot = ctx->d_keep.as<int32_t>();
@@ -554,8 +540,7 @@ int run_units(eddy_ctx *ctx, SetRun &sr, int nunits, const uint64_t *masks_host,
             (uintptr_t)ctx->d_js.p, (uintptr_t)ctx->d_U.p, (uintptr_t)ctx->d_status.p,
             (uintptr_t)ctx->d_keep.p, (uintptr_t)ctx->d_uset.p, (uintptr_t)ctx->d_uperm.p,
             (uintptr_t)ctx->d_stats.p, (uintptr_t)ctx->d_afp8.p, (uintptr_t)ctx->d_Y.p,
-            (uintptr_t)ctx->d_err.p, (uintptr_t)ctx->d_mask0.p, (uintptr_t)ctx->stream,
-            (uintptr_t)bd.js_all, (uintptr_t)bd.js_pos};
+            (uintptr_t)ctx->d_err.p, (uintptr_t)ctx->d_mask0.p, (uintptr_t)ctx->stream};
         if (key != ctx->graph_key || !ctx->graph_exec) {
           if (ctx->graph_exec) {
             cudaGraphExecDestroy(ctx->graph_exec);
@@ -852,8 +837,7 @@ static int set_iterations(const eddy_ctx *ctx, const SetHost &S) {
   return ctx->o.rng == EDDY_RNG_EXTERNAL ? std::max(S.R_ext, 0) : ctx->o.permutations;
 }
 
-// Runs one set; its JS values also go to d_jsall[js_off ..] for the fit.
-static int run_set(eddy_ctx *ctx, int set_id, long long js_off) {
+static int run_set(eddy_ctx *ctx, int set_id) {
   SetHost &S = ctx->sets[set_id];
   const int n = ctx->samples, W = ctx->W;
   const int g = (int)S.genes.size();
@@ -892,7 +876,7 @@ static int run_set(eddy_ctx *ctx, int set_id, long long js_off) {
     for (int i = 0; i < R; i++) perms[i] = i;
     KeepOut K;
     rc = run_units(ctx, sr, R, nullptr, perms.data(), S.js.data(), S.U.data(),
-                   ctx->o.keep_networks ? &K : nullptr, mpk0, js_off);
+                   ctx->o.keep_networks ? &K : nullptr, mpk0);
     if (rc) return rc;
     if (ctx->o.keep_networks) store_keep(ctx, S, K, g);
     else S.U0 = S.U[0];
@@ -917,7 +901,7 @@ static int run_set(eddy_ctx *ctx, int set_id, long long js_off) {
     labels_to_mask(lab.data(), n, W, masks.data());
     KeepOut K;
     rc = run_units(ctx, sr, 1, masks.data(), nullptr, S.js.data(), S.U.data(),
-                   ctx->o.keep_networks ? &K : nullptr, mpk0, js_off);
+                   ctx->o.keep_networks ? &K : nullptr, mpk0);
     if (rc) return rc;
     if (ctx->o.keep_networks) store_keep(ctx, S, K, g);
     else S.U0 = S.U[0];
@@ -951,7 +935,7 @@ static int run_set(eddy_ctx *ctx, int set_id, long long js_off) {
         }
       }
       rc = run_units(ctx, sr, nu, device_counter ? nullptr : mh.data(), perms.data(), S.js.data() + 1,
-                     S.U.data() + 1, nullptr, 1, js_off + 1);
+                     S.U.data() + 1, nullptr, 1);
       if (rc) return rc;
     }
     S.iterations = R;
@@ -962,43 +946,11 @@ static int run_set(eddy_ctx *ctx, int set_id, long long js_off) {
   S.tables += st[1];
   for (int i = 0; i < R; i++)
     if (!finite_js(S.js[i])) S.failed = 1;
-  S.done = true;  // the beta fit follows in eddy_run, on the device
-  return EDDY_OK;
-}
-
-// Beta fit and pDDN (main.cu:1488-1502) of the sets of one eddy_run call
-// whose JS values are all finite (main.cu:1465-1479), in one launch over
-// d_jsall; offsets and counts in and four doubles per set out through the
-// pinned staging.
-static int fit_sets(eddy_ctx *ctx, const std::vector<int> &run, const std::vector<long long> &off) {
-  std::vector<int> fit;
-  for (size_t k = 0; k < run.size(); k++)
-    if (!ctx->sets[run[k]].failed) fit.push_back((int)k);
-  const size_t m = fit.size();
-  if (m == 0) return EDDY_OK;
-  CK(ctx->h_stage.ensure(48 * m + 64));
-  CK(ctx->d_fit.ensure(48 * m));
-  long long *ho = ctx->h_stage.as<long long>();
-  int32_t *hr = ctx->h_stage.as<int32_t>(8 * m);
-  double *hout = ctx->h_stage.as<double>(16 * m);
-  for (size_t i = 0; i < m; i++) {
-    ho[i] = off[fit[i]];
-    hr[i] = ctx->sets[run[fit[i]]].iterations;
-  }
-  char *d = ctx->d_fit.as<char>();
-  CK(cudaMemcpyAsync(d, ho, 12 * m, cudaMemcpyHostToDevice, ctx->stream));
-  CK(launch_beta_fit(ctx->d_jsall.as<double>(), (const long long *)d, (const int *)(d + 8 * m),
-                     (int)m, (double *)(d + 16 * m), ctx->stream));
-  ctx->launches++;
-  CK(cudaMemcpyAsync(hout, d + 16 * m, 32 * m, cudaMemcpyDeviceToHost, ctx->stream));
-  CK(cudaStreamSynchronize(ctx->stream));
-  for (size_t i = 0; i < m; i++) {
-    SetHost &S = ctx->sets[run[fit[i]]];
-    S.alpha = hout[4 * i];
-    S.beta = hout[4 * i + 1];
-    S.pddn = hout[4 * i + 2];
-    S.betafit_ok = hout[4 * i + 3] != 0.0 ? 1 : 0;
-  }
+  // beta fit on the host: the sequential FP64 moment loop and the continued
+  // fraction are chains of dependent FP64 operations, which run faster on
+  // the host cores than on the GPU
+  if (!S.failed) S.betafit_ok = beta_pddn(S.js.data(), R, S.alpha, S.beta, S.pddn) ? 1 : 0;
+  S.done = true;
   return EDDY_OK;
 }
 
@@ -1007,23 +959,12 @@ int eddy_run(eddy_ctx *ctx) {
   if (ctx->samples == 0) return fail(ctx, EDDY_ERR_STATE, "no matrix loaded");
   ctx->ms_total = ctx->ms_pairs = ctx->ms_units = 0;
   ctx->launches = 0;
-  // the JS values of every pending set in one device array (R per set)
-  std::vector<int> run;
-  std::vector<long long> off;
-  long long total = 0;
   for (int s = 0; s < (int)ctx->sets.size(); s++) {
     if (ctx->sets[s].done) continue;
-    run.push_back(s);
-    off.push_back(total);
-    total += std::max(1, set_iterations(ctx, ctx->sets[s]));
-  }
-  if (total > INT32_MAX) return fail(ctx, EDDY_ERR_CAPACITY, "over 2^31 iterations in one run");
-  if (total > 0) CK(ctx->d_jsall.ensure(sizeof(double) * (size_t)total));
-  for (size_t k = 0; k < run.size(); k++) {
-    int rc = run_set(ctx, run[k], off[k]);
+    int rc = run_set(ctx, s);
     if (rc) return rc;
   }
-  return fit_sets(ctx, run, off);
+  return EDDY_OK;
 }
 
 int eddy_get_set_summary(const eddy_ctx *ctx, int set_id, eddy_set_summary *out) {

@@ -297,6 +297,87 @@ __device__ __forceinline__ bool quick_zero_f(const float *o, float chiA) {
   return fmaf(lhs, 1.0001f, 1e-3f * q * D) < chiA * q * D;
 }
 
+// Packed FP32 pairs (add/sub/mul/fma .rn.f32x2, sm_100 and later): two
+// lanes per instruction.  quick_zero_f2 runs the bound of quick_zero_f on
+// both classes of a pair at once, lane x = class 1, lane y = class 2.
+typedef unsigned long long f32x2;
+__device__ __forceinline__ f32x2 f2_pack(float x, float y) {
+  f32x2 r;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(x), "f"(y));
+  return r;
+}
+__device__ __forceinline__ float f2_x(f32x2 v) {
+  float x, y;
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(x), "=f"(y) : "l"(v));
+  return x;
+}
+__device__ __forceinline__ float f2_y(f32x2 v) {
+  float x, y;
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(x), "=f"(y) : "l"(v));
+  return y;
+}
+__device__ __forceinline__ f32x2 f2_add(f32x2 a, f32x2 b) {
+  f32x2 d;
+  asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+  return d;
+}
+__device__ __forceinline__ f32x2 f2_sub(f32x2 a, f32x2 b) {
+  f32x2 d;
+  asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+  return d;
+}
+__device__ __forceinline__ f32x2 f2_mul(f32x2 a, f32x2 b) {
+  f32x2 d;
+  asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+  return d;
+}
+__device__ __forceinline__ f32x2 f2_fma(f32x2 a, f32x2 b, f32x2 c) {
+  f32x2 d;
+  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+  return d;
+}
+// o[k] = {class-1 count, class-2 count} of cell k (exact FP32 integers);
+// chiA as in quick_zero_f.  Bit 0 / bit 1 of the result: class 1 / class 2
+// settled (no edge in any of its ten tables).  Same formula and margins as
+// quick_zero_f, evaluated lane-wise.
+__device__ __forceinline__ unsigned quick_zero_f2(const f32x2 *o, float chiA) {
+  const f32x2 one = f2_pack(1.f, 1.f);
+  const f32x2 R0 = f2_add(f2_add(o[0], o[1]), o[2]), R1 = f2_add(f2_add(o[3], o[4]), o[5]),
+              R2 = f2_add(f2_add(o[6], o[7]), o[8]);
+  const f32x2 C0 = f2_add(f2_add(o[0], o[3]), o[6]), C1 = f2_add(f2_add(o[1], o[4]), o[7]),
+              C2 = f2_add(f2_add(o[2], o[5]), o[8]);
+  const f32x2 N = f2_add(f2_add(R0, R1), R2);
+  const float rmx = fminf(f2_x(R0), fminf(f2_x(R1), f2_x(R2)));
+  const float rmy = fminf(f2_y(R0), fminf(f2_y(R1), f2_y(R2)));
+  const float cmx = fminf(f2_x(C0), fminf(f2_x(C1), f2_x(C2)));
+  const float cmy = fminf(f2_y(C0), fminf(f2_y(C1), f2_y(C2)));
+  const f32x2 rm = f2_pack(rmx, rmy), cm = f2_pack(cmx, cmy);
+  const f32x2 q = f2_mul(f2_sub(rm, one), f2_sub(cm, one)), rc = f2_mul(rm, cm);
+  const float Nx = f2_x(N), Ny = f2_y(N);
+  const bool okx = rmx >= 2.f && cmx >= 2.f && Nx >= 32.f && Nx <= 4096.f &&
+                   f2_x(q) >= 5.f * (Nx - 1.f) && f2_x(rc) >= 5.f * Nx;
+  const bool oky = rmy >= 2.f && cmy >= 2.f && Ny >= 32.f && Ny <= 4096.f &&
+                   f2_y(q) >= 5.f * (Ny - 1.f) && f2_y(rc) >= 5.f * Ny;
+  const f32x2 PR0 = f2_mul(R1, R2), PR1 = f2_mul(R0, R2), PR2 = f2_mul(R0, R1);
+  const f32x2 PC0 = f2_mul(C1, C2), PC1 = f2_mul(C0, C2), PC2 = f2_mul(C0, C1);
+  const f32x2 D = f2_mul(f2_mul(R0, PR0), f2_mul(C0, PC0));
+  const f32x2 s0 = f2_fma(f2_mul(o[0], o[0]), PC0,
+                          f2_fma(f2_mul(o[1], o[1]), PC1, f2_mul(f2_mul(o[2], o[2]), PC2)));
+  const f32x2 s1 = f2_fma(f2_mul(o[3], o[3]), PC0,
+                          f2_fma(f2_mul(o[4], o[4]), PC1, f2_mul(f2_mul(o[5], o[5]), PC2)));
+  const f32x2 s2 = f2_fma(f2_mul(o[6], o[6]), PC0,
+                          f2_fma(f2_mul(o[7], o[7]), PC1, f2_mul(f2_mul(o[8], o[8]), PC2)));
+  const f32x2 QD = f2_fma(PR0, s0, f2_fma(PR1, s1, f2_mul(PR2, s2)));
+  // q D bound = (N (rm + cm - 1) + rc (N (Q - 1) + 1e-5 N)) D
+  const f32x2 rcN = f2_mul(rc, N);
+  const f32x2 t1 = f2_fma(N, f2_sub(f2_add(rm, cm), one), f2_mul(rcN, f2_pack(1e-5f, 1e-5f)));
+  const f32x2 lhs = f2_fma(t1, D, f2_mul(rcN, f2_sub(QD, D)));
+  const f32x2 qD = f2_mul(q, D);
+  const f32x2 L = f2_fma(lhs, f2_pack(1.0001f, 1.0001f), f2_mul(f2_pack(1e-3f, 1e-3f), qD));
+  const f32x2 Rr = f2_mul(f2_pack(chiA, chiA), qD);
+  return ((okx && f2_x(L) < f2_x(Rr)) ? 1u : 0u) | ((oky && f2_y(L) < f2_y(Rr)) ? 2u : 0u);
+}
+
 // The general path: full-table decision, the Minkowski leave-one-out filter
 // and, when that cannot settle them, the nine cell-removed tables one by one.
 // Counts by value and not inlined: it runs for a small share of the tables.

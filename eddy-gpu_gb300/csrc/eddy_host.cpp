@@ -166,6 +166,65 @@ void counter_labels(uint64_t seed, int set_id, int perm, int n, int n_class1, ui
   for (int k = 0; k < n; k++) labels[kv[k].second] = (uint8_t)(k < n_class1 ? 0 : 1);
 }
 
+// ------------------------------------------------------------ incomplete beta
+// Continued fraction of I_x(a,b) (DLMF 8.17.22):
+//   I_x(a,b) = x^a (1-x)^b / (a B(a,b)) * 1/(1 + d1/(1 + d2/(1 + ...)))
+//   d_{2m+1} = -(a+m)(a+b+m)x / ((a+2m)(a+2m+1)),
+//   d_{2m}   =  m(b-m)x / ((a+2m-1)(a+2m)),
+// evaluated with the modified Lentz method (Lentz 1976; Thompson & Barnett
+// 1986).  Returns 1/(1 + d1/(1 + ...)).
+static double beta_cf(double a, double b, double x) {
+  const double tiny = 1e-300;
+  double f = 1.0, C = 1.0, D = 0.0;
+  for (int j = 1; j <= 400000; j++) {
+    const int m = j / 2;
+    const double dj = (j & 1) ? -((a + m) * (a + b + m) * x) / ((a + 2.0 * m) * (a + 2.0 * m + 1.0))
+                              : (m * (b - m) * x) / ((a + 2.0 * m - 1.0) * (a + 2.0 * m));
+    D = 1.0 + dj * D;
+    if (fabs(D) < tiny) D = tiny;
+    D = 1.0 / D;
+    C = 1.0 + dj / C;
+    if (fabs(C) < tiny) C = tiny;
+    const double delta = C * D;
+    f *= delta;
+    if (fabs(delta - 1.0) < 1e-15) break;
+  }
+  return 1.0 / f;
+}
+
+static double ibeta_lower_cf(double a, double b, double x) {
+  const double lfront = a * log(x) + b * log1p(-x) - (lgamma(a) + lgamma(b) - lgamma(a + b));
+  return exp(lfront) / a * beta_cf(a, b, x);
+}
+
+double ibetac(double a, double b, double x) {
+  if (!(a > 0) || !(b > 0) || !std::isfinite(a) || !std::isfinite(b) || !(x >= 0) || !(x <= 1))
+    return NAN;
+  if (x == 0) return 1.0;
+  if (x == 1) return 0.0;
+  if (x < (a + 1.0) / (a + b + 2.0)) return 1.0 - ibeta_lower_cf(a, b, x);
+  return ibeta_lower_cf(b, a, 1.0 - x);
+}
+
+// routines.cu:494-508 and main.cu:1491-1497
+bool beta_pddn(const double *js, int R, double &alpha, double &beta, double &pddn) {
+  double sum = 0.0;
+  for (int i = 0; i < R; i++) sum += js[i];
+  const double mu = sum / R;
+  double v = 0.0;
+  for (int i = 0; i < R; i++) v += pow(js[i] - mu, 2);
+  const double var = v / R;
+  alpha = (((1 - mu) / var) - (1 / mu)) * pow(mu, 2);
+  beta = alpha * (1 / mu - 1);
+  if (!(alpha > 0) || !(beta > 0) || !std::isfinite(alpha) || !std::isfinite(beta) ||
+      !(js[0] >= 0) || !(js[0] <= 1)) {
+    pddn = NAN;
+    return false;
+  }
+  pddn = ibetac(alpha, beta, js[0]);
+  return true;
+}
+
 // ------------------------------------------------------------ BDeu table
 void bdeu_table_into(int n, int64_t *lg, int &shift, int8_t dmap[82]) {
   static const int D[kDivisors] = {1, 2, 3, 4, 6, 8, 9, 12, 16, 18, 24, 27, 36, 54, 81};

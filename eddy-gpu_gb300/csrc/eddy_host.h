@@ -1,6 +1,6 @@
 // eddy_host.h -- host-side numerics of libeddy_gpu shared by the C ABI and
 // the eddy CLI: decision thresholds, the glibc-compatible label stream,
-// the counter label stream and the fixed-point BDeu table.
+// the counter label stream, incomplete beta and the beta fit.
 #pragma once
 #include <stdint.h>
 
@@ -46,6 +46,13 @@ void glibc_permutation(GlibcRand &rng, int n, int n_class1, bool relabel, uint8_
 
 // Counter labelling (Philox-4x32-10), same definition as the GPU kernel.
 void counter_labels(uint64_t seed, int set_id, int perm, int n, int n_class1, uint8_t *labels);
+
+// 1 - I_x(a, b) (regularised incomplete beta complement).
+double ibetac(double a, double b, double x);
+
+// Beta fit of js[0..R) by moments and pDDN = ibetac(alpha, beta, js[0]).
+// Returns false when alpha or beta is not positive finite.
+bool beta_pddn(const double *js, int R, double &alpha, double &beta, double &pddn);
 
 // Fixed-point BDeu table lg[d][m] = (lgamma(m + 4/d) - lgamma(4/d)) * 2^shift.
 void bdeu_table(int n, std::vector<int64_t> &lg, int &shift, int8_t dmap[82]);

@@ -84,8 +84,6 @@ struct BatchDev {
   uint8_t *scratch;            // per-unit scratch, unit_bytes each
   size_t unit_bytes;
   double *js;                  // [B]
-  double *js_all;              // null, or the run's JS array, where unit u's
-  const int32_t *js_pos;       //   JS also goes, at index js_pos[u]
   int32_t *U;                  // [B]
   uint32_t *status;            // [B]
   int32_t *keep_slot;          // [B] -1 or slot of detailed output

@@ -1319,7 +1319,6 @@ __global__ void __launch_bounds__(256) k_js(const __grid_constant__ SetDev sd,
     double js = ls / log(2.0);
     if (h0 == l0 || h1 == l1) js = __longlong_as_double(0x7ff8000000000000ll);
     bd.js[u] = js;
-    if (bd.js_all) bd.js_all[bd.js_pos[u]] = js;
   }
 }
 

@@ -18,8 +18,4 @@ cudaError_t launch_pairs(const SetDev &sd, const uint64_t *masks, uint32_t *dmas
                          unsigned long long *stats, cudaStream_t st);
 cudaError_t launch_units(const SetDev &sd, const BatchDev &bd, cudaStream_t st);
 cudaError_t set_divisor_map(const int8_t *map82);
-// Beta fit and pDDN of nsets sets: set i's R[i] JS values start at
-// js_all[off[i]]; out[4 i ..] = alpha, beta, pDDN, 1 (valid fit) or 0.
-cudaError_t launch_beta_fit(const double *js_all, const long long *off, const int *R, int nsets,
-                            double *out, cudaStream_t st);
 }  // namespace eddy

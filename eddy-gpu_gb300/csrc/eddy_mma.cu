@@ -212,7 +212,6 @@ __global__ void __maxnreg__(max_regs<kEpi>())
   constexpr uint32_t kIdesc = idesc_for(kTN);
   constexpr int kPerQuad = kEpi / 4, kGpw = kGroups / kPerQuad;
   static_assert(kEpi % 4 == 0 && kGroups % kPerQuad == 0 && kGroups <= kMaxGroups, "shape");
-  static_assert(2 * kGpw * kPairsPerGroup <= 32, "one bit per table of a thread");
   extern __shared__ __align__(1024) uint8_t smraw[];
   // 1024-byte aligned stage ring, then barriers, then the epilogue buffer
   uint8_t *base = (uint8_t *)(((uintptr_t)smraw + 1023) & ~(uintptr_t)1023);
@@ -346,83 +345,72 @@ __global__ void __maxnreg__(max_regs<kEpi>())
       const int u = mb * kTM + row;
       // pairs of the tile below c (the last tile's tail is padding)
       const int lim = sd.c - tn * kPairsPerTile;
-      // the warp's column groups out of TMEM, every load issued before one
-      // wait; pair q of a group = columns 9q .. 9q+8
-      uint32_t r[kGpw][32];
-#pragma unroll
+      // the warp's column groups, one at a time out of TMEM (pair q of a
+      // group = columns 9q .. 9q+8)
+#pragma unroll 1
       for (int gi = 0; gi < kGpw; gi++) {
         const int grp = wq + gi * kPerQuad;
-        tmem_ld32(tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)(acc * kTN + grp * 32), r[gi]);
-      }
-      tmem_ld_wait();
-      // one pair's class-1 counts (FP32 integers from TMEM) and class-2
-      // counts (full-sample table - class 1), and its prior flag
-      auto tables = [&](int gi, int q, float *oA, float *oB) -> int {
-        const int lp = (wq + gi * kPerQuad) * kPairsPerGroup + q;
-        const float4 *cf = reinterpret_cast<const float4 *>(ctile + lp * 12);
-        const float4 f0 = cf[0], f1 = cf[1], f2 = cf[2];
-#pragma unroll
-        for (int k = 0; k < 9; k++) oA[k] = __uint_as_float(r[gi][9 * q + k]);
-        oB[0] = f0.x - oA[0]; oB[1] = f0.y - oA[1]; oB[2] = f0.z - oA[2];
-        oB[3] = f0.w - oA[3]; oB[4] = f1.x - oA[4]; oB[5] = f1.y - oA[5];
-        oB[6] = f1.z - oA[6]; oB[7] = f1.w - oA[7]; oB[8] = f2.x - oA[8];
-        return (f2.y != 0.f) ? 1 : 0;
-      };
-      // pass 1: the all-zero bound of every table of the thread, straight
-      // line; bit 2 j + class of qmask (j = pair slot gi * 3 + q) = the
-      // table goes to the general path
-      uint32_t qmask = 0u, vmask = 0u;
-#pragma unroll
-      for (int gi = 0; gi < kGpw; gi++) {
+        uint32_t r[32];
+        tmem_ld32(tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)(acc * kTN + grp * 32), r);
+        tmem_ld_wait();
+        // pass 1: the all-zero bound of the group's six tables, both classes
+        // of a pair in the two lanes of packed FP32 pairs; bit 2 q + class of
+        // qmask = the table goes to the general path
+        uint32_t qmask = 0u, vmask = 0u;
 #pragma unroll
         for (int q = 0; q < kPairsPerGroup; q++) {
-          float oA[9], oB[9];
-          const int prior = tables(gi, q, oA, oB);
-          const float chiA = prior ? thr1 : thr0;
-          const int j = gi * kPairsPerGroup + q;
-          const int lp = (wq + gi * kPerQuad) * kPairsPerGroup + q;
-          qmask |= (quick_zero_f(oA, chiA) ? 0u : 1u) << (2 * j);
-          qmask |= (quick_zero_f(oB, chiA) ? 0u : 1u) << (2 * j + 1);
-          vmask |= (lp < lim ? 3u : 0u) << (2 * j);
-        }
-      }
-      if (u >= B) vmask = 0u;
-      qmask &= vmask;
-      ntab += (unsigned)__popc(vmask);
-      nfilt += (unsigned)__popc(vmask & ~qmask);
-      // pass 2 (rare): the flagged tables into the launch's queue, one atomic
-      // per warp: counts, class, prior, pair and unit
-      if (__any_sync(0xffffffffu, qmask != 0u)) {
-        const unsigned cnt = (unsigned)__popc(qmask);
-        unsigned incl = cnt;
+          const int lp = grp * kPairsPerGroup + q;
+          const float *f = ctile + lp * 12;
+          f32x2 o2[9];
 #pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-          const unsigned y = __shfl_up_sync(0xffffffffu, incl, o);
-          if (lane >= o) incl += y;
+          for (int k = 0; k < 9; k++) {
+            const float a = __uint_as_float(r[9 * q + k]);
+            o2[k] = f2_pack(a, f[k] - a);
+          }
+          const float chiA = (f[9] != 0.f) ? thr1 : thr0;
+          qmask |= (~quick_zero_f2(o2, chiA) & 3u) << (2 * q);
+          vmask |= (lp < lim ? 3u : 0u) << (2 * q);
         }
-        unsigned qbase = 0;
-        if (lane == 31) qbase = atomicAdd(gqueue, incl);
-        unsigned idx = __shfl_sync(0xffffffffu, qbase, 31) + incl - cnt;
+        if (u >= B) vmask = 0u;
+        qmask &= vmask;
+        ntab += (unsigned)__popc(vmask);
+        nfilt += (unsigned)__popc(vmask & ~qmask);
+        // pass 2 (rare): the flagged tables into the launch's queue, one
+        // atomic per warp: counts, class, prior, pair and unit
+        if (__any_sync(0xffffffffu, qmask != 0u)) {
+          const unsigned cnt = (unsigned)__popc(qmask);
+          unsigned incl = cnt;
 #pragma unroll
-        for (int gi = 0; gi < kGpw; gi++) {
+          for (int o = 1; o < 32; o <<= 1) {
+            const unsigned y = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += y;
+          }
+          unsigned qbase = 0;
+          if (lane == 31) qbase = atomicAdd(gqueue, incl);
+          unsigned idx = __shfl_sync(0xffffffffu, qbase, 31) + incl - cnt;
 #pragma unroll
           for (int q = 0; q < kPairsPerGroup; q++) {
-            const int j = gi * kPairsPerGroup + q;
-            if (((qmask >> (2 * j)) & 3u) == 0u) continue;
-            float oA[9], oB[9];
-            const int prior = tables(gi, q, oA, oB);
-            const int p = tn * kPairsPerTile + (wq + gi * kPerQuad) * kPairsPerGroup + q;
+            if (((qmask >> (2 * q)) & 3u) == 0u) continue;
+            const int lp = grp * kPairsPerGroup + q;
+            const float *f = ctile + lp * 12;
+            const int prior = (f[9] != 0.f) ? 1 : 0;
+            const int p = tn * kPairsPerTile + lp;
 #pragma unroll
             for (int cls = 0; cls < 2; cls++) {
-              if (!((qmask >> (2 * j + cls)) & 1u)) continue;
-              const float *o = cls ? oB : oA;
+              if (!((qmask >> (2 * q + cls)) & 1u)) continue;
+              uint32_t o[9];
+#pragma unroll
+              for (int k = 0; k < 9; k++) {
+                const float a = __uint_as_float(r[9 * q + k]);
+                o[k] = (uint32_t)(cls ? f[k] - a : a);
+              }
               if (idx < qcap) {
                 unsigned *it = qitems + (size_t)idx * kQWords;
-                it[0] = (uint32_t)o[0] | ((uint32_t)o[1] << 16);
-                it[1] = (uint32_t)o[2] | ((uint32_t)o[3] << 16);
-                it[2] = (uint32_t)o[4] | ((uint32_t)o[5] << 16);
-                it[3] = (uint32_t)o[6] | ((uint32_t)o[7] << 16);
-                it[4] = (uint32_t)o[8] | ((uint32_t)cls << 16) | ((uint32_t)prior << 17);
+                it[0] = o[0] | (o[1] << 16);
+                it[1] = o[2] | (o[3] << 16);
+                it[2] = o[4] | (o[5] << 16);
+                it[3] = o[6] | (o[7] << 16);
+                it[4] = o[8] | ((uint32_t)cls << 16) | ((uint32_t)prior << 17);
                 it[5] = (uint32_t)p | ((uint32_t)u << 17);  // pair < 2^17, unit < 2^15
               } else {
                 atomicOr(err, 2u);

@@ -1,10 +1,10 @@
-"""The beta fit and pDDN on the device (main.cu:1488-1502, routines.cu:
-494-508): every set of one eddy_run call is fitted in one launch, from the
-JS values the device kept.  alpha and beta must equal, bit for bit, the
-reference's sequential moment loop run here in Python on the same JS
-values; pDDN agrees with the oracle's continued fraction (and scipy's
-betaincc) to 1e-10 relative.  A set whose JS is NaN (no fit) between
-fitted sets leaves the others' offsets intact."""
+"""The beta fit and pDDN of every set of one eddy_run call (main.cu:
+1488-1502, routines.cu:494-508), from the JS values the GPU computed.
+alpha and beta must equal, bit for bit, the reference's sequential moment
+loop run here in Python on the same JS values; pDDN agrees with the
+oracle's continued fraction (and scipy's betaincc) to 1e-10 relative.  A
+set whose JS is NaN (no fit) between fitted sets leaves the others intact,
+and sets added after an earlier run are fitted in their own run."""
 import numpy as np
 import pytest
 
