@@ -215,7 +215,7 @@ int prepare_set(eddy_ctx *ctx, int set_id, SetRun &sr) {
     ctx->prepared_set = -1;
     CK(ctx->d_vals.ensure((size_t)g * n + 16));
     CK(ctx->d_valsT.ensure((size_t)g * n + 16));
-    CK(ctx->d_planes.ensure(sizeof(uint64_t) * (size_t)g * 3 * W));
+    CK(ctx->d_planes.ensure(2 * sizeof(uint64_t) * (size_t)g * 3 * W));  // planes, word-major copy
     CK(ctx->d_valid.ensure(sizeof(uint64_t) * W));
     CK(ctx->d_ctot.ensure(sizeof(uint16_t) * 9 * (size_t)(c > 0 ? c : 1)));
     CK(ctx->d_prior.ensure(pbits.size()));
@@ -261,6 +261,7 @@ int prepare_set(eddy_ctx *ctx, int set_id, SetRun &sr) {
     if (dm && strcmp(dm, "fp64") == 0) sd.exact_all = 1;
   }
   sd.planes = ctx->d_planes.as<uint64_t>();
+  sd.planesT = sd.planes + (size_t)g * 3 * sd.W;
   sd.valid = ctx->d_valid.as<uint64_t>();
   sd.vals = ctx->d_vals.as<int8_t>();
   sd.valsT = ctx->d_valsT.as<int8_t>();

@@ -40,6 +40,7 @@ struct SetDev {
   double alpha_edge, alpha_edge_prior;
   Thr thr[2][kDofSlots];  // [0] = no prior (alpha_edge), [1] = prior pairs
   const uint64_t *planes; // [g][3][W]  bit s of plane (i, a) = (x_i(s) == a-1)
+  const uint64_t *planesT; // [W][g][3] the same planes word-major (follows planes)
   const uint64_t *valid;  // [W] all-sample mask
   const int8_t *vals;     // [g][n]  -1/0/1, 2 = any other value
   const int8_t *valsT;    // [n][g]  the same, sample-major

@@ -47,6 +47,11 @@ __global__ void k_planes(const int8_t *vals, int g, int n, int W, uint64_t *plan
   planes[((size_t)i * 3 + 0) * W + w] = b0;
   planes[((size_t)i * 3 + 1) * W + w] = b1;
   planes[((size_t)i * 3 + 2) * W + w] = b2;
+  // the word-major copy after the planes: [W][g][3]
+  uint64_t *planesT = planes + (size_t)g * 3 * W + (size_t)w * g * 3 + (size_t)i * 3;
+  planesT[0] = b0;
+  planesT[1] = b1;
+  planesT[2] = b2;
   if (i == 0) valid[w] = v;
 }
 
@@ -529,12 +534,15 @@ __global__ void __launch_bounds__(256, 3) k_units(const __grid_constant__ SetDev
   for (int i = tid; i < 4 * g; i += nt) P.phs[i] = (i < 2 * g) ? 0x7fffffff : 0;
   for (int i = tid; i < 82; i += nt) P.dmap[i] = c_dmap[i];
   __syncthreads();
+  // state counts per class from the word-major planes: a warp's loads of a
+  // word are 32 consecutive planes
   for (int i = tid; i < g * 3; i += nt) {
-    const uint64_t *pl = sd.planes + (size_t)i * W;
+    const uint64_t *pl = sd.planesT + i;
     int a = 0, b = 0;
     for (int w = 0; w < W; w++) {
-      a += __popcll(pl[w] & P.mA[w]);
-      b += __popcll(pl[w] & P.mB[w]);
+      const uint64_t x = pl[(size_t)w * 3 * g];
+      a += __popcll(x & P.mA[w]);
+      b += __popcll(x & P.mB[w]);
     }
     P.cnt3[i] = (uint16_t)a;
     P.cnt3[3 * g + i] = (uint16_t)b;
@@ -757,6 +765,78 @@ __global__ void __launch_bounds__(256, 3) k_units(const __grid_constant__ SetDev
     }
     return any ? (key | 1ull) : 0ull;
   };
+  // The same from the trigger bitsets: entry o of class k fires for sample
+  // sigma when bit sigma of trig[(koff + o) W ..] is set.  Until the BDeu
+  // phase, the task prefix (tq) holds the entries by ordinal and the base
+  // score array (fsc) the bitsets.
+  uint32_t *ent = (uint32_t *)P.tq;
+  uint64_t *trig = (uint64_t *)P.fsc;
+  auto signature_t = [&](int k, int sigma, unsigned long long &bits) -> unsigned long long {
+    const int ne = SM.nent[k];
+    const bool exact = ne <= 64;
+    const unsigned long long ks = k ? ksalt1 : ksalt0;
+    const uint64_t *T = trig + (size_t)(k ? SM.nent[0] : 0) * W + (sigma >> 6);
+    const int sh = sigma & 63;
+    unsigned long long key = 0;
+    bits = 0;
+    int any = 0;
+    for (int o = 0; o < ne; o++) {
+      if ((T[(size_t)o * W] >> sh) & 1ull) {
+        key += mix64(ks + (unsigned long long)o);
+        if (exact) bits |= 1ull << o;
+        any = 1;
+      }
+    }
+    return any ? (key | 1ull) : 0ull;
+  };
+  // Trigger bitsets, when they fit: entries by ordinal (rows in order, then
+  // entries in position order, as signature() counts them), then per entry
+  // and sample word the OR over the set bits (a, b) of fb of
+  // plane(t, a) & plane(j, b), read 64 samples at a time.
+  const int ne0 = SM.nent[0], ne1 = SM.nent[1];
+  const bool tbits = ne0 + ne1 <= 2 * kItems + 1 && (ne0 + ne1) * W <= 4 * g;
+  if (tbits) {
+    for (int k = 0; k < 2; k++) {
+      const int nrk = SM.nrphi[k];
+      int running = k ? ne0 : 0;
+      for (int r0 = 0; r0 < nrk; r0 += nt) {
+        const int r = r0 + tid;
+        int t = 0, e0 = 0, cnt = 0;
+        if (r < nrk) {
+          t = P.rphi[k * g + r];
+          e0 = P.phs[k * g + t];
+          cnt = P.phe[k * g + t] - e0;
+        }
+        int total;
+        const int off = block_scan(cnt, total, SM.scan);
+        for (int i = 0; i < cnt; i++)
+          ent[running + off + i] = (uint32_t)t | ((uint32_t)pcol[k][e0 + i] << 9) |
+                                     ((phi[k][e0 + i] & 0x1FFu) << 18);
+        running += total;
+      }
+    }
+    __syncthreads();
+    for (int idx = tid; idx < (ne0 + ne1) * W; idx += nt) {
+      const int o = idx / W, w = idx - o * W;
+      const uint32_t en = ent[o];
+      const uint32_t fb = en >> 18;
+      const uint64_t *pt = sd.planes + (size_t)(en & 0x1FFu) * 3 * W + w;
+      const uint64_t *pj = sd.planes + (size_t)((en >> 9) & 0x1FFu) * 3 * W + w;
+      const uint64_t t0 = pt[0], t1 = pt[W], t2 = pt[2 * W];
+      const uint64_t j0 = pj[0], j1 = pj[W], j2 = pj[2 * W];
+      uint64_t x = 0;
+      if (fb & 0x001u) x |= t0 & j0;
+      if (fb & 0x002u) x |= t0 & j1;
+      if (fb & 0x004u) x |= t0 & j2;
+      if (fb & 0x008u) x |= t1 & j0;
+      if (fb & 0x010u) x |= t1 & j1;
+      if (fb & 0x020u) x |= t1 & j2;
+      if (fb & 0x040u) x |= t2 & j0;
+      if (fb & 0x080u) x |= t2 & j1;
+      if (fb & 0x100u) x |= t2 & j2;
+      trig[idx] = x;
+    }
+  }
   // Tables (key -> smallest network index) in shared memory first; a unit
   // whose keys do not fit there within kSmProbes probes uses its global
   // table of HT slots instead (initialised only then).
@@ -781,7 +861,8 @@ __global__ void __launch_bounds__(256, 3) k_units(const __grid_constant__ SetDev
   __syncthreads();
   for (int s = 1 + tid; s < S - 1; s += nt) {
     unsigned long long bits;
-    const unsigned long long key = signature(class_of(s), sig[s - 1], bits);
+    const unsigned long long key = tbits ? signature_t(class_of(s), sig[s - 1], bits)
+                                         : signature(class_of(s), sig[s - 1], bits);
     skey[s] = key;
     sbits[s] = bits;
     if (key && !sig_sm.insert_min(key, s)) SM.tfull = 1;

@@ -45,7 +45,7 @@ __host__ __device__ constexpr size_t al256(size_t x) { return (x + 255) & ~(size
 constexpr size_t kOffVals = 0;
 constexpr size_t kOffValsT = kOffVals + al256((size_t)kNAMaxGenes * kNAMaxSamples);
 constexpr size_t kOffPlanes = kOffValsT + al256((size_t)kNAMaxGenes * kNAMaxSamples);
-constexpr size_t kOffValid = kOffPlanes + al256(8ull * kNAMaxGenes * 3 * kNAW);
+constexpr size_t kOffValid = kOffPlanes + al256(2 * 8ull * kNAMaxGenes * 3 * kNAW);  // + word-major
 constexpr size_t kOffCtot = kOffValid + al256(8ull * kNAW);
 constexpr size_t kOffPrior = kOffCtot + al256(2ull * 9 * kNAPairs);
 constexpr size_t kOffMask = kOffPrior + al256((size_t)kNAPairs);
@@ -153,6 +153,7 @@ extern "C" int eddy_unit_noalloc(const eddy_opts *opts, const int8_t *vals, int 
   sd.alpha_edge_prior = opts->alpha_edge_prior;
   sd.exact_all = compute_thresholds(sd.alpha_edge, sd.alpha_edge_prior, g, sd.bonf, sd.thr) ? 1 : 0;
   sd.planes = (const uint64_t *)(base + kOffPlanes);
+  sd.planesT = sd.planes + (size_t)g * 3 * W;
   sd.valid = (const uint64_t *)(base + kOffValid);
   sd.vals = (const int8_t *)(base + kOffVals);
   sd.valsT = (const int8_t *)(base + kOffValsT);
