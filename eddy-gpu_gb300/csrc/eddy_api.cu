@@ -375,7 +375,7 @@ int launch_pairs_any(eddy_ctx *ctx, const SetDev &sd, const uint64_t *masks, int
         best = ms;
         bi = v;
       }
-      ctx->launches += 3;  // operand, GEMM + epilogue, general path
+      ctx->launches += 4;  // operand, GEMM + epilogue, general path, exact path
     }
     ctx->tuned[tune_key(sd)] = bi;
     variant = bi;
@@ -383,7 +383,7 @@ int launch_pairs_any(eddy_ctx *ctx, const SetDev &sd, const uint64_t *masks, int
   ctx->tuned_variant = variant;
   CK(launch_pairs_mma(sd, masks, B, ctx->d_afp8.as<uint8_t>(), ctx->d_Y.as<uint8_t>(), dmask, stats,
                       ctx->d_err.as<unsigned>(), ctx->sms, ctx->stream, variant));
-  ctx->launches += 3;  // operand, GEMM + epilogue, general path
+  ctx->launches += 4;  // operand, GEMM + epilogue, general path, exact path
   return EDDY_OK;
 }
 

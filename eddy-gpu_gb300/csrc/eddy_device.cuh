@@ -37,8 +37,26 @@ __device__ __forceinline__ void pair_rc(int p, int &row, int &col) {
 }
 
 // ------------------------------------------------------------ decisions
+// RN(n / a) for a divisor a whose odd part A (a = A 2^s) is below 2^18,
+// given y = RN(1 / a).  With q0 = RN(n y) (within 1.5 ulp of n / a) and the
+// residual r = RN(n - a q0) (one FMA), q0 + r y differs from n / a by less
+// than 2^-50 ulp.  n / a is never closer than 2^-19 ulp to a rounding
+// midpoint: a midpoint m has an odd 54-bit significand, so a m is a lattice
+// point of spacing 2^-53 ulp(m) * a that no 53-bit double n equals, and
+// |n / a - m| >= 2^-53 ulp(m) / A.  Hence RN(q0 + r y) = RN(n / a), the
+// correctly rounded quotient, in three dependent operations instead of a
+// full division.
+__device__ __forceinline__ double div_by_small(double n, double a, double y) {
+  const double q0 = __dmul_rn(n, y);
+  const double r = __fma_rn(-q0, a, n);
+  return __fma_rn(r, y, q0);
+}
+
 // Exact FP64 evaluation of one table exactly as kernel1.cu:121-203 and
 // 419-431 compute it, without FMA contraction (explicit _rn intrinsics).
+// Every rounding is the reference's: divisions by the table size use
+// div_by_small (N < 2^16), and the AS 147 series step cc x / a, a = p + k
+// (p = dof / 2, so the odd part of a is below 2^18), too.
 static __device__ __noinline__ int exact_decision(int a0, int a1, int a2, int a3, int a4, int a5,
                                                   int a6, int a7, int a8, int prior,
                                                   const SetDev &sd) {
@@ -50,10 +68,11 @@ static __device__ __noinline__ int exact_decision(int a0, int a1, int a2, int a3
   }
   ex[6] = ex[0] + ex[1] + ex[2];
   const double divisor = (double)ex[6];
+  const double rdiv = __drcp_rn(divisor);
   double e[9];
   for (int c = 0; c < 3; c++)
     for (int c1 = 0; c1 < 3; c1++)
-      e[c * 3 + c1] = __ddiv_rn(__dmul_rn((double)ex[c1], (double)ex[c + 3]), divisor);
+      e[c * 3 + c1] = div_by_small(__dmul_rn((double)ex[c1], (double)ex[c + 3]), divisor, rdiv);
   double yates = 0.0;
   bool flag = false;
   for (int c = 0; c < 3 && !flag; c++)
@@ -83,12 +102,35 @@ static __device__ __noinline__ int exact_decision(int a0, int a1, int a2, int a3
     if (!(arg < log(1.0e-37))) {
       double f = exp(arg);
       if (f != 0.0) {
-        double cc = 1.0, value = 1.0, a = p;
-        for (int it = 0; it < 100000; it++) {
-          a = __dadd_rn(a, 1.0);
-          cc = __ddiv_rn(__dmul_rn(cc, x), a);
-          value = __dadd_rn(value, cc);
-          if (cc <= __dmul_rn(1.0e-09, value)) break;
+        // for it < 100000: a += 1; cc = cc x / a; value += cc; stop when
+        // cc <= 1e-9 value.  Four steps per round, the stop tests after
+        // them (the steps past the stop are discarded); the reciprocals of
+        // the next round's divisors are formed off the dependent chain.
+        double cc = 1.0, value = 1.0, a = __dadd_rn(p, 1.0);
+        double y0 = __drcp_rn(a), y1 = __drcp_rn(__dadd_rn(a, 1.0)),
+               y2 = __drcp_rn(__dadd_rn(a, 2.0)), y3 = __drcp_rn(__dadd_rn(a, 3.0));
+        for (int it = 0; it < 100000; it += 4) {
+          const double a1 = __dadd_rn(a, 1.0), a2 = __dadd_rn(a, 2.0), a3 = __dadd_rn(a, 3.0);
+          const double an = __dadd_rn(a, 4.0);
+          const double z0 = __drcp_rn(an), z1 = __drcp_rn(__dadd_rn(an, 1.0)),
+                       z2 = __drcp_rn(__dadd_rn(an, 2.0)), z3 = __drcp_rn(__dadd_rn(an, 3.0));
+          const double c0 = div_by_small(__dmul_rn(cc, x), a, y0);
+          const double c1 = div_by_small(__dmul_rn(c0, x), a1, y1);
+          const double c2 = div_by_small(__dmul_rn(c1, x), a2, y2);
+          const double c3 = div_by_small(__dmul_rn(c2, x), a3, y3);
+          const double v0 = __dadd_rn(value, c0), v1 = __dadd_rn(v0, c1);
+          const double v2 = __dadd_rn(v1, c2), v3 = __dadd_rn(v2, c3);
+          if (c0 <= __dmul_rn(1.0e-09, v0)) { value = v0; break; }
+          if (c1 <= __dmul_rn(1.0e-09, v1)) { value = v1; break; }
+          if (c2 <= __dmul_rn(1.0e-09, v2)) { value = v2; break; }
+          value = v3;
+          if (c3 <= __dmul_rn(1.0e-09, v3)) break;
+          cc = c3;
+          a = an;
+          y0 = z0;
+          y1 = z1;
+          y2 = z2;
+          y3 = z3;
         }
         G = __dmul_rn(value, f);
       }

@@ -43,9 +43,11 @@ constexpr int kTM = 128, kPairsPerGroup = 3, kKC = 128;
 constexpr int kGroupPad = 24;
 constexpr int kMaxGroups = 8;
 constexpr unsigned long long kTimeoutNs = 2000000000ull;
-// tables the quick filter cannot settle go into one queue per launch (a
-// counter, then 6-word items) that k_general decides afterwards; a full
-// queue sets bit 2 of the error word and the batch is re-run elsewhere
+// tables the quick filter cannot settle go into one queue per launch that
+// k_general decides afterwards: a 4-word header (word 0 = tables, word 1 =
+// decisions deferred to k_exact), 6-word items, then the list of deferred
+// decisions; a full queue or list sets bit 2 of the error word and the batch
+// is re-run elsewhere
 constexpr int kQWords = 6;
 // full-sample tables of one group: 3 pairs x 12 floats
 constexpr uint32_t kGroupCtBytes = kPairsPerGroup * 12 * sizeof(float);
@@ -450,18 +452,80 @@ __global__ void __maxnreg__(max_regs<kEpi>())
   }
 }
 
+// Decision `slot` of queued table `it`: 0 = the full table, 1 + 3a + b =
+// the table with one sample of cell (a, b) removed.  The full table is
+// decided in FP32, and when the Minkowski leave-one-out window settles the
+// cells (or the cell is empty) the slot shares its decision; otherwise the
+// slot decides its own cell-removed table.  A decision in a guard band needs
+// the exact FP64 path: with allow_exact it is taken, else 2 is returned.
+__device__ __forceinline__ int general_task(const unsigned *it, int slot, const SetDev &sd,
+                                            bool allow_exact, unsigned &nexact,
+                                            unsigned &nfilt) {
+  const int prior = (it[4] >> 17) & 1;
+  int t[9] = {(int)(it[0] & 0xFFFFu), (int)(it[0] >> 16), (int)(it[1] & 0xFFFFu),
+              (int)(it[1] >> 16),     (int)(it[2] & 0xFFFFu), (int)(it[2] >> 16),
+              (int)(it[3] & 0xFFFFu), (int)(it[3] >> 16),     (int)(it[4] & 0xFFFFu)};
+  TabInfo ti;
+  table_info(t, ti);
+  const bool safe = loo_safe(ti, prior, sd);
+  if (slot == 0 && safe) nfilt++;
+  const int cell = slot - 1;
+  if (slot == 0 || safe || t[cell] == 0) {
+    int bit0 = fast_decision(ti, prior, sd);
+    if (bit0 == 2) {
+      if (!allow_exact) return 2;
+      nexact++;
+      bit0 = exact_decision(t[0], t[1], t[2], t[3], t[4], t[5], t[6], t[7], t[8], prior, sd);
+    }
+    return bit0;
+  }
+  t[cell]--;
+  TabInfo tj;
+  table_info(t, tj);
+  int bit = fast_decision(tj, prior, sd);
+  if (bit == 2) {
+    if (!allow_exact) return 2;
+    nexact++;
+    bit = exact_decision(t[0], t[1], t[2], t[3], t[4], t[5], t[6], t[7], t[8], prior, sd);
+  }
+  return bit;
+}
+
+__device__ __forceinline__ void set_decision(uint32_t *dmask, int B, const SetDev &sd,
+                                             const unsigned *it, int slot) {
+  const int cls = (it[4] >> 16) & 1;
+  const int p = (int)(it[5] & 0x1FFFFu), u = (int)(it[5] >> 17);
+  atomicOr(&dmask[(size_t)u * sd.c + p], 1u << (slot + 16 * cls));
+  mark_chunk(dmask, B, sd.c, u, p);
+}
+
+__device__ __forceinline__ void add_stats(unsigned long long *stats, unsigned nexact,
+                                          unsigned nfilt) {
+  if (!stats) return;
+  for (int o = 16; o > 0; o >>= 1) {
+    nexact += __shfl_down_sync(0xffffffffu, nexact, o);
+    nfilt += __shfl_down_sync(0xffffffffu, nfilt, o);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    if (nexact) atomicAdd(&stats[0], (unsigned long long)nexact);
+    if (nfilt) atomicAdd(&stats[2], (unsigned long long)nfilt);
+  }
+}
+
 // The general path for the queued tables of a launch, one thread per
-// (table, decision): decision 0 = the full table, decision 1 + 3a + b = the
-// table with one sample of cell (a, b) removed.  A thread decides the full
-// table (FP32, exact FP64 in the guard bands) and, when the Minkowski
-// leave-one-out window cannot settle the cells, its own cell-removed table;
-// so a table's ten decisions, some of them exact FP64 series, run in
-// parallel.  Set bits are OR-ed into the masks.
+// (table, decision), so a table's ten decisions run in parallel.  Set bits
+// are OR-ed into the masks.  Decisions that need the exact FP64 path are
+// listed (queue word 1 counts them) for k_exact: on this part a dependent
+// FP64 operation costs ~128 cycles and an SM issues one FP64 warp
+// instruction per ~32 cycles, so rechecks spread one per warp over the grid
+// would share the SMs' FP64 units, while k_exact runs them 32 to a warp.
 __global__ void __launch_bounds__(256) k_general(const __grid_constant__ SetDev sd,
-                                                 const unsigned *queue, unsigned qcap, int B,
-                                                 uint32_t *dmask, unsigned long long *stats) {
+                                                 unsigned *queue, unsigned qcap, int B,
+                                                 uint32_t *dmask, unsigned long long *stats,
+                                                 unsigned *err) {
   const unsigned cnt = queue[0] < qcap ? queue[0] : qcap;
   const unsigned *items = queue + 4;
+  unsigned *elist = queue + 4 + (size_t)qcap * kQWords;
   unsigned nexact = 0, nfilt = 0;
   const unsigned long long ntask = 10ull * cnt;
   for (unsigned long long task = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -469,43 +533,35 @@ __global__ void __launch_bounds__(256) k_general(const __grid_constant__ SetDev 
     const unsigned i = (unsigned)(task / 10);
     const int slot = (int)(task % 10);
     const unsigned *it = items + (size_t)i * kQWords;
-    const int cls = (it[4] >> 16) & 1, prior = (it[4] >> 17) & 1;
-    const int p = (int)(it[5] & 0x1FFFFu), u = (int)(it[5] >> 17);
-    int t[9] = {(int)(it[0] & 0xFFFFu), (int)(it[0] >> 16), (int)(it[1] & 0xFFFFu),
-                (int)(it[1] >> 16),     (int)(it[2] & 0xFFFFu), (int)(it[2] >> 16),
-                (int)(it[3] & 0xFFFFu), (int)(it[3] >> 16),     (int)(it[4] & 0xFFFFu)};
-    TabInfo ti;
-    unsigned nx = 0;
-    const int bit0 = decide(t, prior, sd, ti, nx);
-    int bit = bit0;
-    if (slot == 0) {
-      nexact += nx;
-      if (loo_safe(ti, prior, sd)) nfilt++;
-    } else if (!loo_safe(ti, prior, sd)) {
-      const int cell = slot - 1;
-      if (t[cell] > 0) {
-        t[cell]--;
-        TabInfo tj;
-        unsigned ny = 0;
-        bit = decide(t, prior, sd, tj, ny);
-        nexact += ny;
-      }
-    }
-    if (bit) {
-      atomicOr(&dmask[(size_t)u * sd.c + p], 1u << (slot + 16 * cls));
-      mark_chunk(dmask, B, sd.c, u, p);
+    const int bit = general_task(it, slot, sd, false, nexact, nfilt);
+    if (bit == 2) {
+      const unsigned k = atomicAdd(&queue[1], 1u);
+      if (k < qcap) elist[k] = (unsigned)task;
+      else atomicOr(err, 2u);
+    } else if (bit) {
+      set_decision(dmask, B, sd, it, slot);
     }
   }
-  if (stats) {
-    for (int o = 16; o > 0; o >>= 1) {
-      nexact += __shfl_down_sync(0xffffffffu, nexact, o);
-      nfilt += __shfl_down_sync(0xffffffffu, nfilt, o);
-    }
-    if ((threadIdx.x & 31) == 0) {
-      if (nexact) atomicAdd(&stats[0], (unsigned long long)nexact);
-      if (nfilt) atomicAdd(&stats[2], (unsigned long long)nfilt);
-    }
+  add_stats(stats, nexact, nfilt);
+}
+
+// The listed decisions of k_general through the exact FP64 path, one lane
+// each, one warp per block (one per SM at the launch size used).
+__global__ void __launch_bounds__(32) k_exact(const __grid_constant__ SetDev sd,
+                                              const unsigned *queue, unsigned qcap, int B,
+                                              uint32_t *dmask, unsigned long long *stats) {
+  const unsigned n = queue[1] < qcap ? queue[1] : qcap;
+  const unsigned *items = queue + 4;
+  const unsigned *elist = queue + 4 + (size_t)qcap * kQWords;
+  unsigned nexact = 0, nfilt = 0;
+  for (unsigned k = blockIdx.x * 32u + threadIdx.x; k < n; k += gridDim.x * 32u) {
+    const unsigned task = elist[k];
+    const unsigned *it = items + (size_t)(task / 10) * kQWords;
+    const int slot = (int)(task % 10);
+    unsigned nf = 0;
+    if (general_task(it, slot, sd, true, nexact, nf)) set_decision(dmask, B, sd, it, slot);
   }
+  add_stats(stats, nexact, nfilt);
 }
 
 // -------------------------------------------------------------- operands
@@ -640,7 +696,8 @@ static unsigned queue_cap_used(int B, int c) {
   return (v >= 1 && (unsigned long)v < cap) ? (unsigned)v : cap;
 }
 size_t mma_a_bytes(int B, int n, int c) {
-  return a_operand_bytes(B, n) + 16 + (size_t)queue_cap(B, c) * kQWords * sizeof(uint32_t);
+  // operand, queue header, items, then the list of exact decisions
+  return a_operand_bytes(B, n) + 16 + (size_t)queue_cap(B, c) * (kQWords + 1) * sizeof(uint32_t);
 }
 
 cudaError_t launch_build_y(const SetDev &sd, uint8_t *Y, cudaStream_t st) {
@@ -679,7 +736,10 @@ static cudaError_t launch_variant(const SetDev &sd, const uint8_t *Afp8, const u
                                             stats, err, gqueue, qcap);
   e = cudaGetLastError();
   if (e != cudaSuccess) return e;
-  k_general<<<sms * 8, 256, 0, st>>>(sd, gqueue, qcap, B, dmask, stats);
+  k_general<<<sms * 8, 256, 0, st>>>(sd, gqueue, qcap, B, dmask, stats, err);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  k_exact<<<sms, 32, 0, st>>>(sd, gqueue, qcap, B, dmask, stats);
   return cudaGetLastError();
 }
 

@@ -19,8 +19,8 @@ size_t mma_y_bytes(int c, int n);
 // the FP32 copy of the full-sample tables the epilogue reads.
 cudaError_t launch_build_y(const SetDev &sd, uint8_t *Y, cudaStream_t st);
 // Masks -> e4m3 operand (Afp8, mma_a_bytes(B, n, c) bytes), then the GEMM +
-// decision kernel and the general-path kernel for the tables its filter
-// could not settle.  Only bits of dmask are set: its masks and chunk bitmap
+// decision kernel, the general-path kernel for the tables its filter could
+// not settle and the exact-path kernel for that path's guard-band cases.  Only bits of dmask are set: its masks and chunk bitmap
 // must be zero when the launch starts.  *err: bit 0 = a bounded wait timed
 // out, bit 1 = the general-path queue overflowed (the batch must be decided
 // another way).  Variants (mma_variants()): tile widths N = 128 / 192 / 256
