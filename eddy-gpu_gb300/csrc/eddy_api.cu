@@ -147,6 +147,9 @@ struct eddy_ctx {
   // instantiated graph; prep_gen counts rebuilds of the resident set
   std::vector<uintptr_t> graph_key;
   cudaGraphExec_t graph_exec = nullptr;
+  // the last batch launched directly: a batch that repeats it is captured
+  // (a graph pays off only when it is replayed)
+  std::vector<uintptr_t> direct_key;
   long long graph_launches = 0;  // kernels in one replay
   unsigned prep_gen = 0;
   int prepared_set = -1;  // set whose data is resident in d_vals/d_planes/d_ctot
@@ -451,8 +454,9 @@ int run_units(eddy_ctx *ctx, SetRun &sr, int nunits, const uint64_t *masks_host,
       // before any copy uses it)
       CK(ctx->h_stage.ensure(16 * (size_t)Bt + 64));
       // steady state (device labellings, nothing kept, tile shape known, the
-      // set's operand built): the batch's launches as one CUDA graph,
-      // captured once per set / batch shape / buffers and replayed
+      // set's operand built): a batch that repeats the previous one's set /
+      // shape / buffers is captured as one CUDA graph and later replayed (a
+      // set that runs a single batch launches directly: no capture cost)
       const bool graphable = !masks_host && !keeping && !popc_batch && !use_popc() && c > 0 &&
                              ctx->y_ready && ctx->stream != nullptr &&
                              pick_variant(ctx, sd, Bt) >= 0;
@@ -542,31 +546,39 @@ int run_units(eddy_ctx *ctx, SetRun &sr, int nunits, const uint64_t *masks_host,
             (uintptr_t)ctx->d_keep.p, (uintptr_t)ctx->d_uset.p, (uintptr_t)ctx->d_uperm.p,
             (uintptr_t)ctx->d_stats.p, (uintptr_t)ctx->d_afp8.p, (uintptr_t)ctx->d_Y.p,
             (uintptr_t)ctx->d_err.p, (uintptr_t)ctx->d_mask0.p, (uintptr_t)ctx->stream};
-        if (key != ctx->graph_key || !ctx->graph_exec) {
-          if (ctx->graph_exec) {
-            cudaGraphExecDestroy(ctx->graph_exec);
-            ctx->graph_exec = nullptr;
+        const bool replay = ctx->graph_exec && key == ctx->graph_key;
+        if (!replay && key != ctx->direct_key) {
+          // first batch of this shape: direct launches, remembered
+          ctx->direct_key = key;
+          int rc = enqueue(false);
+          if (rc) return rc;
+        } else {
+          if (!replay) {
+            if (ctx->graph_exec) {
+              cudaGraphExecDestroy(ctx->graph_exec);
+              ctx->graph_exec = nullptr;
+            }
+            ctx->graph_key.clear();
+            const long long l0 = ctx->launches;
+            CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+            const int rc = enqueue(true);
+            cudaGraph_t graph = nullptr;
+            const cudaError_t ce = cudaStreamEndCapture(ctx->stream, &graph);
+            if (rc) {
+              if (graph) cudaGraphDestroy(graph);
+              return rc;
+            }
+            CK(ce);
+            const cudaError_t ie = cudaGraphInstantiate(&ctx->graph_exec, graph, 0);
+            cudaGraphDestroy(graph);
+            CK(ie);
+            ctx->graph_key = key;
+            ctx->graph_launches = ctx->launches - l0;
+            ctx->launches = l0;
           }
-          ctx->graph_key.clear();
-          const long long l0 = ctx->launches;
-          CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
-          const int rc = enqueue(true);
-          cudaGraph_t graph = nullptr;
-          const cudaError_t ce = cudaStreamEndCapture(ctx->stream, &graph);
-          if (rc) {
-            if (graph) cudaGraphDestroy(graph);
-            return rc;
-          }
-          CK(ce);
-          const cudaError_t ie = cudaGraphInstantiate(&ctx->graph_exec, graph, 0);
-          cudaGraphDestroy(graph);
-          CK(ie);
-          ctx->graph_key = key;
-          ctx->graph_launches = ctx->launches - l0;
-          ctx->launches = l0;
+          CK(cudaGraphLaunch(ctx->graph_exec, ctx->stream));
+          ctx->launches += ctx->graph_launches;
         }
-        CK(cudaGraphLaunch(ctx->graph_exec, ctx->stream));
-        ctx->launches += ctx->graph_launches;
       } else {
         int rc = enqueue(false);
         if (rc) return rc;

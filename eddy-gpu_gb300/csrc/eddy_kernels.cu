@@ -94,52 +94,86 @@ __device__ __forceinline__ void philox10(uint32_t c[4], uint32_t k0, uint32_t k1
 // One block per unit.  key(s) = Philox(ctr = (s, perm, set, 0), key = seed)
 // word 0; the nA samples with the smallest (key, s) are class 1.
 // Bitonic sort of the padded (key << 32 | s) array in shared memory.
-__global__ void k_counter_masks(int n, int nA, int W, uint64_t seed, const int32_t *unit_set,
-                                const int32_t *unit_perm, const uint64_t *mask0,
-                                uint64_t *masks) {
-  extern __shared__ unsigned long long kv[];
-  const int u = blockIdx.x;
+__global__ void __launch_bounds__(256) k_counter_masks(int n, int nA, int W, uint64_t seed,
+                                                       const int32_t *unit_set,
+                                                       const int32_t *unit_perm,
+                                                       const uint64_t *mask0, uint64_t *masks) {
+  // class 1 = the nA samples with the smallest (key, sample) pairs, keys
+  // from Philox-4x32-10 of (sample, permutation, set): the nA-th smallest
+  // key T is found by a radix select (four 8-bit digits, a 256-bin
+  // histogram each), then every sample with key < T is in, and of those
+  // with key == T the lowest-indexed ones that are still needed.  The same
+  // set as sorting the pairs and taking the first nA.
+  extern __shared__ uint32_t key[];  // [n], then [W] u64 mask words
+  __shared__ int hist[256];
+  __shared__ uint32_t s_prefix;
+  __shared__ int s_need;
+  const int u = blockIdx.x, tid = threadIdx.x, nt = blockDim.x;
   const int perm = unit_perm[u];
   uint64_t *out = masks + (size_t)u * W;
   if (perm == 0) {
-    for (int w = threadIdx.x; w < W; w += blockDim.x) out[w] = mask0[w];
+    for (int w = tid; w < W; w += nt) out[w] = mask0[w];
     return;
   }
-  int P = 1;
-  while (P < n) P <<= 1;
+  unsigned long long *mw = reinterpret_cast<unsigned long long *>(key + ((n + 1) & ~1));
   const uint32_t k0 = (uint32_t)seed, k1 = (uint32_t)(seed >> 32);
-  for (int s = threadIdx.x; s < P; s += blockDim.x) {
-    if (s < n) {
-      uint32_t c[4] = {(uint32_t)s, (uint32_t)perm, (uint32_t)unit_set[u], 0u};
-      philox10(c, k0, k1);
-      kv[s] = ((unsigned long long)c[0] << 32) | (unsigned)s;
-    } else {
-      kv[s] = ~0ull;
-    }
+  for (int s = tid; s < n; s += nt) {
+    uint32_t c[4] = {(uint32_t)s, (uint32_t)perm, (uint32_t)unit_set[u], 0u};
+    philox10(c, k0, k1);
+    key[s] = c[0];
   }
-  __syncthreads();
-  for (int k = 2; k <= P; k <<= 1) {
-    for (int j = k >> 1; j > 0; j >>= 1) {
-      for (int i = threadIdx.x; i < P; i += blockDim.x) {
-        int ixj = i ^ j;
-        if (ixj > i) {
-          unsigned long long a = kv[i], b = kv[ixj];
-          bool up = (i & k) == 0;
-          if ((a > b) == up) {
-            kv[i] = b;
-            kv[ixj] = a;
-          }
-        }
+  for (int w = tid; w < W; w += nt) mw[w] = 0ull;
+  if (tid == 0) {
+    s_prefix = 0u;
+    s_need = nA;
+  }
+  uint32_t pmask = 0u;
+  for (int shift = 24; shift >= 0; shift -= 8) {
+    for (int i = tid; i < 256; i += nt) hist[i] = 0;
+    __syncthreads();
+    const uint32_t prefix = s_prefix;
+    for (int s = tid; s < n; s += nt)
+      if ((key[s] & pmask) == prefix) atomicAdd(&hist[(key[s] >> shift) & 255u], 1);
+    __syncthreads();
+    if (tid < 32) {
+      // the digit whose bin holds the need-th candidate (warp scan of the
+      // 256 bins, 8 per lane)
+      const int need = s_need;
+      int loc[8], sum = 0;
+      for (int j = 0; j < 8; j++) {
+        loc[j] = hist[tid * 8 + j];
+        sum += loc[j];
       }
-      __syncthreads();
+      int incl = sum;
+      for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, incl, o);
+        if (tid >= o) incl += y;
+      }
+      int before = incl - sum;  // candidates in the bins of lower lanes
+      for (int j = 0; j < 8; j++) {
+        if (before < need && need <= before + loc[j]) {
+          s_prefix = prefix | ((uint32_t)(tid * 8 + j) << shift);
+          s_need = need - before;
+        }
+        before += loc[j];
+      }
     }
+    pmask |= 255u << shift;
+    __syncthreads();
   }
-  for (int w = threadIdx.x; w < W; w += blockDim.x) out[w] = 0;
+  const uint32_t T = s_prefix;
+  const int need = s_need;  // samples with key == T that are in
+  for (int s = tid; s < n; s += nt) {
+    bool in = key[s] < T;
+    if (key[s] == T) {
+      int rank = 0;  // equal keys before s (rare: 32-bit keys)
+      for (int t = 0; t < s; t++) rank += key[t] == T;
+      in = rank < need;
+    }
+    if (in) atomicOr(&mw[s >> 6], 1ull << (s & 63));
+  }
   __syncthreads();
-  for (int i = threadIdx.x; i < nA; i += blockDim.x) {
-    int s = (int)(kv[i] & 0xffffffffu);
-    atomicOr((unsigned long long *)&out[s >> 6], 1ull << (s & 63));
-  }
+  for (int w = tid; w < W; w += nt) out[w] = mw[w];
 }
 
 // ------------------------------------------------------------ k_pairs
@@ -1416,13 +1450,14 @@ cudaError_t launch_prep(const int8_t *vals, int g, int n, int W, int c, uint64_t
 cudaError_t launch_counter_masks(int n, int nA, int W, uint64_t seed, const int32_t *unit_set,
                                  const int32_t *unit_perm, const uint64_t *mask0, uint64_t *masks,
                                  int B, cudaStream_t st) {
-  int P = 1;
-  while (P < n) P <<= 1;
-  size_t smem = sizeof(unsigned long long) * P;
-  if (smem > 96 * 1024) {
-    cudaFuncSetAttribute(k_counter_masks, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  // keys [n] u32 (padded to 8 bytes), then the W mask words
+  const size_t smem = sizeof(uint32_t) * (size_t)((n + 1) & ~1) + sizeof(uint64_t) * W;
+  if (smem > 48 * 1024) {
+    cudaError_t e =
+        cudaFuncSetAttribute(k_counter_masks, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
   }
-  k_counter_masks<<<B, 512, smem, st>>>(n, nA, W, seed, unit_set, unit_perm, mask0, masks);
+  k_counter_masks<<<B, 256, smem, st>>>(n, nA, W, seed, unit_set, unit_perm, mask0, masks);
   return cudaGetLastError();
 }
 

@@ -146,9 +146,10 @@ def test_counter_stream_matches_oracle(eddy_lib, oracle_lib):
 
 
 def test_graph_replays_match_oracle(eddy_lib, oracle_lib, monkeypatch):
-    """Repeated batches of one set run as a captured CUDA graph (after the
-    first batch builds the operand); replays with new permutation indices,
-    a switch to another set and back (re-capture) all match the oracle."""
+    """Repeated batches of one set run as a captured CUDA graph: the first
+    batch of a shape launches directly, the second is captured, later ones
+    replay it with new permutation indices; a switch to another set and back
+    (direct, then re-capture) all match the oracle."""
     monkeypatch.setenv("EDDY_MMA_VARIANT", "2")  # a known tile shape: no tuning batch
     rng = np.random.default_rng(21)
     g, n, nA = 24, 180, 80
@@ -161,7 +162,8 @@ def test_graph_replays_match_oracle(eddy_lib, oracle_lib, monkeypatch):
     sb = ctx.add_set(np.arange(0, g, 2))
     B = 48
     prm = oracle_lib.params(mp=3)
-    for sid, first in [(sa, 1), (sa, 1 + B), (sa, 1 + 2 * B), (sb, 1), (sb, 1 + B), (sa, 1 + 3 * B)]:
+    for sid, first in [(sa, 1), (sa, 1 + B), (sa, 1 + 2 * B), (sb, 1), (sb, 1 + B), (sb, 1 + 2 * B),
+                       (sa, 1 + 3 * B), (sa, 1 + 4 * B), (sa, 1 + 5 * B)]:
         js, U = ctx.run_permutations(sid, first, B)
         genes = np.arange(g) if sid == sa else np.arange(0, g, 2)
         lab = oracle_lib.counter_labels(seed, sid, labels0, first + B)[first:first + B]
