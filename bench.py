@@ -364,7 +364,9 @@ def run_ours(args, rank, world, local):
     k1 = {"kernel": "k_pairs_mma", "bound": "tensor", "achieved": k1_flops / (k1_ms / 1e3) / 1e12,
           "peak": e4m3, "unit": "TFLOP/s", "ms_per_launch": k1_ms,
           "algorithmic_flops_per_launch": k1_flops,
-          "traffic": traffic_info.get("k_pairs_mma_bytes_per_unit", 0) * B or None}
+          "traffic": traffic_info.get("k_pairs_mma_bytes_per_unit", 0) * B or None,
+          "ncu_sm_throughput_pct": traffic_info.get("k_pairs_mma_sm_throughput_pct"),
+          "ncu_tensor_pipe_pct": traffic_info.get("k_pairs_mma_tensor_pipe_pct")}
     k1["frac"] = k1["achieved"] / e4m3
     # network assembly, dedup, BDeu, JS: algorithmic bytes (each stage's
     # inputs and outputs once through HBM)
@@ -372,7 +374,11 @@ def run_ours(args, rank, world, local):
     k2 = {"kernel": "k_units", "bound": "hbm", "achieved": bu * B / (k2_ms / 1e3) / 1e9,
           "peak": hbm, "unit": "GB/s", "ms_per_launch": k2_ms,
           "algorithmic_bytes_per_launch": bu * B,
-          "traffic": traffic_info.get("k_units_bytes_per_unit", 0) * B or None}
+          "traffic": traffic_info.get("k_units_bytes_per_unit", 0) * B or None,
+          # the kernel is bound by SM issue and latency, not HBM: the SM
+          # throughput share from ncu (2048-unit launch) goes with the HBM one
+          "ncu_sm_throughput_pct": traffic_info.get("k_units_sm_throughput_pct"),
+          "ncu_issue_active_pct": traffic_info.get("k_units_issue_active_pct")}
     k2["frac"] = k2["achieved"] / hbm
     dom = k1 if k1_ms >= k2_ms else k2
     roofline = dict(dom)
