@@ -346,7 +346,8 @@ struct UnitSmem {
   int nent[2];  // flip entries per class
   int nwl;      // work-list length
   int firstB0;  // first class-2 network equal to the class-2 full network
-  int repB;     // first occurrence of the class-2 full network
+  int firstE2;  // first class-2 network with an empty signature (S - 1: none)
+  int ncand;    // candidates for unique networks
   int scan[32];
   unsigned status;
   int U;
@@ -891,6 +892,7 @@ __global__ void __launch_bounds__(256, 3) k_units(const __grid_constant__ SetDev
     srep[0] = 0;
     srep[S - 1] = S - 1;
     SM.tfull = 0;
+    SM.firstE2 = S - 1;
   }
   __syncthreads();
   for (int s = 1 + tid; s < S - 1; s += nt) {
@@ -900,6 +902,7 @@ __global__ void __launch_bounds__(256, 3) k_units(const __grid_constant__ SetDev
     skey[s] = key;
     sbits[s] = bits;
     if (key && !sig_sm.insert_min(key, s)) SM.tfull = 1;
+    if (!key && s > sd.nA) atomicMin(&SM.firstE2, s);
   }
   if (tid == 0) SM.nwl = 0;
   __syncthreads();
@@ -1042,22 +1045,39 @@ __global__ void __launch_bounds__(256, 3) k_units(const __grid_constant__ SetDev
 
   // ---- P4: first-occurrence dedup.  Networks without changed nodes are
   // their class's full network: class-1 ones duplicate network 0, class-2
-  // ones the first class-2 network without changes (firstB0), whose own first
-  // occurrence the hash table decides.  Only network 0, firstB0 and the
-  // signature representatives with changes go into the table.
+  // ones the first class-2 network without changes (firstB0).  Every other
+  // network shares its signature representative's network, and that
+  // representative comes first.  So the unique networks are the candidates
+  // -- network 0, firstB0 and the signature representatives with changes --
+  // that are the first occurrence of their network hash; only they go into
+  // the table, and only they are looked up.
   const int HT = L.HT;
-  if (tid == 0) SM.firstB0 = S - 1;
+  const int nrep = SM.nwl;  // signature representatives in wl
+  // firstB0: the first class-2 network with an empty signature, or a class-2
+  // representative (its group's first network) whose record has no changes
+  if (tid == 0) {
+    SM.firstB0 = SM.firstE2;
+    SM.ncand = 2;
+  }
   __syncthreads();
-  for (int s = sd.nA + 1 + tid; s < S - 1; s += nt)
-    if (rec_of(s)[1] == 0) atomicMin(&SM.firstB0, s);
+  for (int i = tid; i < nrep; i += nt) {
+    const int s = wl[i];
+    if (s > sd.nA && rec[(size_t)s * L.rec_words + 1] == 0) atomicMin(&SM.firstB0, s);
+  }
   __syncthreads();
   const int firstB0 = SM.firstB0;
-  auto inserted = [&](int s) -> bool {
-    return s == 0 || s == firstB0 ||
-           (s != S - 1 && skey[s] != 0 && srep[s] == s && rec[(size_t)s * L.rec_words + 1] != 0);
-  };
+  // candidates (in the per-network id array, no longer needed per network)
+  int *cand = uid;
+  if (tid == 0) {
+    cand[0] = 0;
+    cand[1] = firstB0;
+  }
+  for (int i = tid; i < nrep; i += nt) {
+    const int s = wl[i];
+    if (rec[(size_t)s * L.rec_words + 1] != 0) cand[atomicAdd(&SM.ncand, 1)] = s;
+  }
   // network table: shared memory first (the signature table is done with),
-  // the global one when the inserted networks do not fit
+  // the global one when the candidates do not fit
   const MinTable net_sm{smk, smv, kSmSlots - 1, ~0ull, kSmProbes};
   const MinTable net_gl{htk, htv, (unsigned)HT - 1, ~0ull, (unsigned)HT};
   auto net_key = [&](int s) -> unsigned long long {
@@ -1067,49 +1087,49 @@ __global__ void __launch_bounds__(256, 3) k_units(const __grid_constant__ SetDev
   table_init(smk, smv, kSmSlots, ~0ull);
   if (tid == 0) SM.tfull = 0;
   __syncthreads();
-  for (int s = tid; s < S; s += nt)
-    if (inserted(s) && !net_sm.insert_min(net_key(s), s)) SM.tfull = 1;
+  const int m = SM.ncand;
+  for (int i = tid; i < m; i += nt)
+    if (!net_sm.insert_min(net_key(cand[i]), cand[i])) SM.tfull = 1;
+  // bitmap of the unique networks over the network ids, and the merged
+  // candidates with their representatives (both in the signature-bitset
+  // scratch, free after the signature phase)
+  uint32_t *ubits = (uint32_t *)sbits;
+  const int nbw = (S + 31) >> 5;
+  int *vrep = (int *)sbits + nbw;
+  for (int i = tid; i < nbw; i += nt) ubits[i] = 0u;
+  if (tid == 0) SM.nwl = 0;
   __syncthreads();
   const bool net_global = SM.tfull != 0;
   if (net_global) {
     table_init(htk, htv, HT, ~0ull);
     __syncthreads();
-    for (int s = tid; s < S; s += nt)
-      if (inserted(s)) net_gl.insert_min(net_key(s), s);
+    for (int i = tid; i < m; i += nt) net_gl.insert_min(net_key(cand[i]), cand[i]);
     __syncthreads();
   }
   const MinTable &net_tab = net_global ? net_gl : net_sm;
-  if (tid == 0) {
-    SM.repB = net_tab.get(net_key(firstB0));
-    SM.nwl = 0;
+  for (int i = tid; i < m; i += nt) {
+    const int c = cand[i];
+    const int r = net_tab.get(net_key(c));
+    if (r == c) {
+      atomicOr(&ubits[c >> 5], 1u << (c & 31));
+    } else {
+      // merged by hash: checked list by list below
+      const int k = atomicAdd(&SM.nwl, 1);
+      wl[k] = c;
+      vrep[k] = r;
+    }
   }
   __syncthreads();
-  const int repB = SM.repB;
+  // unique networks in network order: the set bits before each one
   int running = 0;
-  for (int s0 = 0; s0 < S; s0 += nt) {
-    const int s = s0 + tid;
-    int uq = 0;
-    int rep = -1;
-    if (s < S) {
-      const unsigned long long *Rs = rec_of(s);
-      if (Rs[1] == 0) {
-        rep = (class_of(s) == 0) ? 0 : repB;
-      } else {
-        rep = net_tab.get(net_key(s));
-      }
-      uq = (rep == s) ? 1 : 0;
-      // inserted networks merged by hash are checked list by list below
-      if (rep != s && inserted(s)) wl[atomicAdd(&SM.nwl, 1)] = s;
-    }
+  for (int w0 = 0; w0 < nbw; w0 += nt) {
+    const int w = w0 + tid;
+    const uint32_t word = w < nbw ? ubits[w] : 0u;
     int total;
-    int off = block_scan(uq, total, SM.scan);
-    if (s < S) {
-      if (uq) {
-        uid[s] = running + off;
-        urep[running + off] = s;
-      } else {
-        uid[s] = -1 - rep;  // encodes the representative
-      }
+    const int off = block_scan(__popc(word), total, SM.scan);
+    for (uint32_t x = word; x; x &= x - 1) {
+      const int b = __ffs(x) - 1;
+      urep[running + off + __popc(word & ((1u << b) - 1u))] = 32 * w + b;
     }
     running += total;
   }
@@ -1120,7 +1140,7 @@ __global__ void __launch_bounds__(256, 3) k_units(const __grid_constant__ SetDev
   const int nver = SM.nwl;
   for (int wi = warp; wi < nver; wi += nw) {
     const int s = wl[wi];
-    const int r = -1 - uid[s];
+    const int r = vrep[wi];
     int ks, ss, kr, sr;
     net_of(s, sd, sig, ks, ss);
     net_of(r, sd, sig, kr, sr);
