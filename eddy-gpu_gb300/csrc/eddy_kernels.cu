@@ -1384,30 +1384,35 @@ __global__ void __launch_bounds__(256, 3) k_units(const __grid_constant__ SetDev
 }
 
 // Normalisation (main.cu:1302-1404) and JS (main.cu:1406-1428) of every
-// unit of a batch, one warp per unit, from the node-summed fixed-point
-// scores k_units left in the unit's scratch: per class min, max and mean of
-// the scores, likelihoods exp((d - mean) 10 / (max - min)) normalised to
-// sum 1, then the two KL terms of kool() (routines.cu:42-60), zeros
-// skipped, in FP64.  A unit k_units gave up on (U < 0) is left as it is.
+// unit of a batch from the node-summed fixed-point scores k_units left in
+// the unit's scratch: per class min, max and mean of the scores,
+// likelihoods exp((d - mean) 10 / (max - min)) normalised to sum 1, then the
+// two KL terms of kool() (routines.cu:42-60), zeros skipped, in FP64.  A
+// unit k_units gave up on (U < 0) is left as it is.  One warp per unit
+// (kJsLanes lanes, so the FP64 chains of the unique networks run side by
+// side); the exponentials of the first kJsCache * kJsLanes networks are
+// kept in registers between the sum and the KL pass instead of being
+// computed twice (FP64 is slow on this part).
+constexpr int kJsLanes = 32, kJsCache = 1;
 __global__ void __launch_bounds__(256) k_js(const __grid_constant__ SetDev sd,
                                             const __grid_constant__ BatchDev bd) {
-  const int u = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
-  const int lane = threadIdx.x & 31;
-  if (u >= bd.B) return;
-  const int U = bd.U[u];
-  if (U < 0) return;
+  const int u = (int)((blockIdx.x * blockDim.x + threadIdx.x) / kJsLanes);
+  const int sub = threadIdx.x & (kJsLanes - 1);
+  const int U = u < bd.B ? bd.U[u] : -1;
+  const bool act = U > 0;  // (inactive lanes join the shuffles with neutral values)
   const int S = sd.S;
   const UnitLayout L = unit_layout(sd.c, S, bd.kmax);
-  const long long *dist = (const long long *)(bd.scratch + (size_t)u * bd.unit_bytes + L.dist);
+  const long long *dist =
+      act ? (const long long *)(bd.scratch + (size_t)u * bd.unit_bytes + L.dist) : nullptr;
   long long l0 = LLONG_MAX, h0 = LLONG_MIN, l1 = LLONG_MAX, h1 = LLONG_MIN;
-  for (int uu = lane; uu < U; uu += 32) {
+  for (int uu = sub; act && uu < U; uu += kJsLanes) {
     const long long a = dist[uu], b = dist[S + uu];
     l0 = a < l0 ? a : l0;
     h0 = a > h0 ? a : h0;
     l1 = b < l1 ? b : l1;
     h1 = b > h1 ? b : h1;
   }
-  for (int o = 16; o > 0; o >>= 1) {
+  for (int o = kJsLanes / 2; o > 0; o >>= 1) {
     long long x;
     x = __shfl_xor_sync(0xffffffffu, l0, o); l0 = x < l0 ? x : l0;
     x = __shfl_xor_sync(0xffffffffu, h0, o); h0 = x > h0 ? x : h0;
@@ -1415,30 +1420,44 @@ __global__ void __launch_bounds__(256) k_js(const __grid_constant__ SetDev sd,
     x = __shfl_xor_sync(0xffffffffu, h1, o); h1 = x > h1 ? x : h1;
   }
   double s0 = 0.0, s1 = 0.0;
-  for (int uu = lane; uu < U; uu += 32) {
+  for (int uu = sub; act && uu < U; uu += kJsLanes) {
     s0 += (double)(dist[uu] - l0);
     s1 += (double)(dist[S + uu] - l1);
   }
-  for (int o = 16; o > 0; o >>= 1) {
+  for (int o = kJsLanes / 2; o > 0; o >>= 1) {
     s0 += __shfl_xor_sync(0xffffffffu, s0, o);
     s1 += __shfl_xor_sync(0xffffffffu, s1, o);
   }
-  const double m0 = s0 / (double)U, m1 = s1 / (double)U;
-  const double sA = 10.0 / (double)(h0 - l0), sB = 10.0 / (double)(h1 - l1);
+  const double m0 = act ? s0 / (double)U : 0.0, m1 = act ? s1 / (double)U : 0.0;
+  const double sA = act ? 10.0 / (double)(h0 - l0) : 0.0, sB = act ? 10.0 / (double)(h1 - l1) : 0.0;
+  auto ea_of = [&](int uu) { return exp(((double)(dist[uu] - l0) - m0) * sA); };
+  auto eb_of = [&](int uu) { return exp(((double)(dist[S + uu] - l1) - m1) * sB); };
+  double ea[kJsCache], eb[kJsCache];
   double e0 = 0.0, e1 = 0.0;
-  for (int uu = lane; uu < U; uu += 32) {
-    e0 += exp(((double)(dist[uu] - l0) - m0) * sA);
-    e1 += exp(((double)(dist[S + uu] - l1) - m1) * sB);
+#pragma unroll
+  for (int j = 0; j < kJsCache; j++) {
+    const int uu = sub + kJsLanes * j;
+    ea[j] = eb[j] = 0.0;
+    if (act && uu < U) {
+      ea[j] = ea_of(uu);
+      eb[j] = eb_of(uu);
+      e0 += ea[j];
+      e1 += eb[j];
+    }
   }
-  for (int o = 16; o > 0; o >>= 1) {
+  for (int uu = sub + kJsLanes * kJsCache; act && uu < U; uu += kJsLanes) {
+    e0 += ea_of(uu);
+    e1 += eb_of(uu);
+  }
+  for (int o = kJsLanes / 2; o > 0; o >>= 1) {
     e0 += __shfl_xor_sync(0xffffffffu, e0, o);
     e1 += __shfl_xor_sync(0xffffffffu, e1, o);
   }
-  const int keep = bd.keep_slot ? bd.keep_slot[u] : -1;
+  const int keep = (act && bd.keep_slot) ? bd.keep_slot[u] : -1;
   double ls = 0.0;
-  for (int uu = lane; uu < U; uu += 32) {
-    const double Pu = exp(((double)(dist[uu] - l0) - m0) * sA) / e0;
-    const double Qu = exp(((double)(dist[S + uu] - l1) - m1) * sB) / e1;
+  auto term = [&](int uu, double a, double b) {
+    const double Pu = a / e0;
+    const double Qu = b / e1;
     const double M = (Pu + Qu) / 2;
     if (M != 0) {
       if (Pu != 0) ls += 0.5 * (Pu * log(Pu / M));
@@ -1448,9 +1467,16 @@ __global__ void __launch_bounds__(256) k_js(const __grid_constant__ SetDev sd,
       bd.out_lval[((size_t)keep * 2 + 0) * S + uu] = Pu;
       bd.out_lval[((size_t)keep * 2 + 1) * S + uu] = Qu;
     }
+  };
+#pragma unroll
+  for (int j = 0; j < kJsCache; j++) {
+    const int uu = sub + kJsLanes * j;
+    if (act && uu < U) term(uu, ea[j], eb[j]);
   }
-  for (int o = 16; o > 0; o >>= 1) ls += __shfl_xor_sync(0xffffffffu, ls, o);
-  if (lane == 0) {
+  for (int uu = sub + kJsLanes * kJsCache; act && uu < U; uu += kJsLanes)
+    term(uu, ea_of(uu), eb_of(uu));
+  for (int o = kJsLanes / 2; o > 0; o >>= 1) ls += __shfl_xor_sync(0xffffffffu, ls, o);
+  if (act && sub == 0) {
     double js = ls / log(2.0);
     if (h0 == l0 || h1 == l1) js = __longlong_as_double(0x7ff8000000000000ll);
     bd.js[u] = js;
@@ -1497,7 +1523,7 @@ cudaError_t launch_units(const SetDev &sd, const BatchDev &bd, cudaStream_t st) 
   k_units<<<bd.B, threads, smem, st>>>(sd, bd);
   e = cudaGetLastError();
   if (e != cudaSuccess) return e;
-  k_js<<<(bd.B + 7) / 8, 256, 0, st>>>(sd, bd);
+  k_js<<<(bd.B + 256 / kJsLanes - 1) / (256 / kJsLanes), 256, 0, st>>>(sd, bd);
   return cudaGetLastError();
 }
 
