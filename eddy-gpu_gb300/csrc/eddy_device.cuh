@@ -305,42 +305,8 @@ __device__ __forceinline__ bool quick_zero(const TabInfo &ti, int prior, const S
   return bound < sd.thr[prior][ds].chiA;
 }
 
-// quick_zero on the FP32 counts of the tensor-core epilogue: o = the nine
-// counts as exact floats.  Demands every marginal >= 2 (dof 4 in t and every
-// t', support unchanged), Yates off everywhere and N <= 4096, so that every
-// marginal product below is an exact FP32 integer.  The test of quick_zero,
-//   (N (rho - 1) + rho chi_hi) 1.0001 + 1e-3 < chiA,
-// chi_hi = N (Q - 1) + 1e-5 N, rho = rm cm / q, q = (rm - 1)(cm - 1),
-// multiplied through by q D with D = R0 R1 R2 C0 C1 C2 > 0, so no division
-// is left on the path:  Q D = sum_a PR_a sum_b o_ab^2 PC_b, PR_a / PC_b =
-// the products of the other two marginals.  FP32 error of Q D - D:
-// <= 6e-7 D (all products of marginals exact, o^2 exact), i.e. <= 6e-7 N in
-// chi^2, inside the 1e-5 N term; the other roundings are relative 1e-6,
-// inside the 1.0001 and 1e-3 terms.  chiA: the no-edge threshold of dof 4
-// (negative: never).
-__device__ __forceinline__ bool quick_zero_f(const float *o, float chiA) {
-  const float R0 = o[0] + o[1] + o[2], R1 = o[3] + o[4] + o[5], R2 = o[6] + o[7] + o[8];
-  const float C0 = o[0] + o[3] + o[6], C1 = o[1] + o[4] + o[7], C2 = o[2] + o[5] + o[8];
-  const float N = R0 + R1 + R2;
-  const float rm = fminf(R0, fminf(R1, R2)), cm = fminf(C0, fminf(C1, C2));
-  const float q = (rm - 1.f) * (cm - 1.f), rc = rm * cm;
-  if (!(rm >= 2.f && cm >= 2.f && N >= 32.f && N <= 4096.f && q >= 5.f * (N - 1.f) &&
-        rc >= 5.f * N))
-    return false;
-  const float PR0 = R1 * R2, PR1 = R0 * R2, PR2 = R0 * R1;
-  const float PC0 = C1 * C2, PC1 = C0 * C2, PC2 = C0 * C1;
-  const float D = (R0 * PR0) * (C0 * PC0);
-  const float s0 = fmaf(o[0] * o[0], PC0, fmaf(o[1] * o[1], PC1, o[2] * o[2] * PC2));
-  const float s1 = fmaf(o[3] * o[3], PC0, fmaf(o[4] * o[4], PC1, o[5] * o[5] * PC2));
-  const float s2 = fmaf(o[6] * o[6], PC0, fmaf(o[7] * o[7], PC1, o[8] * o[8] * PC2));
-  const float QD = fmaf(PR0, s0, fmaf(PR1, s1, PR2 * s2));
-  // q D bound = (N (rm + cm - 1) + rc (N (Q - 1) + 1e-5 N)) D
-  const float lhs = fmaf(N * (rm + cm - 1.f) + rc * (1e-5f * N), D, rc * N * (QD - D));
-  return fmaf(lhs, 1.0001f, 1e-3f * q * D) < chiA * q * D;
-}
-
 // Packed FP32 pairs (add/sub/mul/fma .rn.f32x2, sm_100 and later): two
-// lanes per instruction.  quick_zero_f2 runs the bound of quick_zero_f on
+// lanes per instruction.  quick_zero_f2 (below) runs quick_zero's bound on
 // both classes of a pair at once, lane x = class 1, lane y = class 2.
 typedef unsigned long long f32x2;
 __device__ __forceinline__ f32x2 f2_pack(float x, float y) {
@@ -378,10 +344,21 @@ __device__ __forceinline__ f32x2 f2_fma(f32x2 a, f32x2 b, f32x2 c) {
   asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
   return d;
 }
-// o[k] = {class-1 count, class-2 count} of cell k (exact FP32 integers);
-// chiA as in quick_zero_f.  Bit 0 / bit 1 of the result: class 1 / class 2
-// settled (no edge in any of its ten tables).  Same formula and margins as
-// quick_zero_f, evaluated lane-wise.
+// quick_zero on the FP32 counts of the tensor-core epilogue, both classes
+// of a pair at once: o[k] = {class-1 count, class-2 count} of cell k, exact
+// floats; bit 0 / bit 1 of the result: class 1 / class 2 settled (no edge
+// in any of its ten tables).  Demands every marginal >= 2 (dof 4 in t and every
+// t', support unchanged), Yates off everywhere and N <= 4096, so that every
+// marginal product below is an exact FP32 integer.  The test of quick_zero,
+//   (N (rho - 1) + rho chi_hi) 1.0001 + 1e-3 < chiA,
+// chi_hi = N (Q - 1) + 1e-5 N, rho = rm cm / q, q = (rm - 1)(cm - 1),
+// multiplied through by q D with D = R0 R1 R2 C0 C1 C2 > 0, so no division
+// is left on the path:  Q D = sum_a PR_a sum_b o_ab^2 PC_b, PR_a / PC_b =
+// the products of the other two marginals.  FP32 error of Q D - D:
+// <= 6e-7 D (all products of marginals exact, o^2 exact), i.e. <= 6e-7 N in
+// chi^2, inside the 1e-5 N term; the other roundings are relative 1e-6,
+// inside the 1.0001 and 1e-3 terms.  chiA: the no-edge threshold of dof 4
+// (negative: never).
 __device__ __forceinline__ unsigned quick_zero_f2(const f32x2 *o, float chiA) {
   const f32x2 one = f2_pack(1.f, 1.f);
   const f32x2 R0 = f2_add(f2_add(o[0], o[1]), o[2]), R1 = f2_add(f2_add(o[3], o[4]), o[5]),
@@ -526,68 +503,26 @@ struct ListGen {
 // ------------------------------------------------------------------ BDeu
 static __device__ __constant__ int8_t c_dmap[82];
 
-// BDeu score of node t with parent set ps[0..np) over the samples of one
-// class (mask m), fixed point.  kernel5.cu:30-218: q = product of the
-// parents' observed-state counts, r = node's; score = sum over parent
-// configurations j of [-LG(q)[N_ij] + sum_k LG(q r)[N_ijk]] with
-// LG(d)[m] = lgamma(m + 4/d) - lgamma(4/d).
-static __device__ int64_t bdeu_score(const SetDev &sd, int t, int np, const int *ps,
-                              const uint64_t *m, const uint16_t *cnt3 /*[g][3] of this class*/) {
-  int nstate[4], st[4][3];
-  int idx[4] = {t, np > 0 ? ps[0] : 0, np > 1 ? ps[1] : 0, np > 2 ? ps[2] : 0};
-  for (int k = 0; k <= np; k++) {
-    int c = 0;
-    for (int a = 0; a < 3; a++)
-      if (cnt3[idx[k] * 3 + a] > 0) st[k][c++] = a;
-    nstate[k] = c;
-  }
-  const int r = nstate[0];
-  int q = 1;
-  for (int k = 1; k <= np; k++) q *= nstate[k];
-  if (q == 0) return 0;
-  if (np == 0) {
-    // no parent: N_1k are the node's state counts in this class
-    if (r == 0) return 0;
-    const int64_t *LG1 = sd.lg + (size_t)c_dmap[r] * sd.lg_stride;
-    int nij = 0;
-    int64_t sc = 0;
-    for (int kk = 0; kk < r; kk++) {
-      const int cnt = cnt3[t * 3 + st[0][kk]];
+// BDeu score of node t without parents over the samples of one class
+// (fixed point): with its observed-state count r and state counts N_k in
+// the class (kernel5.cu:30-218 for q = 1), sum_k LG(r)[N_k] - LG(1)[sum_k
+// N_k], LG(d)[m] = lgamma(m + 4/d) - lgamma(4/d).  Nodes with parents are
+// scored as flat tasks (bdeu_config_term).
+static __device__ int64_t bdeu_score0(const SetDev &sd, int t,
+                                      const uint16_t *cnt3 /*[g][3] of this class*/) {
+  int r = 0, nij = 0;
+  int64_t sc = 0;
+  for (int a = 0; a < 3; a++) r += cnt3[t * 3 + a] > 0;
+  if (r == 0) return 0;
+  const int64_t *LG1 = sd.lg + (size_t)c_dmap[r] * sd.lg_stride;
+  for (int a = 0; a < 3; a++) {
+    const int cnt = cnt3[t * 3 + a];
+    if (cnt > 0) {
       nij += cnt;
       sc += LG1[cnt];
     }
-    return sc - sd.lg[(size_t)c_dmap[1] * sd.lg_stride + nij];
   }
-  const int64_t *LGq = sd.lg + (size_t)c_dmap[q] * sd.lg_stride;
-  const int64_t *LGqr = (r > 0) ? sd.lg + (size_t)c_dmap[q * r] * sd.lg_stride : nullptr;
-  const int W = sd.W;
-  const uint64_t *P = sd.planes;
-  int64_t score = 0;
-  for (int j = 0; j < q; j++) {
-    int rem = j;
-    const uint64_t *pp[3] = {nullptr, nullptr, nullptr};
-    for (int k = 1; k <= np; k++) {
-      int s = st[k][rem % nstate[k]];
-      rem /= nstate[k];
-      pp[k - 1] = P + ((size_t)idx[k] * 3 + s) * W;
-    }
-    int nij = 0;
-    for (int kk = 0; kk < r; kk++) {
-      const uint64_t *pt = P + ((size_t)t * 3 + st[0][kk]) * W;
-      int cnt = 0;
-      for (int w = 0; w < W; w++) {
-        uint64_t x = pt[w] & m[w];
-        if (np > 0) x &= pp[0][w];
-        if (np > 1) x &= pp[1][w];
-        if (np > 2) x &= pp[2][w];
-        cnt += __popcll(x);
-      }
-      nij += cnt;
-      score += LGqr[cnt];
-    }
-    score -= LGq[nij];
-  }
-  return score;
+  return sc - sd.lg[(size_t)c_dmap[1] * sd.lg_stride + nij];
 }
 
 // Parent configurations of node t's score (np >= 1 parents) in one class:
@@ -604,7 +539,7 @@ __device__ __forceinline__ int bdeu_q(const uint16_t *cnt3, int np, int p0, int 
 
 // One parent configuration j of node t's score over class mask m (the
 // terms of kernel5.cu:30-218 for that j): sum_k LG(q r)[N_jk] - LG(q)[N_j].
-// Summing the terms of all j gives bdeu_score (fixed point, exact).
+// Summing the terms of all j gives the node's score (fixed point, exact).
 // dmap: the divisor map in shared memory.
 static __device__ __noinline__ int64_t bdeu_config_term(const SetDev &sd, int t, int np, int p0,
                                                         int p1, int p2, const uint64_t *m,

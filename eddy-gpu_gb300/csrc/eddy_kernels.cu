@@ -1235,9 +1235,8 @@ __global__ void __launch_bounds__(256, 3) k_units(const __grid_constant__ SetDev
   for (int i = tid; i < 2 * g; i += nt) {
     if (P.fcnt[i] != 0) continue;
     const int k = i / g, t = i % g;
-    int ps[3] = {0xFFFF, 0xFFFF, 0xFFFF};
-    P.fsc[(k * 2 + 0) * g + t] = bdeu_score(sd, t, 0, ps, P.mA, P.cnt3);
-    P.fsc[(k * 2 + 1) * g + t] = bdeu_score(sd, t, 0, ps, P.mB, P.cnt3 + 3 * g);
+    P.fsc[(k * 2 + 0) * g + t] = bdeu_score0(sd, t, P.cnt3);
+    P.fsc[(k * 2 + 1) * g + t] = bdeu_score0(sd, t, P.cnt3 + 3 * g);
   }
   bdeu_items(
       sd, P, SM.scan, 2 * g,
@@ -1331,9 +1330,8 @@ __global__ void __launch_bounds__(256, 3) k_units(const __grid_constant__ SetDev
         if (!differs(k, rec)) return;
         const int t = (int)(rec & 0x3FFF), np = (int)((rec >> 14) & 3);
         if (np == 0) {
-          int ps[3] = {0xFFFF, 0xFFFF, 0xFFFF};
-          s1 = bdeu_score(sd, t, 0, ps, P.mA, P.cnt3);
-          s2 = bdeu_score(sd, t, 0, ps, P.mB, P.cnt3 + 3 * g);
+          s1 = bdeu_score0(sd, t, P.cnt3);
+          s2 = bdeu_score0(sd, t, P.cnt3 + 3 * g);
         }
         atomicAdd((unsigned long long *)&dist[uu],
                   (unsigned long long)(s1 - P.fsc[(k * 2 + 0) * g + t]));

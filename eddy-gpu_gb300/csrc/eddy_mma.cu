@@ -333,7 +333,7 @@ __global__ void __maxnreg__(max_regs<kEpi>())
     int acc = 0;
     uint32_t accphase = 0;
     unsigned nexact = 0, nfilt = 0, ntab = 0;
-    // no-edge thresholds of dof 4 without / with a prior (quick_zero_f)
+    // no-edge thresholds of dof 4 without / with a prior (quick_zero_f2)
     const float thr0 = sd.exact_all ? -1.f : sd.thr[0][2].chiA;
     const float thr1 = sd.exact_all ? -1.f : sd.thr[1][2].chiA;
     unsigned *qitems = gqueue + 4;
