@@ -2,10 +2,11 @@
 units per second, exact edges.
 
 Workload (one gene set, the largest single-GPU configuration the metric is
-quoted on): 200 genes x 1000 samples (classes 400/600), -mp 4, a stretch of
-the -r 10000 permutation test; synthetic seeded data with the shapes of the
-"precision stress" workload (eddy_gpu/synth.py config 4).  One step = one
-batch of `--units` permutations (default 8192) of that set.
+quoted on): 200 genes x 1000 samples (classes 400/600), -mp 4, the -r 10000
+permutation test; synthetic seeded data with the shapes of the "precision
+stress" workload (eddy_gpu/synth.py config 4).  One step = one batch of
+`--units` permutations of that set (default 10000: the whole -r 10000 run,
+which the library decides as one batch).
 
   value  device time of the hot path with the set resident in HBM (CUDA
          events on the library's launching stream around K steps; labellings
@@ -432,7 +433,7 @@ def main():
     ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--units", type=int, default=8192, help="permutations per step")
+    ap.add_argument("--units", type=int, default=10000, help="permutations per step")
     ap.add_argument("--cpu-units", type=int, default=16, help="permutations in the CPU sample")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-fp64", action="store_true")
