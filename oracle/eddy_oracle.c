@@ -1,7 +1,7 @@
 /*
  * eddy_oracle.c -- CPU restatement of the EDDY hot path of skimlab/eddy-gpu.
  *
- * TEST INFRASTRUCTURE ONLY (the checker).  See eddy_oracle.h for the map
+ * TEST INFRASTRUCTURE ONLY (the oracle).  See eddy_oracle.h for the map
  * from each function to the reference file:line it restates.  FP64 and the
  * reference's operation order are kept wherever the reference's own result
  * depends on it (chi-square terms, AS 147 series, BDeu sums, normalisation,

@@ -2,7 +2,7 @@
  * eddy_oracle.h -- CPU restatement of the EDDY per-class dependency-network
  * inference and label-permutation test of skimlab/eddy-gpu.
  *
- * TEST INFRASTRUCTURE ONLY.  This library is the checker: the parity tests,
+ * TEST INFRASTRUCTURE ONLY.  This library is the oracle: the parity tests,
  * the smoke check and the CPU baseline leg of bench.py call it.  The product
  * (libeddy_gpu.so and the eddy CLI) never links or calls it.
  *
