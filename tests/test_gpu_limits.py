@@ -1,8 +1,9 @@
 """GPU parity at the edges of the supported shapes and on the fallback
-paths, against the oracle: more than 4096 samples (labellings generated on
-the host), the 512-gene maximum, a general-path queue that overflows (the
-batch is then decided by the popcount kernel) and networks with more changed
-nodes than the first pass records (the units are re-run)."""
+paths, against the oracle: 4096 samples (the largest labelling drawn on the
+device), more than 4096 samples (labellings generated on the host), the
+512-gene maximum, a general-path queue that overflows (the batch is then
+decided by the popcount kernel) and networks with more changed nodes than
+the first pass records (the units are re-run)."""
 import numpy as np
 import pytest
 
@@ -24,6 +25,24 @@ def test_many_samples_counter_stream(eddy_lib, oracle_lib):
     data = planted(rng, g, n, nA=nA, planted=3)
     labels0 = np.concatenate([np.zeros(nA, np.uint8), np.ones(n - nA, np.uint8)])
     R, seed = 4, 99
+    ctx = eddy_lib.Context(max_parents=3, permutations=R, rng=eddy_lib.RNG_COUNTER, seed=seed)
+    ctx.load_matrix(data, labels0)
+    sid = ctx.add_set(np.arange(g))
+    js, U = ctx.run_permutations(sid, 0, R)
+    ojs, oU = _oracle(oracle_lib, data, oracle_lib.counter_labels(seed, sid, labels0, R))
+    assert np.array_equal(U, oU)
+    assert js_close(js, ojs)
+
+
+def test_largest_device_labelling(eddy_lib, oracle_lib):
+    """n = 4096, the largest sample count whose counter labellings are drawn
+    on the device (radix select over 4096 keys): labels, U and JS as the
+    oracle's sorted Philox keys give them."""
+    rng = np.random.default_rng(35)
+    g, n, nA = 6, 4096, 1500
+    data = planted(rng, g, n, nA=nA, planted=3)
+    labels0 = np.concatenate([np.zeros(nA, np.uint8), np.ones(n - nA, np.uint8)])
+    R, seed = 6, 123
     ctx = eddy_lib.Context(max_parents=3, permutations=R, rng=eddy_lib.RNG_COUNTER, seed=seed)
     ctx.load_matrix(data, labels0)
     sid = ctx.add_set(np.arange(g))
