@@ -513,10 +513,12 @@ __device__ __forceinline__ void add_stats(unsigned long long *stats, unsigned ne
 }
 
 // The general path for the queued tables of a launch, one thread per
-// (table, decision), so a table's ten decisions run in parallel.  Set bits
-// are OR-ed into the masks.  Decisions that need the exact FP64 path are
-// listed (queue word 1 counts them) for k_exact: on this part a dependent
-// FP64 operation costs ~128 cycles and an SM issues one FP64 warp
+// table: the full table's FP32 decision and its Minkowski leave-one-out
+// window once, then, when the window cannot settle them, the nine
+// cell-removed tables (an empty cell shares the full table's decision).  A
+// table's bits go into its mask with one atomic.  Decisions in a guard band
+// are listed (queue word 1 counts them) for k_exact: on this part a
+// dependent FP64 operation costs ~128 cycles and an SM issues one FP64 warp
 // instruction per ~32 cycles, so rechecks spread one per warp over the grid
 // would share the SMs' FP64 units, while k_exact runs them 32 to a warp.
 __global__ void __launch_bounds__(256) k_general(const __grid_constant__ SetDev sd,
@@ -527,19 +529,45 @@ __global__ void __launch_bounds__(256) k_general(const __grid_constant__ SetDev 
   const unsigned *items = queue + 4;
   unsigned *elist = queue + 4 + (size_t)qcap * kQWords;
   unsigned nexact = 0, nfilt = 0;
-  const unsigned long long ntask = 10ull * cnt;
-  for (unsigned long long task = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x;
-       task < ntask; task += (unsigned long long)gridDim.x * blockDim.x) {
-    const unsigned i = (unsigned)(task / 10);
-    const int slot = (int)(task % 10);
+  for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < cnt; i += gridDim.x * blockDim.x) {
     const unsigned *it = items + (size_t)i * kQWords;
-    const int bit = general_task(it, slot, sd, false, nexact, nfilt);
-    if (bit == 2) {
-      const unsigned k = atomicAdd(&queue[1], 1u);
-      if (k < qcap) elist[k] = (unsigned)task;
-      else atomicOr(err, 2u);
-    } else if (bit) {
-      set_decision(dmask, B, sd, it, slot);
+    const int prior = (it[4] >> 17) & 1;
+    int t[9] = {(int)(it[0] & 0xFFFFu), (int)(it[0] >> 16), (int)(it[1] & 0xFFFFu),
+                (int)(it[1] >> 16),     (int)(it[2] & 0xFFFFu), (int)(it[2] >> 16),
+                (int)(it[3] & 0xFFFFu), (int)(it[3] >> 16),     (int)(it[4] & 0xFFFFu)};
+    TabInfo ti;
+    table_info(t, ti);
+    const bool safe = loo_safe(ti, prior, sd);
+    if (safe) nfilt++;
+    const int bit0 = fast_decision(ti, prior, sd);
+    uint32_t bits = 0u;
+    auto put = [&](int slot, int bit) {
+      if (bit == 2) {
+        const unsigned k = atomicAdd(&queue[1], 1u);
+        if (k < qcap) elist[k] = i * 10u + (unsigned)slot;
+        else atomicOr(err, 2u);
+      } else {
+        bits |= (uint32_t)bit << slot;
+      }
+    };
+    put(0, bit0);
+#pragma unroll
+    for (int cell = 0; cell < 9; cell++) {
+      if (safe || t[cell] == 0) {
+        put(1 + cell, bit0);
+      } else {
+        t[cell]--;
+        TabInfo tj;
+        table_info(t, tj);
+        put(1 + cell, fast_decision(tj, prior, sd));
+        t[cell]++;
+      }
+    }
+    if (bits) {
+      const int cls = (it[4] >> 16) & 1;
+      const int p = (int)(it[5] & 0x1FFFFu), u = (int)(it[5] >> 17);
+      atomicOr(&dmask[(size_t)u * sd.c + p], bits << (16 * cls));
+      mark_chunk(dmask, B, sd.c, u, p);
     }
   }
   add_stats(stats, nexact, nfilt);
