@@ -317,8 +317,8 @@ int pick_variant(eddy_ctx *ctx, const SetDev &sd, int B) {
   if (it != ctx->tuned.end()) return it->second;
   if (B >= 512) return -1;
   // untuned small batch: the tile shape that measured fastest on 200 x 1000
-  // sets (N = 256, 16 epilogue warps)
-  return 4 % mma_variants();
+  // sets (N = 256, 8 epilogue warps)
+  return 3 % mma_variants();
 }
 
 // Buffers of the tensor-core path for a batch of B units (and the set's Y
