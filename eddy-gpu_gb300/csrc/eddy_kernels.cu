@@ -94,7 +94,7 @@ __device__ __forceinline__ void philox10(uint32_t c[4], uint32_t k0, uint32_t k1
 // One block per unit.  key(s) = Philox(ctr = (s, perm, set, 0), key = seed)
 // word 0; the nA samples with the smallest (key, s) are class 1.
 // Bitonic sort of the padded (key << 32 | s) array in shared memory.
-__global__ void __launch_bounds__(256) k_counter_masks(int n, int nA, int W, uint64_t seed,
+__global__ void __launch_bounds__(128) k_counter_masks(int n, int nA, int W, uint64_t seed,
                                                        const int32_t *unit_set,
                                                        const int32_t *unit_perm,
                                                        const uint64_t *mask0, uint64_t *masks) {
@@ -1494,14 +1494,15 @@ cudaError_t launch_prep(const int8_t *vals, int g, int n, int W, int c, uint64_t
 cudaError_t launch_counter_masks(int n, int nA, int W, uint64_t seed, const int32_t *unit_set,
                                  const int32_t *unit_perm, const uint64_t *mask0, uint64_t *masks,
                                  int B, cudaStream_t st) {
-  // keys [n] u32 (padded to 8 bytes), then the W mask words
+  // keys [n] u32 (padded to 8 bytes), then the W mask words; 128-thread
+  // blocks (the select is barrier-bound: more blocks per SM hide it)
   const size_t smem = sizeof(uint32_t) * (size_t)((n + 1) & ~1) + sizeof(uint64_t) * W;
   if (smem > 48 * 1024) {
     cudaError_t e =
         cudaFuncSetAttribute(k_counter_masks, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
   }
-  k_counter_masks<<<B, 256, smem, st>>>(n, nA, W, seed, unit_set, unit_perm, mask0, masks);
+  k_counter_masks<<<B, 128, smem, st>>>(n, nA, W, seed, unit_set, unit_perm, mask0, masks);
   return cudaGetLastError();
 }
 
