@@ -105,6 +105,7 @@ struct eddy_ctx {
   std::string err = "";
   int genes = 0, samples = 0, nA = 0, nB = 0, W = 0;
   std::vector<int8_t> data;
+  std::vector<uint8_t> gene_full;  // gene i holds only -1/0/1 values
   std::vector<uint8_t> labels0;
   std::vector<SetHost> sets;
   cudaStream_t stream = nullptr;
@@ -154,6 +155,7 @@ struct eddy_ctx {
   unsigned prep_gen = 0;
   int prepared_set = -1;  // set whose data is resident in d_vals/d_planes/d_ctot
   bool y_ready = false;
+  int y_core = -1;  // layout the resident Y operand was built for
 };
 
 static int fail(eddy_ctx *c, int code, const char *fmt, ...) {
@@ -263,6 +265,15 @@ int prepare_set(eddy_ctx *ctx, int set_id, SetRun &sr) {
     const char *dm = getenv("EDDY_DECISIONS");
     if (dm && strcmp(dm, "fp64") == 0) sd.exact_all = 1;
   }
+  {
+    // the 4-cell tensor-core layout needs every sample of every gene in one
+    // of the three states (a table's margins are then the genes' own class
+    // counts); EDDY_PAIR_LAYOUT=full keeps the 9-cell layout
+    const char *pl = getenv("EDDY_PAIR_LAYOUT");
+    bool full = true;
+    for (int v : S.genes) full = full && ctx->gene_full[v];
+    sd.core = (full && !(pl && strcmp(pl, "full") == 0)) ? 1 : 0;
+  }
   sd.planes = ctx->d_planes.as<uint64_t>();
   sd.planesT = sd.planes + (size_t)g * 3 * sd.W;
   sd.valid = ctx->d_valid.as<uint64_t>();
@@ -317,20 +328,22 @@ int pick_variant(eddy_ctx *ctx, const SetDev &sd, int B) {
   if (it != ctx->tuned.end()) return it->second;
   if (B >= 512) return -1;
   // untuned small batch: the tile shape that measured fastest on 200 x 1000
-  // sets (N = 256, 8 epilogue warps)
-  return 3 % mma_variants();
+  // sets (9-cell layout: N = 256 with 8 epilogue warps; 4-cell layout, whose
+  // epilogue decides 8 pairs per column group: N = 192 with 12)
+  return (sd.core ? 2 : 3) % mma_variants();
 }
 
 // Buffers of the tensor-core path for a batch of B units (and the set's Y
 // operand, built once per resident set).
 int prepare_pairs(eddy_ctx *ctx, const SetDev &sd, int B) {
-  if (!ctx->y_ready) {
-    CK(ctx->d_Y.ensure(mma_y_bytes(sd.c, sd.n)));
+  if (!ctx->y_ready || ctx->y_core != sd.core) {
+    CK(ctx->d_Y.ensure(mma_y_bytes(sd)));
     CK(launch_build_y(sd, ctx->d_Y.as<uint8_t>(), ctx->stream));
-    ctx->launches += 1;
+    ctx->launches += mma_build_launches(sd);
     ctx->y_ready = true;
+    ctx->y_core = sd.core;
   }
-  CK(ctx->d_afp8.ensure(mma_a_bytes(B, sd.n, sd.c)));
+  CK(ctx->d_afp8.ensure(mma_a_bytes(sd, B)));
   CK(ctx->d_err.ensure(sizeof(unsigned)));
   return EDDY_OK;
 }
@@ -378,7 +391,7 @@ int launch_pairs_any(eddy_ctx *ctx, const SetDev &sd, const uint64_t *masks, int
         best = ms;
         bi = v;
       }
-      ctx->launches += 4;  // operand, GEMM + epilogue, general path, exact path
+      ctx->launches += mma_launches(sd);
     }
     ctx->tuned[tune_key(sd)] = bi;
     variant = bi;
@@ -386,7 +399,7 @@ int launch_pairs_any(eddy_ctx *ctx, const SetDev &sd, const uint64_t *masks, int
   ctx->tuned_variant = variant;
   CK(launch_pairs_mma(sd, masks, B, ctx->d_afp8.as<uint8_t>(), ctx->d_Y.as<uint8_t>(), dmask, stats,
                       ctx->d_err.as<unsigned>(), ctx->sms, ctx->stream, variant));
-  ctx->launches += 4;  // operand, GEMM + epilogue, general path, exact path
+  ctx->launches += mma_launches(sd);
   return EDDY_OK;
 }
 
@@ -539,7 +552,7 @@ int run_units(eddy_ctx *ctx, SetRun &sr, int nunits, const uint64_t *masks_host,
         // and every buffer address
         std::vector<uintptr_t> key = {
             (uintptr_t)sr.set_id, (uintptr_t)ctx->prep_gen, (uintptr_t)sd.salt,
-            (uintptr_t)sd.exact_all, (uintptr_t)Bt, (uintptr_t)kmax_run, (uintptr_t)ub,
+            (uintptr_t)sd.exact_all, (uintptr_t)sd.core, (uintptr_t)Bt, (uintptr_t)kmax_run, (uintptr_t)ub,
             (uintptr_t)pick_variant(ctx, sd, Bt), (uintptr_t)ctx->o.seed,
             (uintptr_t)ctx->d_masks.p, (uintptr_t)ctx->d_dmask.p, (uintptr_t)ctx->d_scratch.p,
             (uintptr_t)ctx->d_js.p, (uintptr_t)ctx->d_U.p, (uintptr_t)ctx->d_status.p,
@@ -808,6 +821,15 @@ int eddy_load_matrix(eddy_ctx *ctx, const int8_t *data, int genes, int samples,
   ctx->nB = nB;
   ctx->W = (samples + 63) / 64;
   ctx->data.assign(data, data + (size_t)genes * samples);
+  ctx->gene_full.assign(genes, 1);
+  for (int i = 0; i < genes; i++)
+    for (int s = 0; s < samples; s++) {
+      const int8_t v = data[(size_t)i * samples + s];
+      if (v < -1 || v > 1) {
+        ctx->gene_full[i] = 0;
+        break;
+      }
+    }
   ctx->labels0.assign(class_of_sample, class_of_sample + samples);
   ctx->prepared_set = -1;
   std::vector<uint64_t> m0(ctx->W);

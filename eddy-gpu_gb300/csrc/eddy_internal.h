@@ -37,6 +37,9 @@ struct SetDev {
   int GW;                 // 32-bit words per network row bitset (ceil(g/32))
   int bonf;               // Bonferroni on
   int exact_all;          // pathological alphas: every table goes exact
+  int core;               // every value of the set is -1/0/1: the tensor-core
+                          // path counts 4 cells per table and derives the
+                          // other 5 from the genes' class counts
   double alpha_edge, alpha_edge_prior;
   Thr thr[2][kDofSlots];  // [0] = no prior (alpha_edge), [1] = prior pairs
   const uint64_t *planes; // [g][3][W]  bit s of plane (i, a) = (x_i(s) == a-1)

@@ -13,8 +13,15 @@
 // k_general, which sets the bits of the 10-bit decision masks of both
 // classes (kernel1.cu:121-203, 419-431) in a buffer that starts at zero.
 //
+// When every value of the set is -1/0/1 (kCore), a table's margins are the
+// two genes' own class counts, which a small kernel counts per unit: the
+// GEMM then holds only cells (-1,-1), (-1,0), (0,-1) and (0,0) of each table
+// (8 pairs per 32-column group instead of 3) and the epilogue derives the
+// other five by subtraction, exactly.
+//
 // Tile: 128 units (TMEM lanes) x kGroups column groups of 32 pair-cells
-// (3 pairs x 9 cells + 5 pad columns; N = 128, 192 or 256) x K in
+// (3 pairs x 9 cells + 5 pad columns, or 8 pairs x 4 cells; N = 128, 192 or
+// 256) x K in
 // 128-sample chunks; operands staged by TMA (cp.async.bulk.tensor, 128B
 // swizzle) through an mbarrier ring.  Warp roles: 0 = TMA producer, 1 =
 // TMEM owner + MMA issuer (it also stages each tile's full-sample tables
@@ -37,7 +44,7 @@
 namespace eddy {
 
 namespace {
-constexpr int kTM = 128, kPairsPerGroup = 3, kKC = 128;
+constexpr int kTM = 128, kPairsPerGroup = 3, kCorePairs = 8, kKC = 128;
 // the pair groups of Y are padded to a multiple of every variant's groups
 // per tile (4, 6, 8)
 constexpr int kGroupPad = 24;
@@ -49,8 +56,11 @@ constexpr unsigned long long kTimeoutNs = 2000000000ull;
 // decisions; a full queue or list sets bit 2 of the error word and the batch
 // is re-run elsewhere
 constexpr int kQWords = 6;
-// full-sample tables of one group: 3 pairs x 12 floats
+// full-sample tables of one group: 3 pairs x 12 floats (nine counts, the
+// prior flag, two pad), or in the 4-cell layout 8 pairs x 4 floats (the four
+// counted cells) followed by the group's prior bits and three pad words
 constexpr uint32_t kGroupCtBytes = kPairsPerGroup * 12 * sizeof(float);
+static_assert(kGroupCtBytes == (kCorePairs * 4 + 4) * sizeof(float), "group table size");
 constexpr uint32_t kBarBytes = 4096;  // barriers and table buffers after the stage ring
 constexpr uint32_t kCtOff = 256;      // table buffers inside the barrier block
 
@@ -177,6 +187,113 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t *r) {
 __device__ __forceinline__ void tmem_ld_wait() {
   asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 }
+
+// ------------------------------------------------------ the 4-cell layout
+// One gene of a pair: its counts {class 1, class 2} of the states -1, 0
+// and 1, the products of the other two states' counts, the product of all
+// three (the factors quick_zero_f2 forms from a table's margins) and the
+// smallest count minus one.  w = class-1 counts of states -1 and 0 (16 bits
+// each), F = the full-sample counts, N = the class sizes; a gene of this
+// layout has no missing value, so its class-2 counts and its state-1 count
+// follow by subtraction.  Every value is an exact integer in FP32, equal to
+// the margin quick_zero_f2 sums from the nine cells.
+struct CoreGene {
+  f32x2 M0, M1, M2, P0, P1, P2, Dg, m1;
+  float mx, my;
+};
+__device__ __forceinline__ void core_gene(CoreGene &G, uint32_t w, float4 F, f32x2 N) {
+  // 2^23 + c as a float, minus 2^23: the 16-bit count c, exactly
+  const float c0 = __uint_as_float(__byte_perm(w, 0x4B000000u, 0x7610)) - 8388608.f;
+  const float c1 = __uint_as_float(__byte_perm(w, 0x4B000000u, 0x7632)) - 8388608.f;
+  G.M0 = f2_pack(c0, F.x - c0);
+  G.M1 = f2_pack(c1, F.y - c1);
+  G.M2 = f2_sub(f2_sub(N, G.M0), G.M1);
+  G.P0 = f2_mul(G.M1, G.M2);
+  G.P1 = f2_mul(G.M0, G.M2);
+  G.P2 = f2_mul(G.M0, G.M1);
+  G.Dg = f2_mul(G.M0, G.P0);
+  G.mx = fminf(f2_x(G.M0), fminf(f2_x(G.M1), f2_x(G.M2)));
+  G.my = fminf(f2_y(G.M0), fminf(f2_y(G.M1), f2_y(G.M2)));
+  G.m1 = f2_sub(f2_pack(G.mx, G.my), f2_pack(1.f, 1.f));
+}
+// Terms of the bound that depend on a unit's class sizes N only.
+struct CoreN {
+  f32x2 N;
+  float n5m_x, n5m_y, n5_x, n5_y;
+  bool okx, oky;
+};
+__device__ __forceinline__ void core_n(f32x2 N, CoreN &K) {
+  const float Nx = f2_x(N), Ny = f2_y(N);
+  K.N = N;
+  K.okx = Nx >= 32.f && Nx <= 4096.f;
+  K.oky = Ny >= 32.f && Ny <= 4096.f;
+  K.n5m_x = 5.f * (Nx - 1.f);
+  K.n5m_y = 5.f * (Ny - 1.f);
+  K.n5_x = 5.f * Nx;
+  K.n5_y = 5.f * Ny;
+}
+// The nine cells {class 1, class 2} of a table, o[3a + b] for states a - 1
+// (row gene) and b - 1 (column gene), from its four counted class-1 cells
+// a[0..3] (TMEM columns), their full-sample counts F and the genes' counts.
+__device__ __forceinline__ void core_cells(const uint32_t *a, float4 F, const CoreGene &R,
+                                           const CoreGene &C, f32x2 *o) {
+  const float a0 = __uint_as_float(a[0]), a1 = __uint_as_float(a[1]);
+  const float a3 = __uint_as_float(a[2]), a4 = __uint_as_float(a[3]);
+  o[0] = f2_pack(a0, F.x - a0);
+  o[1] = f2_pack(a1, F.y - a1);
+  o[3] = f2_pack(a3, F.z - a3);
+  o[4] = f2_pack(a4, F.w - a4);
+  o[2] = f2_sub(f2_sub(R.M0, o[0]), o[1]);
+  o[5] = f2_sub(f2_sub(R.M1, o[3]), o[4]);
+  o[6] = f2_sub(f2_sub(C.M0, o[0]), o[3]);
+  o[7] = f2_sub(f2_sub(C.M1, o[1]), o[4]);
+  o[8] = f2_sub(f2_sub(R.M2, o[6]), o[7]);
+}
+// quick_zero_f2 on a table of the 4-cell layout: the same operations on the
+// same values (margins, their products and minima from the genes' terms),
+// so the same outcome, bit for bit.
+__device__ __forceinline__ unsigned core_zero_f2(const f32x2 *o, const CoreGene &R,
+                                                 const CoreGene &C, const CoreN &K, float chiA) {
+  const f32x2 N = K.N;
+  const f32x2 rm = f2_pack(R.mx, R.my), cm = f2_pack(C.mx, C.my);
+  const f32x2 q = f2_mul(R.m1, C.m1), rc = f2_mul(rm, cm);
+  const bool okx = K.okx && R.mx >= 2.f && C.mx >= 2.f && f2_x(q) >= K.n5m_x && f2_x(rc) >= K.n5_x;
+  const bool oky = K.oky && R.my >= 2.f && C.my >= 2.f && f2_y(q) >= K.n5m_y && f2_y(rc) >= K.n5_y;
+  const f32x2 D = f2_mul(R.Dg, C.Dg);
+  const f32x2 s0 = f2_fma(f2_mul(o[0], o[0]), C.P0,
+                          f2_fma(f2_mul(o[1], o[1]), C.P1, f2_mul(f2_mul(o[2], o[2]), C.P2)));
+  const f32x2 s1 = f2_fma(f2_mul(o[3], o[3]), C.P0,
+                          f2_fma(f2_mul(o[4], o[4]), C.P1, f2_mul(f2_mul(o[5], o[5]), C.P2)));
+  const f32x2 s2 = f2_fma(f2_mul(o[6], o[6]), C.P0,
+                          f2_fma(f2_mul(o[7], o[7]), C.P1, f2_mul(f2_mul(o[8], o[8]), C.P2)));
+  const f32x2 QD = f2_fma(R.P0, s0, f2_fma(R.P1, s1, f2_mul(R.P2, s2)));
+  const f32x2 rcN = f2_mul(rc, N);
+  // (rm - 1) + cm = (rm + cm) - 1: exact integers
+  const f32x2 t1 = f2_fma(N, f2_add(R.m1, cm), f2_mul(rcN, f2_pack(1e-5f, 1e-5f)));
+  const f32x2 lhs = f2_fma(t1, D, f2_mul(rcN, f2_sub(QD, D)));
+  const f32x2 qD = f2_mul(q, D);
+  const f32x2 L = f2_fma(lhs, f2_pack(1.0001f, 1.0001f), f2_mul(f2_pack(1e-3f, 1e-3f), qD));
+  const f32x2 Rr = f2_mul(f2_pack(chiA, chiA), qD);
+  return ((okx && f2_x(L) < f2_x(Rr)) ? 1u : 0u) | ((oky && f2_y(L) < f2_y(Rr)) ? 2u : 0u);
+}
+// The class-1 table of pair q of a group as integers, for the queue: the
+// four counted cells from TMEM and the five derived from the row gene's and
+// the column gene's class-1 counts wr, wc and the class-1 size n1.
+__device__ __forceinline__ void core_table(const uint32_t *r, int q, uint32_t wr, uint32_t wc,
+                                           int n1, int *t) {
+  t[0] = (int)__uint_as_float(r[4 * q]);
+  t[1] = (int)__uint_as_float(r[4 * q + 1]);
+  t[3] = (int)__uint_as_float(r[4 * q + 2]);
+  t[4] = (int)__uint_as_float(r[4 * q + 3]);
+  const int r0 = (int)(wr & 0xFFFFu), r1 = (int)(wr >> 16);
+  const int c0 = (int)(wc & 0xFFFFu), c1 = (int)(wc >> 16);
+  t[2] = r0 - t[0] - t[1];
+  t[5] = r1 - t[3] - t[4];
+  t[6] = c0 - t[0] - t[3];
+  t[7] = c1 - t[1] - t[4];
+  t[8] = (n1 - r0 - r1) - t[6] - t[7];
+}
+
 }  // namespace
 
 template <int kStages>
@@ -200,14 +317,18 @@ constexpr int max_regs() {
 // kStages: depth of the TMA ring; kEpi: epilogue warps (a multiple of 4);
 // kGroups: 32-column pair groups per tile (N = 32 kGroups).  One CTA per SM.
 // All variants produce identical masks; the autotuner picks by time.
-template <int kStages, int kEpi, int kGroups>
+template <int kStages, int kEpi, int kGroups, bool kCore>
 __global__ void __maxnreg__(max_regs<kEpi>())
     k_pairs_mma(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
                 const __grid_constant__ SetDev sd, const float *__restrict__ ctotf, int B, int nk,
                 int ntiles, int mblocks, unsigned long long *stats,
-                unsigned *err, unsigned *gqueue, unsigned qcap) {
+                unsigned *err, unsigned *gqueue, unsigned qcap,
+                const uint32_t *__restrict__ margc, const float *__restrict__ nc1,
+                const float4 *__restrict__ gcnt, const uint32_t *__restrict__ gtab) {
   constexpr int kTN = 32 * kGroups;
-  constexpr int kPairsPerTile = kGroups * kPairsPerGroup;
+  constexpr int kPPG = kCore ? kCorePairs : kPairsPerGroup;  // pairs per column group
+  constexpr int kPairsPerTile = kGroups * kPPG;
+  const int Bp = mblocks * kTM;
   constexpr uint32_t kStageBytes = (kTM + kTN) * kKC;
   constexpr uint32_t kCtBytes = kGroups * kGroupCtBytes;
   constexpr uint32_t kTmemCols = 2 * kTN <= 256 ? 256u : 512u;
@@ -242,6 +363,11 @@ __global__ void __maxnreg__(max_regs<kEpi>())
                  "n"(kTmemCols));
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
   }
+  // 4-cell layout: the genes' full-sample counts in shared memory, after
+  // the barrier block
+  float4 *sgcnt = reinterpret_cast<float4 *>(base + kStages * kStageBytes + kBarBytes);
+  if constexpr (kCore)
+    for (int i = threadIdx.x; i < sd.g; i += blockDim.x) sgcnt[i] = gcnt[i];
   tc_fence_before();
   __syncthreads();
   tc_fence_after();
@@ -290,7 +416,7 @@ __global__ void __maxnreg__(max_regs<kEpi>())
           const uint32_t cb = smem_u32(&S.ctfull[acc]);
           mbar_expect_tx(cb, kCtBytes);
           bulk_load(smem_u32(base + kStages * kStageBytes + kCtOff + acc * kCtBytes),
-                    ctotf + (size_t)tn * kPairsPerTile * 12, kCtBytes, cb);
+                    ctotf + (size_t)tn * kGroups * (kGroupCtBytes / 4), kCtBytes, cb);
           nct++;
         }
         const uint32_t dcol = tmem + (uint32_t)(acc * kTN);
@@ -337,6 +463,31 @@ __global__ void __maxnreg__(max_regs<kEpi>())
     const float thr0 = sd.exact_all ? -1.f : sd.thr[0][2].chiA;
     const float thr1 = sd.exact_all ? -1.f : sd.thr[1][2].chiA;
     unsigned *qitems = gqueue + 4;
+    // 4-cell layout: the class-1 count words of a group for this thread's
+    // unit (w[q] = column gene of pair q, w[8] = the row gene) and the
+    // unit's class-1 size, fetched one group ahead so that their L2 latency
+    // passes while the previous group is decided
+    uint32_t wcur[kCorePairs + 1], wnext[kCorePairs + 1];
+    float n1next = 0.f;
+    auto fetch = [&](int t2, int gi2) {
+      if constexpr (kCore) {
+        const int u2 = (t2 % mblocks) * kTM + row;
+        const uint32_t e = t2 < ntot ? gtab[(t2 / mblocks) * kGroups + wq + gi2 * kPerQuad]
+                                     : 0xFFFF0000u;
+        const int r2 = (int)(e >> 16), c2 = (int)(e & 0xFFFFu);
+        if (r2 != 0xFFFF) {
+          wnext[kCorePairs] = margc[(size_t)r2 * Bp + u2];
+#pragma unroll
+          for (int q = 0; q < kCorePairs; q++)
+            wnext[q] = margc[(size_t)(c2 + q < r2 ? c2 + q : r2 - 1) * Bp + u2];
+        }
+        if (gi2 == 0 && t2 < ntot) n1next = nc1[u2];
+      }
+    };
+    // with 16 epilogue warps the warps themselves hide the latency and the
+    // registers of a second word set would spill: words are loaded when used
+    constexpr bool kAhead = kEpi <= 12;
+    if (kAhead) fetch(blockIdx.x, 0);
     for (int t = blockIdx.x; t < ntot; t += gridDim.x) {
       const int tn = t / mblocks, mb = t % mblocks;
       if (!mbar_wait(smem_u32(&S.accfull[acc]), accphase, verr)) break;
@@ -345,33 +496,93 @@ __global__ void __maxnreg__(max_regs<kEpi>())
       const float *ctile =
           reinterpret_cast<const float *>(base + kStages * kStageBytes + kCtOff + acc * kCtBytes);
       const int u = mb * kTM + row;
-      // pairs of the tile below c (the last tile's tail is padding)
-      const int lim = sd.c - tn * kPairsPerTile;
-      // the warp's column groups, one at a time out of TMEM (pair q of a
-      // group = columns 9q .. 9q+8)
+      // 4-cell layout: the unit's class sizes {class 1, class 2}
+      f32x2 N = f2_pack(0.f, 0.f);
+      CoreN NC{};
+      if constexpr (kCore) {
+        const float n1 = kAhead ? n1next : nc1[u];
+        N = f2_pack(n1, (float)sd.n - n1);
+        core_n(N, NC);
+      }
+      // the warp's column groups, one at a time out of TMEM; pairs past c
+      // (the last tile's tail) are padding
 #pragma unroll 1
       for (int gi = 0; gi < kGpw; gi++) {
         const int grp = wq + gi * kPerQuad;
+        // the group's 32 TMEM columns (the 4-cell layout reads them in two
+        // halves in pass 1, and again in full for pass 2)
+        const uint32_t taddr = tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)(acc * kTN + grp * 32);
         uint32_t r[32];
-        tmem_ld32(tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)(acc * kTN + grp * 32), r);
-        tmem_ld_wait();
-        // pass 1: the all-zero bound of the group's six tables, both classes
-        // of a pair in the two lanes of packed FP32 pairs; bit 2 q + class of
+        if constexpr (!kCore) {
+          tmem_ld32(taddr, r);
+          tmem_ld_wait();
+        }
+        // pass 1: the all-zero bound of the group's tables, both classes of
+        // a pair in the two lanes of packed FP32 pairs; bit 2 q + class of
         // qmask = the table goes to the general path
         uint32_t qmask = 0u, vmask = 0u;
+        const float *gct = ctile + grp * (int)(kGroupCtBytes / 4);
+        const int p0 = tn * kPairsPerTile + grp * kPPG;
+        // 4-cell layout: the group's row gene and first column gene
+        int crow = 0, ccol0 = 0;
+        if constexpr (kCore) {
+          const uint32_t e = gtab[tn * kGroups + grp];
+          crow = (int)(e >> 16);
+          ccol0 = (int)(e & 0xFFFFu);
+          if (!kAhead) fetch(t, gi);
 #pragma unroll
-        for (int q = 0; q < kPairsPerGroup; q++) {
-          const int lp = grp * kPairsPerGroup + q;
-          const float *f = ctile + lp * 12;
-          f32x2 o2[9];
-#pragma unroll
-          for (int k = 0; k < 9; k++) {
-            const float a = __uint_as_float(r[9 * q + k]);
-            o2[k] = f2_pack(a, f[k] - a);
+          for (int k = 0; k <= kCorePairs; k++) wcur[k] = wnext[k];
+          if (kAhead) {
+            if (gi + 1 < kGpw) fetch(t, gi + 1);
+            else fetch(t + gridDim.x, 0);
           }
-          const float chiA = (f[9] != 0.f) ? thr1 : thr0;
-          qmask |= (~quick_zero_f2(o2, chiA) & 3u) << (2 * q);
-          vmask |= (lp < lim ? 3u : 0u) << (2 * q);
+        }
+        if constexpr (kCore) {
+          // pair q = columns 4q .. 4q+3 (cells (-1,-1), (-1,0), (0,-1),
+          // (0,0)) = genes (crow, ccol0 + q), live while ccol0 + q < crow;
+          // straight-line code over the eight pairs (a padding group has
+          // crow = 0xFFFF)
+          const uint32_t pbits = __float_as_uint(gct[32]);
+          if (crow != 0xFFFF) {
+            CoreGene Rg;
+            core_gene(Rg, wcur[kCorePairs], sgcnt[crow], N);
+#pragma unroll
+            for (int h = 0; h < 2; h++) {
+              uint32_t rh[16];
+              tmem_ld16(taddr + 16 * h, rh);
+              tmem_ld_wait();
+#pragma unroll
+              for (int qq = 0; qq < kPPG / 2; qq++) {
+                const int q = h * (kPPG / 2) + qq;
+                const bool live = ccol0 + q < crow;
+                const int col = live ? ccol0 + q : crow - 1;
+                CoreGene Cg;
+                core_gene(Cg, wcur[q], sgcnt[col], N);
+                const float4 F = reinterpret_cast<const float4 *>(gct)[q];
+                f32x2 o[9];
+                core_cells(rh + 4 * qq, F, Rg, Cg, o);
+                const float chiA = ((pbits >> q) & 1u) ? thr1 : thr0;
+                const unsigned settled = core_zero_f2(o, Rg, Cg, NC, chiA);
+                qmask |= (live ? (~settled & 3u) : 0u) << (2 * q);
+                vmask |= (live ? 3u : 0u) << (2 * q);
+              }
+            }
+          }
+        } else {
+          // pair q = columns 9q .. 9q+8
+#pragma unroll
+          for (int q = 0; q < kPPG; q++) {
+            const float *f = gct + q * 12;
+            f32x2 o2[9];
+#pragma unroll
+            for (int k = 0; k < 9; k++) {
+              const float a = __uint_as_float(r[9 * q + k]);
+              o2[k] = f2_pack(a, f[k] - a);
+            }
+            const float chiA = (f[9] != 0.f) ? thr1 : thr0;
+            qmask |= (~quick_zero_f2(o2, chiA) & 3u) << (2 * q);
+            vmask |= (p0 + q < sd.c ? 3u : 0u) << (2 * q);
+          }
         }
         if (u >= B) vmask = 0u;
         qmask &= vmask;
@@ -390,22 +601,37 @@ __global__ void __maxnreg__(max_regs<kEpi>())
           unsigned qbase = 0;
           if (lane == 31) qbase = atomicAdd(gqueue, incl);
           unsigned idx = __shfl_sync(0xffffffffu, qbase, 31) + incl - cnt;
+          if constexpr (kCore) {
+            tmem_ld32(taddr, r);
+            tmem_ld_wait();
+          }
 #pragma unroll
-          for (int q = 0; q < kPairsPerGroup; q++) {
+          for (int q = 0; q < kPPG; q++) {
             if (((qmask >> (2 * q)) & 3u) == 0u) continue;
-            const int lp = grp * kPairsPerGroup + q;
-            const float *f = ctile + lp * 12;
-            const int prior = (f[9] != 0.f) ? 1 : 0;
-            const int p = tn * kPairsPerTile + lp;
+            // pair index (row-major over the lower triangle)
+            const int p = kCore ? crow * (crow - 1) / 2 + ccol0 + q : p0 + q;
+            // the class-1 table and the full-sample table, as integers
+            int t1[9], tf[9], prior;
+            if constexpr (kCore) {
+              prior = (int)((__float_as_uint(gct[32]) >> q) & 1u);
+              core_table(r, q, wcur[kCorePairs], wcur[q], (int)f2_x(N), t1);
+#pragma unroll
+              for (int k = 0; k < 9; k++) tf[k] = (int)sd.ctot[(size_t)p * 9 + k];
+            } else {
+              const float *f = gct + q * 12;
+              prior = (f[9] != 0.f) ? 1 : 0;
+#pragma unroll
+              for (int k = 0; k < 9; k++) {
+                t1[k] = (int)__uint_as_float(r[9 * q + k]);
+                tf[k] = (int)f[k];
+              }
+            }
 #pragma unroll
             for (int cls = 0; cls < 2; cls++) {
               if (!((qmask >> (2 * q + cls)) & 1u)) continue;
               uint32_t o[9];
 #pragma unroll
-              for (int k = 0; k < 9; k++) {
-                const float a = __uint_as_float(r[9 * q + k]);
-                o[k] = (uint32_t)(cls ? f[k] - a : a);
-              }
+              for (int k = 0; k < 9; k++) o[k] = (uint32_t)(cls ? tf[k] - t1[k] : t1[k]);
               if (idx < qcap) {
                 unsigned *it = qitems + (size_t)idx * kQWords;
                 it[0] = o[0] | (o[1] << 16);
@@ -644,6 +870,122 @@ __global__ void k_ctot_f(const uint16_t *ctot, const uint8_t *prior, int c, int 
   o[2] = make_float4(v[8], v[9], v[10], v[11]);
 }
 
+// The 4-cell layout's column groups are row-aligned: group k holds the
+// pairs (row, col0 + q), q < 8, of gtab[k] = row << 16 | col0; row r owns
+// ceil(r / 8) groups, rows 1 .. g-1 in order, and pairs with col0 + q >= row
+// are padding (as are whole groups past the last row: row 0xFFFF).  Groups
+// of the rows below r:
+__host__ __device__ constexpr int core_groups_before(int r) {
+  return r <= 1 ? 0 : 4 * ((r - 1) / 8) * ((r - 1) / 8 + 1) + ((r - 1) % 8) * ((r - 1) / 8 + 1);
+}
+static_assert(core_groups_before(9) == 8 && core_groups_before(10) == 10 &&
+                  core_groups_before(17) == 24,
+              "row-aligned group count");
+__global__ void k_core_groups(int g, int ngpad, uint32_t *gtab) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < ngpad && k >= core_groups_before(g)) gtab[k] = 0xFFFF0000u;
+  if (k >= 1 && k < g) {
+    const int b = core_groups_before(k);
+    for (int j = 0; j < (k + 7) / 8; j++) gtab[b + j] = ((uint32_t)k << 16) | (uint32_t)(8 * j);
+  }
+}
+
+// The 4-cell layout's Y: row (group*32 + 4q + 2a + b) = indicator over the
+// samples of pair q of the group having (x_row = a-1, x_col = b-1), a, b in
+// {0, 1}; padding pairs are zero.
+__global__ void k_build_y_core(const uint64_t *planes, const uint32_t *gtab, int W, int n_pad,
+                               int ngroups, uint8_t *Y) {
+  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;  // 16-sample chunk
+  const int chunks = n_pad / 16;
+  const long long rows = (long long)ngroups * 32;
+  if (idx >= rows * chunks) return;
+  const int rr = (int)(idx / chunks), ch = (int)(idx % chunks);
+  const uint32_t e = gtab[rr / 32];
+  const int row = (int)(e >> 16), col = (int)(e & 0xFFFFu) + (rr % 32) / 4;
+  const int a = (rr >> 1) & 1, b = rr & 1;
+  uint32_t bits = 0;
+  if (row != 0xFFFF && col < row) {
+    const int s0 = ch * 16;
+    const int w = s0 >> 6, sh = s0 & 63;
+    if (w < W) {
+      uint64_t x = planes[((size_t)row * 3 + a) * W + w] & planes[((size_t)col * 3 + b) * W + w];
+      bits = (uint32_t)(x >> sh) & 0xFFFFu;
+    }
+  }
+  uint8_t v[16];
+#pragma unroll
+  for (int k = 0; k < 16; k++) v[k] = ((bits >> k) & 1u) ? 0x38 : 0x00;
+  uint4 o;
+  memcpy(&o, v, 16);
+  *reinterpret_cast<uint4 *>(Y + (size_t)rr * n_pad + ch * 16) = o;
+}
+
+// The 4-cell layout's full-sample tables, one group per thread: 8 float4 of
+// the counted cells (0, 1, 3, 4 of the nine; zero for padding pairs), then
+// the prior bits of the group's pairs and three zero words (144 bytes).
+__global__ void k_ctot_core(const uint16_t *ctot, const uint8_t *prior, const uint32_t *gtab,
+                            int ngroups, float *out) {
+  const int grp = blockIdx.x * blockDim.x + threadIdx.x;
+  if (grp >= ngroups) return;
+  float4 *o = reinterpret_cast<float4 *>(out + (size_t)grp * (kGroupCtBytes / 4));
+  const int row = (int)(gtab[grp] >> 16), col0 = (int)(gtab[grp] & 0xFFFFu);
+  uint32_t pb = 0;
+  for (int q = 0; q < kCorePairs; q++) {
+    const int p = row * (row - 1) / 2 + col0 + q;
+    float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (row != 0xFFFF && col0 + q < row) {
+      const uint16_t *t = ctot + (size_t)p * 9;
+      v = make_float4((float)t[0], (float)t[1], (float)t[3], (float)t[4]);
+      if (prior[p]) pb |= 1u << q;
+    }
+    o[q] = v;
+  }
+  o[kCorePairs] = make_float4(__uint_as_float(pb), 0.f, 0.f, 0.f);
+}
+
+// Full-sample counts of each gene's states -1, 0, 1 (4-cell layout).
+__global__ void k_gene_counts(const uint64_t *planes, int g, int W, float4 *out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= g) return;
+  int cnt[3] = {0, 0, 0};
+  for (int a = 0; a < 3; a++)
+    for (int w = 0; w < W; w++) cnt[a] += __popcll(planes[((size_t)i * 3 + a) * W + w]);
+  out[i] = make_float4((float)cnt[0], (float)cnt[1], (float)cnt[2], 0.f);
+}
+
+// Class-1 counts of every gene's states -1 and 0 for each unit of a batch
+// (4-cell layout): margc[i * Bp + u] = count(-1) | count(0) << 16 over the
+// unit's class-1 samples, and nc1[u] = its class-1 sample count (units >= B
+// count nothing).  One thread per unit and kMargGenes genes per block row;
+// the mask word is read once for all of them.
+constexpr int kMargGenes = 8;
+__global__ void __launch_bounds__(128)
+    k_margins(const uint64_t *masks, const uint64_t *planes, int B, int Bp, int g, int W,
+              uint32_t *margc, float *nc1) {
+  const int u = blockIdx.x * blockDim.x + threadIdx.x;
+  const int i0 = blockIdx.y * kMargGenes;
+  if (u >= Bp) return;
+  int cnt[kMargGenes][2];
+#pragma unroll
+  for (int k = 0; k < kMargGenes; k++) cnt[k][0] = cnt[k][1] = 0;
+  int tot = 0;
+  for (int w = 0; w < W; w++) {
+    const uint64_t m = u < B ? masks[(size_t)u * W + w] : 0ull;
+    tot += __popcll(m);
+#pragma unroll
+    for (int k = 0; k < kMargGenes; k++) {
+      if (i0 + k < g) {
+        cnt[k][0] += __popcll(m & planes[((size_t)(i0 + k) * 3 + 0) * W + w]);
+        cnt[k][1] += __popcll(m & planes[((size_t)(i0 + k) * 3 + 1) * W + w]);
+      }
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < kMargGenes; k++)
+    if (i0 + k < g) margc[(size_t)(i0 + k) * Bp + u] = (uint32_t)cnt[k][0] | ((uint32_t)cnt[k][1] << 16);
+  if (blockIdx.y == 0) nc1[u] = (float)tot;
+}
+
 // A: row u = class-1 mask of unit u over the samples, e4m3 0/1; rows >= B zero.
 __global__ void k_masks_fp8(const uint64_t *masks, int B, int B_pad, int W, int n_pad, uint8_t *A) {
   const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -693,18 +1035,29 @@ static bool make_map(CUtensorMap *m, void *ptr, int cols, int rows, int box_rows
 }
 
 // pair groups of a set, and that count padded for every variant
-static int ngroups_of(int c) { return (c + kPairsPerGroup - 1) / kPairsPerGroup; }
-int mma_ngroups_pad(int c) {
-  const int g = ngroups_of(c);
+static int ngroups_of(const SetDev &sd, bool core) {
+  return core ? core_groups_before(sd.g) : (sd.c + kPairsPerGroup - 1) / kPairsPerGroup;
+}
+int mma_ngroups_pad(const SetDev &sd, bool core) {
+  const int g = ngroups_of(sd, core);
   return (g > 0 ? (g + kGroupPad - 1) / kGroupPad : 1) * kGroupPad;
 }
 int mma_npad(int n) { return (n + kKC - 1) / kKC * kKC; }
-// the operand Y, then the FP32 full-sample tables (a multiple of 128 bytes in)
-static size_t y_operand_bytes(int c, int n) {
-  return (size_t)mma_ngroups_pad(c) * 32 * mma_npad(n);
+// the operand Y, then the FP32 full-sample tables (a multiple of 128 bytes
+// in), then in the 4-cell layout the genes' full-sample state counts
+static size_t y_operand_bytes(const SetDev &sd) {
+  return (size_t)mma_ngroups_pad(sd, sd.core) * 32 * mma_npad(sd.n);
 }
-size_t mma_y_bytes(int c, int n) {
-  return y_operand_bytes(c, n) + (size_t)kGroupCtBytes * mma_ngroups_pad(c);
+static size_t gene_counts_offset(const SetDev &sd) {
+  return y_operand_bytes(sd) + (size_t)kGroupCtBytes * mma_ngroups_pad(sd, sd.core);
+}
+// (4-cell layout) then the column-group table
+static size_t group_table_offset(const SetDev &sd) {
+  return gene_counts_offset(sd) + sizeof(float4) * (size_t)sd.g;
+}
+size_t mma_y_bytes(const SetDev &sd) {
+  if (!sd.core) return gene_counts_offset(sd);
+  return group_table_offset(sd) + sizeof(uint32_t) * (size_t)mma_ngroups_pad(sd, true);
 }
 int mma_bpad(int B) { return (B + kTM - 1) / kTM * kTM; }
 static size_t a_operand_bytes(int B, int n) { return (size_t)mma_bpad(B) * mma_npad(n); }
@@ -723,45 +1076,74 @@ static unsigned queue_cap_used(int B, int c) {
   const long v = atol(e);
   return (v >= 1 && (unsigned long)v < cap) ? (unsigned)v : cap;
 }
-size_t mma_a_bytes(int B, int n, int c) {
-  // operand, queue header, items, then the list of exact decisions
-  return a_operand_bytes(B, n) + 16 + (size_t)queue_cap(B, c) * (kQWords + 1) * sizeof(uint32_t);
+// operand, queue header, items and the list of exact decisions, then (4-cell
+// layout, 256-byte aligned) the units' class counts [g][Bp] and class sizes
+static size_t margins_offset(int B, int n, int c) {
+  const size_t q = a_operand_bytes(B, n) + 16 + (size_t)queue_cap(B, c) * (kQWords + 1) * sizeof(uint32_t);
+  return (q + 255) & ~(size_t)255;
+}
+size_t mma_a_bytes(const SetDev &sd, int B) {
+  if (!sd.core)
+    return a_operand_bytes(B, sd.n) + 16 + (size_t)queue_cap(B, sd.c) * (kQWords + 1) * sizeof(uint32_t);
+  return margins_offset(B, sd.n, sd.c) + sizeof(uint32_t) * (size_t)mma_bpad(B) * (sd.g + 1);
 }
 
 cudaError_t launch_build_y(const SetDev &sd, uint8_t *Y, cudaStream_t st) {
-  const int ng = mma_ngroups_pad(sd.c), np = mma_npad(sd.n);
+  const int ng = mma_ngroups_pad(sd, sd.core), np = mma_npad(sd.n);
   const long long work = (long long)ng * 32 * (np / 16);
+  float *ctf = (float *)(Y + y_operand_bytes(sd));
+  if (sd.core) {
+    uint32_t *gtab = (uint32_t *)(Y + group_table_offset(sd));
+    const int nk = ng > sd.g ? ng : sd.g;
+    k_core_groups<<<(nk + 127) / 128, 128, 0, st>>>(sd.g, ng, gtab);
+    k_build_y_core<<<(unsigned)((work + 255) / 256), 256, 0, st>>>(sd.planes, gtab, sd.W, np, ng, Y);
+    k_ctot_core<<<(ng + 127) / 128, 128, 0, st>>>(sd.ctot, sd.prior, gtab, ng, ctf);
+    k_gene_counts<<<(sd.g + 127) / 128, 128, 0, st>>>(sd.planes, sd.g, sd.W,
+                                                     (float4 *)(Y + gene_counts_offset(sd)));
+    return cudaGetLastError();
+  }
   k_build_y<<<(unsigned)((work + 255) / 256), 256, 0, st>>>(sd.planes, sd.g, sd.W, sd.c, np, ng, Y);
   if (sd.c > 0) {
     const int cpad = ng * kPairsPerGroup;  // whole groups, the pad zero
-    k_ctot_f<<<(cpad + 255) / 256, 256, 0, st>>>(sd.ctot, sd.prior, sd.c, cpad,
-                                                  (float *)(Y + y_operand_bytes(sd.c, sd.n)));
+    k_ctot_f<<<(cpad + 255) / 256, 256, 0, st>>>(sd.ctot, sd.prior, sd.c, cpad, ctf);
   }
   return cudaGetLastError();
 }
+int mma_build_launches(const SetDev &sd) { return sd.core ? 4 : (sd.c > 0 ? 2 : 1); }
 
-template <int kStages, int kEpi, int kGroups>
+template <int kStages, int kEpi, int kGroups, bool kCore>
 static cudaError_t launch_variant(const SetDev &sd, const uint8_t *Afp8, const uint8_t *Y,
                                   unsigned *gqueue, unsigned qcap, int B, uint32_t *dmask,
                                   unsigned long long *stats, unsigned *err, int sms,
                                   cudaStream_t st) {
   constexpr int kTN = 32 * kGroups;
   const int np = mma_npad(sd.n), Bp = mma_bpad(B);
-  const int ng = ngroups_of(sd.c), nt = (ng + kGroups - 1) / kGroups;
+  const int ng = ngroups_of(sd, kCore), nt = (ng + kGroups - 1) / kGroups;
   CUtensorMap ma, mb;
   if (!make_map(&ma, (void *)Afp8, np, Bp, kTM) ||
-      !make_map(&mb, (void *)Y, np, mma_ngroups_pad(sd.c) * 32, kTN))
+      !make_map(&mb, (void *)Y, np, mma_ngroups_pad(sd, kCore) * 32, kTN))
     return cudaErrorNotSupported;
   const int mblocks = Bp / kTM;
-  const float *ctotf = (const float *)(Y + y_operand_bytes(sd.c, sd.n));
-  const size_t smem = 1024 + (size_t)kStages * (kTM + kTN) * kKC + kBarBytes;
-  auto kern = k_pairs_mma<kStages, kEpi, kGroups>;
+  const float *ctotf = (const float *)(Y + y_operand_bytes(sd));
+  const uint32_t *margc = nullptr;
+  const float *nc1 = nullptr;
+  const float4 *gcnt = nullptr;
+  const uint32_t *gtab = nullptr;
+  if (kCore) {
+    margc = (const uint32_t *)(Afp8 + margins_offset(B, sd.n, sd.c));
+    nc1 = (const float *)(margc + (size_t)Bp * sd.g);
+    gcnt = (const float4 *)(Y + gene_counts_offset(sd));
+    gtab = (const uint32_t *)(Y + group_table_offset(sd));
+  }
+  const size_t smem = 1024 + (size_t)kStages * (kTM + kTN) * kKC + kBarBytes +
+                      (kCore ? sizeof(float4) * (size_t)sd.g : 0);
+  auto kern = k_pairs_mma<kStages, kEpi, kGroups, kCore>;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   const int ntot = nt * mblocks;
   const int grid = ntot < sms ? ntot : sms;
   kern<<<grid, 32 * (2 + kEpi), smem, st>>>(ma, mb, sd, ctotf, B, np / kKC, nt, mblocks,
-                                            stats, err, gqueue, qcap);
+                                            stats, err, gqueue, qcap, margc, nc1, gcnt, gtab);
   e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   k_general<<<sms * 8, 256, 0, st>>>(sd, gqueue, qcap, B, dmask, stats, err);
@@ -774,6 +1156,27 @@ static cudaError_t launch_variant(const SetDev &sd, const uint8_t *Afp8, const u
 // 0: N=128, 16 epilogue warps; 1: N=128, 8 warps; 2: N=192, 12 warps;
 // 3: N=256, 8 warps; 4: N=256, 16 warps (ring depths fill the shared memory)
 int mma_variants() { return 5; }
+// operand (and class counts), GEMM + epilogue, general path, exact path
+int mma_launches(const SetDev &sd) { return sd.core ? 5 : 4; }
+
+template <bool kCore>
+static cudaError_t launch_shape(const SetDev &sd, uint8_t *Afp8, const uint8_t *Y,
+                                unsigned *gqueue, unsigned qcap, int B, uint32_t *dmask,
+                                unsigned long long *stats, unsigned *err, int sms,
+                                cudaStream_t st, int variant) {
+  switch (variant) {
+    case 1:
+      return launch_variant<6, 8, 4, kCore>(sd, Afp8, Y, gqueue, qcap, B, dmask, stats, err, sms, st);
+    case 2:
+      return launch_variant<5, 12, 6, kCore>(sd, Afp8, Y, gqueue, qcap, B, dmask, stats, err, sms, st);
+    case 3:
+      return launch_variant<4, 8, 8, kCore>(sd, Afp8, Y, gqueue, qcap, B, dmask, stats, err, sms, st);
+    case 4:
+      return launch_variant<4, 16, 8, kCore>(sd, Afp8, Y, gqueue, qcap, B, dmask, stats, err, sms, st);
+    default:
+      return launch_variant<6, 16, 4, kCore>(sd, Afp8, Y, gqueue, qcap, B, dmask, stats, err, sms, st);
+  }
+}
 
 cudaError_t launch_pairs_mma(const SetDev &sd, const uint64_t *masks, int B, uint8_t *Afp8,
                              const uint8_t *Y, uint32_t *dmask, unsigned long long *stats,
@@ -781,22 +1184,19 @@ cudaError_t launch_pairs_mma(const SetDev &sd, const uint64_t *masks, int B, uin
   const int np = mma_npad(sd.n), Bp = mma_bpad(B);
   const long long work = (long long)Bp * (np / 16);
   k_masks_fp8<<<(unsigned)((work + 255) / 256), 256, 0, st>>>(masks, B, Bp, sd.W, np, Afp8);
+  if (sd.core) {
+    uint32_t *margc = (uint32_t *)(Afp8 + margins_offset(B, sd.n, sd.c));
+    const dim3 grid((unsigned)(Bp / 128), (unsigned)((sd.g + kMargGenes - 1) / kMargGenes));
+    k_margins<<<grid, 128, 0, st>>>(masks, sd.planes, B, Bp, sd.g, sd.W, margc,
+                                    (float *)(margc + (size_t)Bp * sd.g));
+  }
   unsigned *gqueue = reinterpret_cast<unsigned *>(Afp8 + a_operand_bytes(B, sd.n));
   const unsigned qcap = queue_cap_used(B, sd.c);
   cudaError_t e = cudaMemsetAsync(gqueue, 0, 16, st);
   if (e != cudaSuccess) return e;
-  switch (variant) {
-    case 1:
-      return launch_variant<6, 8, 4>(sd, Afp8, Y, gqueue, qcap, B, dmask, stats, err, sms, st);
-    case 2:
-      return launch_variant<5, 12, 6>(sd, Afp8, Y, gqueue, qcap, B, dmask, stats, err, sms, st);
-    case 3:
-      return launch_variant<4, 8, 8>(sd, Afp8, Y, gqueue, qcap, B, dmask, stats, err, sms, st);
-    case 4:
-      return launch_variant<4, 16, 8>(sd, Afp8, Y, gqueue, qcap, B, dmask, stats, err, sms, st);
-    default:
-      return launch_variant<6, 16, 4>(sd, Afp8, Y, gqueue, qcap, B, dmask, stats, err, sms, st);
-  }
+  if (sd.core)
+    return launch_shape<true>(sd, Afp8, Y, gqueue, qcap, B, dmask, stats, err, sms, st, variant);
+  return launch_shape<false>(sd, Afp8, Y, gqueue, qcap, B, dmask, stats, err, sms, st, variant);
 }
 
 }  // namespace eddy
