@@ -93,7 +93,6 @@ __device__ __forceinline__ void philox10(uint32_t c[4], uint32_t k0, uint32_t k1
 
 // One block per unit.  key(s) = Philox(ctr = (s, perm, set, 0), key = seed)
 // word 0; the nA samples with the smallest (key, s) are class 1.
-// Bitonic sort of the padded (key << 32 | s) array in shared memory.
 __global__ void __launch_bounds__(128) k_counter_masks(int n, int nA, int W, uint64_t seed,
                                                        const int32_t *unit_set,
                                                        const int32_t *unit_perm,
