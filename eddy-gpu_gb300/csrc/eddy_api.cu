@@ -124,11 +124,12 @@ struct eddy_ctx {
   PinnedBuf h_stage;          // per-batch indices and results
   PinnedBuf h_vals;           // the resident set's values on their way in
   int sms = 148;
-  // autotuned contingency-kernel variant per (n, power of two of the pair
-  // count); tuned_variant: the last one used (-1 = none yet)
+  // autotuned contingency-kernel choice (layout and tile shape) per (n,
+  // power of two of the pair count); tuned_variant: the last one used (-1 =
+  // none yet)
   std::map<std::pair<int, int>, int> tuned;
   int tuned_variant = -1;
-  float tuned_ms[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  float tuned_ms[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
   // decision thresholds per gene-set size (the Bonferroni factor)
   struct ThrSet {
     Thr t[2][kDofSlots];
@@ -311,26 +312,56 @@ bool use_popc() {
   return e && strcmp(e, "popc") == 0;
 }
 
-// autotuning key: samples and the power of two of the pair count (sets of
-// similar size share a tile shape)
+
+// Contingency-kernel choices for a batch: tile shape v % mma_variants(), in
+// the 4-cell layout when v >= mma_variants() and in the 9-cell layout
+// otherwise.  The 4-cell layout is offered to sets that allow it (sd.core)
+// from kCoreMinPairs pairs on, in its two shapes with 12 and 16 epilogue
+// warps: on smaller sets its 2.67x wider tiles leave SMs idle (measured on
+// sets of 30-150 genes), and with fewer warps its epilogue stalls.  Each
+// choice costs one timed run of the tuning batch per (samples, pair-count
+// class), which workloads of many small sets pay many times.
+constexpr int kCoreMinPairs = 8192;
+int choices(const SetDev &sd, int *v) {
+  const int nv = mma_variants();
+  int k = 0;
+  if (sd.core && sd.c >= kCoreMinPairs) {
+    v[k++] = nv + 4;
+    v[k++] = nv + 2;
+  }
+  for (int i = nv - 1; i >= 0; i--) v[k++] = i;
+  return k;
+}
+// autotuning key: samples, the power of two of the pair count (sets of
+// similar size share a choice) and whether the 4-cell layout is on offer
+// (a set with missing values must never take a choice tuned without them)
 std::pair<int, int> tune_key(const SetDev &sd) {
   int lc = 0;
   while ((1 << lc) < sd.c) lc++;
-  return {sd.n, lc};
+  return {sd.n, 2 * lc + (sd.core && sd.c >= kCoreMinPairs ? 1 : 0)};
+}
+SetDev layout_of(const SetDev &sd, int v) {
+  SetDev l = sd;
+  l.core = v >= mma_variants() ? 1 : 0;
+  return l;
 }
 
-// Tile variant for a batch of B units: pinned by EDDY_MMA_VARIANT, tuned
-// for the set's shape, or -1 when this batch is to tune (B >= 512).
+// Choice for a batch of B units: the tile shape pinned by EDDY_MMA_VARIANT
+// (in the set's own layout), the one tuned for the set's shape, or -1 when
+// this batch is to tune (B >= 512).  The 4-cell layout wins on large sets;
+// on small ones its 2.67x wider tiles leave SMs idle.
 int pick_variant(eddy_ctx *ctx, const SetDev &sd, int B) {
+  const int nv = mma_variants();
   const char *ev = getenv("EDDY_MMA_VARIANT");
-  if (ev) return atoi(ev) % mma_variants();
+  if (ev) return (sd.core ? nv : 0) + atoi(ev) % nv;
   auto it = ctx->tuned.find(tune_key(sd));
   if (it != ctx->tuned.end()) return it->second;
   if (B >= 512) return -1;
-  // untuned small batch: the tile shape that measured fastest on 200 x 1000
-  // sets (9-cell layout: N = 256 with 8 epilogue warps; 4-cell layout, whose
-  // epilogue decides 8 pairs per column group: N = 192 with 12)
-  return (sd.core ? 2 : 3) % mma_variants();
+  // untuned small batch: what measured fastest on sets of 39 and of 200
+  // genes (4-cell layout from kCoreMinPairs pairs: N = 192 with 12 epilogue
+  // warps; else the 9-cell layout: N = 256 with 8)
+  if (sd.core && sd.c >= kCoreMinPairs) return nv + 2 % nv;
+  return 3 % nv;
 }
 
 // Buffers of the tensor-core path for a batch of B units (and the set's Y
@@ -367,21 +398,27 @@ int launch_pairs_any(eddy_ctx *ctx, const SetDev &sd, const uint64_t *masks, int
     ctx->launches += 1;
     return EDDY_OK;
   }
-  {
-    int rc = prepare_pairs(ctx, sd, B);
-    if (rc) return rc;
-  }
+  CK(ctx->d_err.ensure(sizeof(unsigned)));
   CK(cudaMemsetAsync(ctx->d_err.p, 0, sizeof(unsigned), ctx->stream));
   int variant = pick_variant(ctx, sd, B);
   if (variant < 0) {
-    // autotune on this batch: time every variant once (same results), keep
+    // autotune on this batch: time every choice once (same results), keep
     // the fastest for this (g, n); the last run leaves dmask filled
     float best = 1e30f;
     int bi = 0;
-    for (int v = mma_variants() - 1; v >= 0; v--) {
+    int cand[16];
+    const int ncand = choices(sd, cand);
+    for (int ci = 0; ci < ncand; ci++) {
+      const int v = cand[ci];
+      const SetDev sv = layout_of(sd, v);
+      {
+        int rc = prepare_pairs(ctx, sv, B);  // (re)builds Y for the layout
+        if (rc) return rc;
+      }
       CK(cudaEventRecord(ctx->ev[2], ctx->stream));
-      CK(launch_pairs_mma(sd, masks, B, ctx->d_afp8.as<uint8_t>(), ctx->d_Y.as<uint8_t>(), dmask,
-                          nullptr, ctx->d_err.as<unsigned>(), ctx->sms, ctx->stream, v));
+      CK(launch_pairs_mma(sv, masks, B, ctx->d_afp8.as<uint8_t>(), ctx->d_Y.as<uint8_t>(), dmask,
+                          nullptr, ctx->d_err.as<unsigned>(), ctx->sms, ctx->stream,
+                          v % mma_variants()));
       CK(cudaEventRecord(ctx->ev[3], ctx->stream));
       CK(cudaEventSynchronize(ctx->ev[3]));
       float ms = 0;
@@ -391,15 +428,20 @@ int launch_pairs_any(eddy_ctx *ctx, const SetDev &sd, const uint64_t *masks, int
         best = ms;
         bi = v;
       }
-      ctx->launches += mma_launches(sd);
+      ctx->launches += mma_launches(sv);
     }
     ctx->tuned[tune_key(sd)] = bi;
     variant = bi;
   }
   ctx->tuned_variant = variant;
-  CK(launch_pairs_mma(sd, masks, B, ctx->d_afp8.as<uint8_t>(), ctx->d_Y.as<uint8_t>(), dmask, stats,
-                      ctx->d_err.as<unsigned>(), ctx->sms, ctx->stream, variant));
-  ctx->launches += mma_launches(sd);
+  const SetDev sv = layout_of(sd, variant);
+  {
+    int rc = prepare_pairs(ctx, sv, B);
+    if (rc) return rc;
+  }
+  CK(launch_pairs_mma(sv, masks, B, ctx->d_afp8.as<uint8_t>(), ctx->d_Y.as<uint8_t>(), dmask, stats,
+                      ctx->d_err.as<unsigned>(), ctx->sms, ctx->stream, variant % mma_variants()));
+  ctx->launches += mma_launches(sv);
   return EDDY_OK;
 }
 
@@ -545,7 +587,7 @@ int run_units(eddy_ctx *ctx, SetRun &sr, int nunits, const uint64_t *masks_host,
       ctx->dmask_clean = nullptr;  // until the batch is seen to finish
       if (graphable) {
         {
-          int rc = prepare_pairs(ctx, sd, Bt);
+          int rc = prepare_pairs(ctx, layout_of(sd, pick_variant(ctx, sd, Bt)), Bt);
           if (rc) return rc;
         }
         // everything a replay bakes in: the set, its state, the batch shape

@@ -315,13 +315,13 @@ __device__ __forceinline__ f32x2 f2_pack(float x, float y) {
   return r;
 }
 __device__ __forceinline__ float f2_x(f32x2 v) {
-  float x, y;
-  asm("mov.b64 {%0, %1}, %2;" : "=f"(x), "=f"(y) : "l"(v));
+  float x;
+  asm("{.reg .f32 t; mov.b64 {%0, t}, %1;}" : "=f"(x) : "l"(v));
   return x;
 }
 __device__ __forceinline__ float f2_y(f32x2 v) {
-  float x, y;
-  asm("mov.b64 {%0, %1}, %2;" : "=f"(x), "=f"(y) : "l"(v));
+  float y;
+  asm("{.reg .f32 t; mov.b64 {t, %0}, %1;}" : "=f"(y) : "l"(v));
   return y;
 }
 __device__ __forceinline__ f32x2 f2_add(f32x2 a, f32x2 b) {

@@ -819,46 +819,49 @@ __global__ void __launch_bounds__(32) k_exact(const __grid_constant__ SetDev sd,
 }
 
 // -------------------------------------------------------------- operands
-// Y: row (group*32 + q*9 + 3a + b), q < 3 = indicator over the samples of
-// pair group*3 + q having (x_row = a-1, x_col = b-1); e4m3 1.0 = 0x38; rows
-// 27..31 of each group and out-of-range pairs are zero.  A tile of any
-// variant is a run of whole groups.
-__global__ void k_build_y(const uint64_t *planes, int g, int W, int c, int n_pad, int ngroups,
-                          uint8_t *Y) {
-  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;  // 16-sample chunk
-  const int chunks = n_pad / 16;
-  const long long rows = (long long)ngroups * 32;
-  if (idx >= rows * chunks) return;
-  const int rr = (int)(idx / chunks), ch = (int)(idx % chunks);
-  const int grp = rr / 32, r32 = rr % 32;
-  const int q = r32 / 9, cell = r32 % 9;
-  const int p = grp * kPairsPerGroup + q;
+// 16 samples of an indicator row as e4m3 0/1 (1.0 = 0x38)
+__device__ __forceinline__ void store_e4m3_16(uint8_t *dst, uint32_t bits) {
   uint8_t v[16];
-  uint32_t bits = 0;
-  if (r32 < kPairsPerGroup * 9 && p < c) {
-    int row, col;
-    pair_rc(p, row, col);
-    const int a = cell / 3, b = cell % 3;
-    const int s0 = ch * 16;
-    const int w = s0 >> 6, sh = s0 & 63;
-    if (w < W) {
-      uint64_t x = planes[((size_t)row * 3 + a) * W + w] & planes[((size_t)col * 3 + b) * W + w];
-      bits = (uint32_t)(x >> sh) & 0xFFFFu;
-    }
-  }
 #pragma unroll
   for (int k = 0; k < 16; k++) v[k] = ((bits >> k) & 1u) ? 0x38 : 0x00;
   uint4 o;
   memcpy(&o, v, 16);
-  *reinterpret_cast<uint4 *>(Y + (size_t)rr * n_pad + ch * 16) = o;
+  *reinterpret_cast<uint4 *>(dst) = o;
+}
+// samples [16 ch, 16 ch + 16) of plane(row, a) & plane(col, b)
+__device__ __forceinline__ uint32_t pair_bits16(const uint64_t *planes, int W, int row, int a,
+                                                int col, int b, int ch) {
+  const int s0 = ch * 16, w = s0 >> 6, sh = s0 & 63;
+  if (w >= W) return 0u;
+  const uint64_t x = planes[((size_t)row * 3 + a) * W + w] & planes[((size_t)col * 3 + b) * W + w];
+  return (uint32_t)(x >> sh) & 0xFFFFu;
 }
 
-// Full-sample tables as FP32 for the epilogue: pair p -> 12 floats (nine
-// counts, the prior flag, two pad), 48 bytes, float4-aligned; pairs past c
-// up to whole tiles are zero.
-__global__ void k_ctot_f(const uint16_t *ctot, const uint8_t *prior, int c, int cpad, float *out) {
-  const int p = blockIdx.x * blockDim.x + threadIdx.x;
-  if (p >= cpad) return;
+// 9-cell Y: row (group*32 + q*9 + 3a + b), q < 3 = indicator over the
+// samples of pair group*3 + q having (x_row = a-1, x_col = b-1); rows 27..31
+// of each group and out-of-range pairs are zero.  A tile of any variant is
+// a run of whole groups.  Work item = one 16-sample chunk of one row.
+__device__ __forceinline__ void build_y_chunk(const uint64_t *planes, int W, int c, int n_pad,
+                                              long long idx, uint8_t *Y) {
+  const int chunks = n_pad / 16;
+  const int rr = (int)(idx / chunks), ch = (int)(idx % chunks);
+  const int grp = rr / 32, r32 = rr % 32;
+  const int q = r32 / 9, cell = r32 % 9;
+  const int p = grp * kPairsPerGroup + q;
+  uint32_t bits = 0;
+  if (r32 < kPairsPerGroup * 9 && p < c) {
+    int row, col;
+    pair_rc(p, row, col);
+    bits = pair_bits16(planes, W, row, cell / 3, col, cell % 3, ch);
+  }
+  store_e4m3_16(Y + (size_t)rr * n_pad + ch * 16, bits);
+}
+
+// 9-cell full-sample tables as FP32 for the epilogue: pair p -> 12 floats
+// (nine counts, the prior flag, two pad), 48 bytes, float4-aligned; pairs
+// past c up to whole groups are zero.
+__device__ __forceinline__ void ctot_f_pair(const uint16_t *ctot, const uint8_t *prior, int c,
+                                            int p, float *out) {
   float v[12];
 #pragma unroll
   for (int k = 0; k < 9; k++) v[k] = p < c ? (float)ctot[(size_t)p * 9 + k] : 0.f;
@@ -871,7 +874,7 @@ __global__ void k_ctot_f(const uint16_t *ctot, const uint8_t *prior, int c, int 
 }
 
 // The 4-cell layout's column groups are row-aligned: group k holds the
-// pairs (row, col0 + q), q < 8, of gtab[k] = row << 16 | col0; row r owns
+// pairs (row, col0 + q), q < 8, of entry k = row << 16 | col0; row r owns
 // ceil(r / 8) groups, rows 1 .. g-1 in order, and pairs with col0 + q >= row
 // are padding (as are whole groups past the last row: row 0xFFFF).  Groups
 // of the rows below r:
@@ -881,59 +884,44 @@ __host__ __device__ constexpr int core_groups_before(int r) {
 static_assert(core_groups_before(9) == 8 && core_groups_before(10) == 10 &&
                   core_groups_before(17) == 24,
               "row-aligned group count");
-__global__ void k_core_groups(int g, int ngpad, uint32_t *gtab) {
-  const int k = blockIdx.x * blockDim.x + threadIdx.x;
-  if (k < ngpad && k >= core_groups_before(g)) gtab[k] = 0xFFFF0000u;
-  if (k >= 1 && k < g) {
-    const int b = core_groups_before(k);
-    for (int j = 0; j < (k + 7) / 8; j++) gtab[b + j] = ((uint32_t)k << 16) | (uint32_t)(8 * j);
+__device__ __forceinline__ uint32_t core_group_entry(int k, int g) {
+  if (k >= core_groups_before(g)) return 0xFFFF0000u;
+  int lo = 1, hi = g - 1;  // the row r with groups_before(r) <= k < groups_before(r + 1)
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (core_groups_before(mid) <= k) lo = mid;
+    else hi = mid - 1;
   }
+  return ((uint32_t)lo << 16) | (uint32_t)(8 * (k - core_groups_before(lo)));
 }
 
-// The 4-cell layout's Y: row (group*32 + 4q + 2a + b) = indicator over the
-// samples of pair q of the group having (x_row = a-1, x_col = b-1), a, b in
-// {0, 1}; padding pairs are zero.
-__global__ void k_build_y_core(const uint64_t *planes, const uint32_t *gtab, int W, int n_pad,
-                               int ngroups, uint8_t *Y) {
-  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;  // 16-sample chunk
+// 4-cell Y: row (group*32 + 4q + 2a + b) = indicator over the samples of
+// pair q of the group having (x_row = a-1, x_col = b-1), a, b in {0, 1};
+// padding pairs are zero.
+__device__ __forceinline__ void build_y_core_chunk(const uint64_t *planes, int g, int W, int n_pad,
+                                                   long long idx, uint8_t *Y) {
   const int chunks = n_pad / 16;
-  const long long rows = (long long)ngroups * 32;
-  if (idx >= rows * chunks) return;
   const int rr = (int)(idx / chunks), ch = (int)(idx % chunks);
-  const uint32_t e = gtab[rr / 32];
+  const uint32_t e = core_group_entry(rr / 32, g);
   const int row = (int)(e >> 16), col = (int)(e & 0xFFFFu) + (rr % 32) / 4;
-  const int a = (rr >> 1) & 1, b = rr & 1;
   uint32_t bits = 0;
-  if (row != 0xFFFF && col < row) {
-    const int s0 = ch * 16;
-    const int w = s0 >> 6, sh = s0 & 63;
-    if (w < W) {
-      uint64_t x = planes[((size_t)row * 3 + a) * W + w] & planes[((size_t)col * 3 + b) * W + w];
-      bits = (uint32_t)(x >> sh) & 0xFFFFu;
-    }
-  }
-  uint8_t v[16];
-#pragma unroll
-  for (int k = 0; k < 16; k++) v[k] = ((bits >> k) & 1u) ? 0x38 : 0x00;
-  uint4 o;
-  memcpy(&o, v, 16);
-  *reinterpret_cast<uint4 *>(Y + (size_t)rr * n_pad + ch * 16) = o;
+  if (row != 0xFFFF && col < row) bits = pair_bits16(planes, W, row, (rr >> 1) & 1, col, rr & 1, ch);
+  store_e4m3_16(Y + (size_t)rr * n_pad + ch * 16, bits);
 }
 
-// The 4-cell layout's full-sample tables, one group per thread: 8 float4 of
-// the counted cells (0, 1, 3, 4 of the nine; zero for padding pairs), then
-// the prior bits of the group's pairs and three zero words (144 bytes).
-__global__ void k_ctot_core(const uint16_t *ctot, const uint8_t *prior, const uint32_t *gtab,
-                            int ngroups, float *out) {
-  const int grp = blockIdx.x * blockDim.x + threadIdx.x;
-  if (grp >= ngroups) return;
+// 4-cell full-sample tables, one group: 8 float4 of the counted cells (0, 1,
+// 3, 4 of the nine; zero for padding pairs), then the prior bits of the
+// group's pairs and three zero words (144 bytes).
+__device__ __forceinline__ void ctot_core_group(const uint16_t *ctot, const uint8_t *prior, int g,
+                                                int grp, float *out) {
   float4 *o = reinterpret_cast<float4 *>(out + (size_t)grp * (kGroupCtBytes / 4));
-  const int row = (int)(gtab[grp] >> 16), col0 = (int)(gtab[grp] & 0xFFFFu);
+  const uint32_t e = core_group_entry(grp, g);
+  const int row = (int)(e >> 16), col0 = (int)(e & 0xFFFFu);
   uint32_t pb = 0;
   for (int q = 0; q < kCorePairs; q++) {
-    const int p = row * (row - 1) / 2 + col0 + q;
     float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
     if (row != 0xFFFF && col0 + q < row) {
+      const int p = row * (row - 1) / 2 + col0 + q;
       const uint16_t *t = ctot + (size_t)p * 9;
       v = make_float4((float)t[0], (float)t[1], (float)t[3], (float)t[4]);
       if (prior[p]) pb |= 1u << q;
@@ -943,28 +931,72 @@ __global__ void k_ctot_core(const uint16_t *ctot, const uint8_t *prior, const ui
   o[kCorePairs] = make_float4(__uint_as_float(pb), 0.f, 0.f, 0.f);
 }
 
-// Full-sample counts of each gene's states -1, 0, 1 (4-cell layout).
-__global__ void k_gene_counts(const uint64_t *planes, int g, int W, float4 *out) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= g) return;
+// Full-sample counts of gene i's states -1, 0, 1 (4-cell layout).
+__device__ __forceinline__ void gene_counts(const uint64_t *planes, int W, int i, float4 *out) {
   int cnt[3] = {0, 0, 0};
   for (int a = 0; a < 3; a++)
     for (int w = 0; w < W; w++) cnt[a] += __popcll(planes[((size_t)i * 3 + a) * W + w]);
   out[i] = make_float4((float)cnt[0], (float)cnt[1], (float)cnt[2], 0.f);
 }
 
-// Class-1 counts of every gene's states -1 and 0 for each unit of a batch
-// (4-cell layout): margc[i * Bp + u] = count(-1) | count(0) << 16 over the
-// unit's class-1 samples, and nc1[u] = its class-1 sample count (units >= B
-// count nothing).  One thread per unit and kMargGenes genes per block row;
-// the mask word is read once for all of them.
+// The per-set operands in one launch of 128-thread blocks: blocks [0, b[0])
+// build Y, [b[0], b[1]) the FP32 tables and, in the 4-cell layout,
+// [b[1], b[2]) the group table and [b[2], b[3]) the genes' counts.
+struct SetupArgs {
+  const uint64_t *planes;
+  const uint16_t *ctot;
+  const uint8_t *prior;
+  int g, W, c, n_pad, ngroups, core;
+  int b[4];
+  uint8_t *Y;
+  float *ctf;
+  uint32_t *gtab;
+  float4 *gcnt;
+};
+__global__ void __launch_bounds__(128) k_setup(const __grid_constant__ SetupArgs a) {
+  const int blk = blockIdx.x;
+  if (blk < a.b[0]) {
+    const long long idx = (long long)blk * 128 + threadIdx.x;
+    if (idx >= (long long)a.ngroups * 32 * (a.n_pad / 16)) return;
+    if (a.core) build_y_core_chunk(a.planes, a.g, a.W, a.n_pad, idx, a.Y);
+    else build_y_chunk(a.planes, a.W, a.c, a.n_pad, idx, a.Y);
+  } else if (blk < a.b[1]) {
+    const int i = (blk - a.b[0]) * 128 + threadIdx.x;
+    if (a.core) {
+      if (i < a.ngroups) ctot_core_group(a.ctot, a.prior, a.g, i, a.ctf);
+    } else if (i < a.ngroups * kPairsPerGroup) {
+      ctot_f_pair(a.ctot, a.prior, a.c, i, a.ctf);
+    }
+  } else if (blk < a.b[2]) {
+    const int k = (blk - a.b[1]) * 128 + threadIdx.x;
+    if (k < a.ngroups) a.gtab[k] = core_group_entry(k, a.g);
+  } else if (blk < a.b[3]) {
+    const int i = (blk - a.b[2]) * 128 + threadIdx.x;
+    if (i < a.g) gene_counts(a.planes, a.W, i, a.gcnt);
+  }
+}
+
+// A: row u = class-1 mask of unit u over the samples, e4m3 0/1; rows >= B
+// zero.  Work item = one 16-sample chunk of one row.
+__device__ __forceinline__ void masks_fp8_chunk(const uint64_t *masks, int B, int W, int n_pad,
+                                                long long idx, uint8_t *A) {
+  const int chunks = n_pad / 16;
+  const int u = (int)(idx / chunks), ch = (int)(idx % chunks);
+  uint32_t bits = 0;
+  const int s0 = ch * 16, w = s0 >> 6, sh = s0 & 63;
+  if (u < B && w < W) bits = (uint32_t)(masks[(size_t)u * W + w] >> sh) & 0xFFFFu;
+  store_e4m3_16(A + (size_t)u * n_pad + ch * 16, bits);
+}
+
+// Class-1 counts of kMargGenes genes' states -1 and 0 for unit u (4-cell
+// layout): margc[i * Bp + u] = count(-1) | count(0) << 16 over the unit's
+// class-1 samples, and (for the first gene block) nc1[u] = its class-1
+// sample count; units >= B count nothing.  The mask word is read once for
+// all the genes.
 constexpr int kMargGenes = 8;
-__global__ void __launch_bounds__(128)
-    k_margins(const uint64_t *masks, const uint64_t *planes, int B, int Bp, int g, int W,
-              uint32_t *margc, float *nc1) {
-  const int u = blockIdx.x * blockDim.x + threadIdx.x;
-  const int i0 = blockIdx.y * kMargGenes;
-  if (u >= Bp) return;
+__device__ __forceinline__ void margins_unit(const uint64_t *masks, const uint64_t *planes, int B,
+                                             int Bp, int g, int W, int u, int i0, uint32_t *margc,
+                                             float *nc1) {
   int cnt[kMargGenes][2];
 #pragma unroll
   for (int k = 0; k < kMargGenes; k++) cnt[k][0] = cnt[k][1] = 0;
@@ -983,24 +1015,25 @@ __global__ void __launch_bounds__(128)
 #pragma unroll
   for (int k = 0; k < kMargGenes; k++)
     if (i0 + k < g) margc[(size_t)(i0 + k) * Bp + u] = (uint32_t)cnt[k][0] | ((uint32_t)cnt[k][1] << 16);
-  if (blockIdx.y == 0) nc1[u] = (float)tot;
+  if (i0 == 0) nc1[u] = (float)tot;
 }
 
-// A: row u = class-1 mask of unit u over the samples, e4m3 0/1; rows >= B zero.
-__global__ void k_masks_fp8(const uint64_t *masks, int B, int B_pad, int W, int n_pad, uint8_t *A) {
-  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  const int chunks = n_pad / 16;
-  if (idx >= (long long)B_pad * chunks) return;
-  const int u = (int)(idx / chunks), ch = (int)(idx % chunks);
-  uint32_t bits = 0;
-  const int s0 = ch * 16, w = s0 >> 6, sh = s0 & 63;
-  if (u < B && w < W) bits = (uint32_t)(masks[(size_t)u * W + w] >> sh) & 0xFFFFu;
-  uint8_t v[16];
-#pragma unroll
-  for (int k = 0; k < 16; k++) v[k] = ((bits >> k) & 1u) ? 0x38 : 0x00;
-  uint4 o;
-  memcpy(&o, v, 16);
-  *reinterpret_cast<uint4 *>(A + (size_t)u * n_pad + ch * 16) = o;
+// The per-batch operands in one launch of 128-thread blocks: blocks
+// [0, bA) the A operand, then (4-cell layout) Bp / 128 x ceil(g / 8) blocks
+// of class counts; block 0 also zeroes the general-path queue's header.
+__global__ void __launch_bounds__(128)
+    k_operands(const uint64_t *masks, const uint64_t *planes, int B, int Bp, int g, int W,
+               int n_pad, int bA, uint8_t *A, uint32_t *margc, float *nc1, unsigned *gqueue) {
+  const int blk = blockIdx.x;
+  if (blk == 0 && threadIdx.x < 4) gqueue[threadIdx.x] = 0u;  // the queue header
+  if (blk < bA) {
+    const long long idx = (long long)blk * 128 + threadIdx.x;
+    if (idx < (long long)Bp * (n_pad / 16)) masks_fp8_chunk(masks, B, W, n_pad, idx, A);
+    return;
+  }
+  const int ub = Bp / 128, m = blk - bA;
+  const int u = (m % ub) * 128 + threadIdx.x, i0 = (m / ub) * kMargGenes;
+  margins_unit(masks, planes, B, Bp, g, W, u, i0, margc, nc1);
 }
 
 // ------------------------------------------------------------ host side
@@ -1091,25 +1124,32 @@ size_t mma_a_bytes(const SetDev &sd, int B) {
 cudaError_t launch_build_y(const SetDev &sd, uint8_t *Y, cudaStream_t st) {
   const int ng = mma_ngroups_pad(sd, sd.core), np = mma_npad(sd.n);
   const long long work = (long long)ng * 32 * (np / 16);
-  float *ctf = (float *)(Y + y_operand_bytes(sd));
+  SetupArgs a{};
+  a.planes = sd.planes;
+  a.ctot = sd.ctot;
+  a.prior = sd.prior;
+  a.g = sd.g;
+  a.W = sd.W;
+  a.c = sd.c;
+  a.n_pad = np;
+  a.ngroups = ng;
+  a.core = sd.core;
+  a.Y = Y;
+  a.ctf = (float *)(Y + y_operand_bytes(sd));
+  a.b[0] = (int)((work + 127) / 128);
+  a.b[1] = a.b[0] + (sd.core ? (ng + 127) / 128 : (ng * kPairsPerGroup + 127) / 128);
+  a.b[2] = a.b[1];
+  a.b[3] = a.b[1];
   if (sd.core) {
-    uint32_t *gtab = (uint32_t *)(Y + group_table_offset(sd));
-    const int nk = ng > sd.g ? ng : sd.g;
-    k_core_groups<<<(nk + 127) / 128, 128, 0, st>>>(sd.g, ng, gtab);
-    k_build_y_core<<<(unsigned)((work + 255) / 256), 256, 0, st>>>(sd.planes, gtab, sd.W, np, ng, Y);
-    k_ctot_core<<<(ng + 127) / 128, 128, 0, st>>>(sd.ctot, sd.prior, gtab, ng, ctf);
-    k_gene_counts<<<(sd.g + 127) / 128, 128, 0, st>>>(sd.planes, sd.g, sd.W,
-                                                     (float4 *)(Y + gene_counts_offset(sd)));
-    return cudaGetLastError();
+    a.gtab = (uint32_t *)(Y + group_table_offset(sd));
+    a.gcnt = (float4 *)(Y + gene_counts_offset(sd));
+    a.b[2] = a.b[1] + (ng + 127) / 128;
+    a.b[3] = a.b[2] + (sd.g + 127) / 128;
   }
-  k_build_y<<<(unsigned)((work + 255) / 256), 256, 0, st>>>(sd.planes, sd.g, sd.W, sd.c, np, ng, Y);
-  if (sd.c > 0) {
-    const int cpad = ng * kPairsPerGroup;  // whole groups, the pad zero
-    k_ctot_f<<<(cpad + 255) / 256, 256, 0, st>>>(sd.ctot, sd.prior, sd.c, cpad, ctf);
-  }
+  k_setup<<<a.b[3], 128, 0, st>>>(a);
   return cudaGetLastError();
 }
-int mma_build_launches(const SetDev &sd) { return sd.core ? 4 : (sd.c > 0 ? 2 : 1); }
+int mma_build_launches(const SetDev &) { return 1; }
 
 template <int kStages, int kEpi, int kGroups, bool kCore>
 static cudaError_t launch_variant(const SetDev &sd, const uint8_t *Afp8, const uint8_t *Y,
@@ -1156,8 +1196,8 @@ static cudaError_t launch_variant(const SetDev &sd, const uint8_t *Afp8, const u
 // 0: N=128, 16 epilogue warps; 1: N=128, 8 warps; 2: N=192, 12 warps;
 // 3: N=256, 8 warps; 4: N=256, 16 warps (ring depths fill the shared memory)
 int mma_variants() { return 5; }
-// operand (and class counts), GEMM + epilogue, general path, exact path
-int mma_launches(const SetDev &sd) { return sd.core ? 5 : 4; }
+// operands (and class counts), GEMM + epilogue, general path, exact path
+int mma_launches(const SetDev &) { return 4; }
 
 template <bool kCore>
 static cudaError_t launch_shape(const SetDev &sd, uint8_t *Afp8, const uint8_t *Y,
@@ -1183,17 +1223,16 @@ cudaError_t launch_pairs_mma(const SetDev &sd, const uint64_t *masks, int B, uin
                              unsigned *err, int sms, cudaStream_t st, int variant) {
   const int np = mma_npad(sd.n), Bp = mma_bpad(B);
   const long long work = (long long)Bp * (np / 16);
-  k_masks_fp8<<<(unsigned)((work + 255) / 256), 256, 0, st>>>(masks, B, Bp, sd.W, np, Afp8);
-  if (sd.core) {
-    uint32_t *margc = (uint32_t *)(Afp8 + margins_offset(B, sd.n, sd.c));
-    const dim3 grid((unsigned)(Bp / 128), (unsigned)((sd.g + kMargGenes - 1) / kMargGenes));
-    k_margins<<<grid, 128, 0, st>>>(masks, sd.planes, B, Bp, sd.g, sd.W, margc,
-                                    (float *)(margc + (size_t)Bp * sd.g));
-  }
+  const int bA = (int)((work + 127) / 128);
+  const int bM = sd.core ? (Bp / 128) * ((sd.g + kMargGenes - 1) / kMargGenes) : 0;
   unsigned *gqueue = reinterpret_cast<unsigned *>(Afp8 + a_operand_bytes(B, sd.n));
-  const unsigned qcap = queue_cap_used(B, sd.c);
-  cudaError_t e = cudaMemsetAsync(gqueue, 0, 16, st);
+  uint32_t *margc = sd.core ? (uint32_t *)(Afp8 + margins_offset(B, sd.n, sd.c)) : nullptr;
+  k_operands<<<bA + bM, 128, 0, st>>>(masks, sd.planes, B, Bp, sd.g, sd.W, np, bA, Afp8, margc,
+                                       margc ? (float *)(margc + (size_t)Bp * sd.g) : nullptr,
+                                       gqueue);
+  cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
+  const unsigned qcap = queue_cap_used(B, sd.c);
   if (sd.core)
     return launch_shape<true>(sd, Afp8, Y, gqueue, qcap, B, dmask, stats, err, sms, st, variant);
   return launch_shape<false>(sd, Afp8, Y, gqueue, qcap, B, dmask, stats, err, sms, st, variant);

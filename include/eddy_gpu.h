@@ -201,7 +201,9 @@ int eddy_unit_noalloc(const eddy_opts *opts, const int8_t *vals, int g, int n,
 /* Decision-path counters of the last batch run: [0] tables re-evaluated in
  * FP64 (guard-band rechecks), [1] (pair, class) tables decided, [2] of them
  * whose ten leave-one-out tables the filter settled at once, [3] duplicate
- * networks; *variant: the autotuned contingency-kernel variant (-1: none). */
+ * networks; *variant: the contingency-kernel choice of the last batch (0-4:
+ * tile shapes in the 9-cell layout, 5-9: the same in the 4-cell layout of
+ * sets without missing values; -1: none). */
 int eddy_last_stats(const eddy_ctx *ctx, uint64_t *stats4, int *variant);
 
 /* Name, SM count and compute capability of a device (the reference's

@@ -85,3 +85,61 @@ def test_missing_values_keep_the_full_layout(eddy_lib, oracle_lib, monkeypatch):
         ojs, oU = oracle_lib.units(data[genes], labs, None, None)
         assert np.array_equal(U, oU)
         assert js_close(js, ojs)
+
+
+@pytest.mark.parametrize("g", [30, 150])
+def test_tuner_chooses_between_layouts(g, eddy_lib, monkeypatch):
+    """Unpinned, the first batch of >= 512 units times every tile shape in
+    both layouts (choices 0-9); whichever wins, the results equal the pinned
+    9-cell ones, on the tuning batch and on the batches after it."""
+    rng = np.random.default_rng(500 + g)
+    n, nA = 400, 180
+    data = planted(rng, g, n, nA=nA, planted=min(6, g // 2), w=0.9, noise=0.4)
+    labels0 = np.concatenate([np.zeros(nA, np.uint8), np.ones(n - nA, np.uint8)])
+    ref = _run(eddy_lib, monkeypatch, "full", data, labels0, np.arange(g), 600, 3)
+    monkeypatch.delenv("EDDY_MMA_VARIANT", raising=False)
+    monkeypatch.delenv("EDDY_PAIR_LAYOUT", raising=False)
+    ctx = eddy_lib.Context(max_parents=3, permutations=600, rng=eddy_lib.RNG_COUNTER,
+                           seed=11, keep_networks=False)
+    ctx.load_matrix(data, labels0)
+    sid = ctx.add_set(np.arange(g))
+    for _ in range(3):  # tuning batch, direct launch, graph replay
+        js, U = ctx.run_permutations(sid, 1, 600)
+        assert 0 <= ctx.stats()["variant"] < 10
+        assert np.array_equal(U, ref[1])
+        assert np.array_equal(js, ref[0], equal_nan=True)
+
+
+def test_tuned_choice_not_shared_with_missing_values(eddy_lib, monkeypatch):
+    """Two sets of the same size class in one context, the second with a
+    missing value: whatever the first set tuned, the second runs the 9-cell
+    layout and matches its pinned 9-cell result."""
+    rng = np.random.default_rng(77)
+    G, n, nA, g = 320, 300, 140, 150
+    data = planted(rng, G, n, nA=nA, planted=8, w=0.9, noise=0.4)
+    data[300, 5] = 2  # gene 300 has a missing value
+    labels0 = np.concatenate([np.zeros(nA, np.uint8), np.ones(n - nA, np.uint8)])
+    genes_a = np.arange(g)
+    genes_b = np.concatenate([np.arange(1, g), [300]])
+
+    def run(pinned):
+        if pinned:
+            monkeypatch.setenv("EDDY_PAIR_LAYOUT", "full")
+            monkeypatch.setenv("EDDY_MMA_VARIANT", "3")
+        else:
+            monkeypatch.delenv("EDDY_MMA_VARIANT", raising=False)
+            monkeypatch.delenv("EDDY_PAIR_LAYOUT", raising=False)
+        ctx = eddy_lib.Context(max_parents=3, permutations=600, rng=eddy_lib.RNG_COUNTER,
+                               seed=11, keep_networks=False)
+        ctx.load_matrix(data, labels0)
+        sa = ctx.add_set(genes_a)  # set 0 (the counter stream is keyed by set)
+        ctx.run_permutations(sa, 1, 600)
+        sb = ctx.add_set(genes_b)
+        js, U = ctx.run_permutations(sb, 1, 600)
+        return js, U, ctx.stats()["variant"]
+
+    ref = run(True)
+    js, U, variant = run(False)
+    assert variant < 5
+    assert np.array_equal(U, ref[1])
+    assert np.array_equal(js, ref[0], equal_nan=True)
