@@ -157,10 +157,10 @@ static inline void philox10(uint32_t c[4], uint32_t k0, uint32_t k1) {
 
 void counter_labels(uint64_t seed, int set_id, int perm, int n, int n_class1, uint8_t *labels) {
   std::vector<std::pair<uint32_t, int>> kv(n);
-  for (int s = 0; s < n; s++) {
-    uint32_t c[4] = {(uint32_t)s, (uint32_t)perm, (uint32_t)set_id, 0u};
+  for (int s = 0; s < n; s += 4) {
+    uint32_t c[4] = {(uint32_t)(s / 4), (uint32_t)perm, (uint32_t)set_id, 0u};
     philox10(c, (uint32_t)seed, (uint32_t)(seed >> 32));
-    kv[s] = {c[0], s};
+    for (int j = 0; j < 4 && s + j < n; j++) kv[s + j] = {c[j], s + j};
   }
   std::sort(kv.begin(), kv.end());
   for (int k = 0; k < n; k++) labels[kv[k].second] = (uint8_t)(k < n_class1 ? 0 : 1);

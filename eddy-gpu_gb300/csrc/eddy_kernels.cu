@@ -91,88 +91,109 @@ __device__ __forceinline__ void philox10(uint32_t c[4], uint32_t k0, uint32_t k1
   }
 }
 
-// One block per unit.  key(s) = Philox(ctr = (s, perm, set, 0), key = seed)
-// word 0; the nA samples with the smallest (key, s) are class 1.
-__global__ void __launch_bounds__(128) k_counter_masks(int n, int nA, int W, uint64_t seed,
-                                                       const int32_t *unit_set,
-                                                       const int32_t *unit_perm,
-                                                       const uint64_t *mask0, uint64_t *masks) {
-  // class 1 = the nA samples with the smallest (key, sample) pairs, keys
-  // from Philox-4x32-10 of (sample, permutation, set): the nA-th smallest
-  // key T is found by a radix select (four 8-bit digits, a 256-bin
-  // histogram each), then every sample with key < T is in, and of those
-  // with key == T the lowest-indexed ones that are still needed.  The same
-  // set as sorting the pairs and taking the first nA.
-  extern __shared__ uint32_t key[];  // [n], then [W] u64 mask words
-  __shared__ int hist[256];
-  __shared__ uint32_t s_prefix;
-  __shared__ int s_need;
-  const int u = blockIdx.x, tid = threadIdx.x, nt = blockDim.x;
+// One block per unit.  key(s) = word s mod 4 of Philox(ctr = (s / 4, perm,
+// set, 0), key = seed); the nA samples with the smallest (key, s) are class 1.
+// Selection: a histogram of the keys' top 11 bits finds the bin that holds
+// the nA-th smallest key; the samples of that bin (about n / 2048 of them)
+// are ranked by (key, s) against each other, which gives the last one in,
+// (T, sT); sample s is in when (key, s) <= (T, sT).  The same set as
+// sorting the pairs and taking the first nA.
+constexpr int kCmBlock = 128, kCmBins = 2048, kCmShift = 21;
+__global__ void __launch_bounds__(kCmBlock) k_counter_masks(int n, int nA, int W, uint64_t seed,
+                                                            const int32_t *unit_set,
+                                                            const int32_t *unit_perm,
+                                                            const uint64_t *mask0,
+                                                            uint64_t *masks) {
+  // keys [n] u32 (padded to 8 bytes), the W mask words, then the bin's
+  // samples [n] u16
+  extern __shared__ uint32_t key[];
+  __shared__ int hist[kCmBins];
+  __shared__ int wsum[kCmBlock / 32];
+  __shared__ int s_bin, s_need, s_cnt;
+  __shared__ uint32_t s_T;
+  __shared__ int s_sT;
+  const int u = blockIdx.x, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int perm = unit_perm[u];
   uint64_t *out = masks + (size_t)u * W;
   if (perm == 0) {
-    for (int w = tid; w < W; w += nt) out[w] = mask0[w];
+    for (int w = tid; w < W; w += kCmBlock) out[w] = mask0[w];
     return;
   }
   unsigned long long *mw = reinterpret_cast<unsigned long long *>(key + ((n + 1) & ~1));
+  uint16_t *cand = reinterpret_cast<uint16_t *>(mw + W);
   const uint32_t k0 = (uint32_t)seed, k1 = (uint32_t)(seed >> 32);
-  for (int s = tid; s < n; s += nt) {
-    uint32_t c[4] = {(uint32_t)s, (uint32_t)perm, (uint32_t)unit_set[u], 0u};
+  // one Philox call gives the keys of four samples
+  for (int s4 = tid; 4 * s4 < n; s4 += kCmBlock) {
+    uint32_t c[4] = {(uint32_t)s4, (uint32_t)perm, (uint32_t)unit_set[u], 0u};
     philox10(c, k0, k1);
-    key[s] = c[0];
+#pragma unroll
+    for (int j = 0; j < 4; j++)
+      if (4 * s4 + j < n) key[4 * s4 + j] = c[j];
   }
-  for (int w = tid; w < W; w += nt) mw[w] = 0ull;
-  if (tid == 0) {
-    s_prefix = 0u;
-    s_need = nA;
+  for (int w = tid; w < W; w += kCmBlock) mw[w] = 0ull;
+  for (int i = tid; i < kCmBins; i += kCmBlock) hist[i] = 0;
+  if (tid == 0) s_cnt = 0;
+  __syncthreads();
+  for (int s = tid; s < n; s += kCmBlock) atomicAdd(&hist[key[s] >> kCmShift], 1);
+  __syncthreads();
+  // the bin of the nA-th smallest key: thread t sums bins [16 t, 16 t + 16),
+  // then a block scan of those sums
+  constexpr int kPer = kCmBins / kCmBlock;
+  int loc = 0;
+#pragma unroll
+  for (int j = 0; j < kPer; j++) loc += hist[tid * kPer + j];
+  int incl = loc;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int y = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += y;
   }
-  uint32_t pmask = 0u;
-  for (int shift = 24; shift >= 0; shift -= 8) {
-    for (int i = tid; i < 256; i += nt) hist[i] = 0;
-    __syncthreads();
-    const uint32_t prefix = s_prefix;
-    for (int s = tid; s < n; s += nt)
-      if ((key[s] & pmask) == prefix) atomicAdd(&hist[(key[s] >> shift) & 255u], 1);
-    __syncthreads();
-    if (tid < 32) {
-      // the digit whose bin holds the need-th candidate (warp scan of the
-      // 256 bins, 8 per lane)
-      const int need = s_need;
-      int loc[8], sum = 0;
-      for (int j = 0; j < 8; j++) {
-        loc[j] = hist[tid * 8 + j];
-        sum += loc[j];
+  if (lane == 31) wsum[warp] = incl;
+  __syncthreads();
+  int before = incl - loc;
+  for (int w = 0; w < warp; w++) before += wsum[w];
+  if (before < nA && nA <= before + loc) {
+    for (int j = 0; j < kPer; j++) {
+      const int h = hist[tid * kPer + j];
+      if (before < nA && nA <= before + h) {
+        s_bin = tid * kPer + j;
+        s_need = nA - before;
       }
-      int incl = sum;
-      for (int o = 1; o < 32; o <<= 1) {
-        const int y = __shfl_up_sync(0xffffffffu, incl, o);
-        if (tid >= o) incl += y;
-      }
-      int before = incl - sum;  // candidates in the bins of lower lanes
-      for (int j = 0; j < 8; j++) {
-        if (before < need && need <= before + loc[j]) {
-          s_prefix = prefix | ((uint32_t)(tid * 8 + j) << shift);
-          s_need = need - before;
-        }
-        before += loc[j];
-      }
+      before += h;
     }
-    pmask |= 255u << shift;
-    __syncthreads();
-  }
-  const uint32_t T = s_prefix;
-  const int need = s_need;  // samples with key == T that are in
-  for (int s = tid; s < n; s += nt) {
-    bool in = key[s] < T;
-    if (key[s] == T) {
-      int rank = 0;  // equal keys before s (rare: 32-bit keys)
-      for (int t = 0; t < s; t++) rank += key[t] == T;
-      in = rank < need;
-    }
-    if (in) atomicOr(&mw[s >> 6], 1ull << (s & 63));
   }
   __syncthreads();
-  for (int w = tid; w < W; w += nt) out[w] = mw[w];
+  const uint32_t bin = (uint32_t)s_bin;
+  const int need = s_need;
+  for (int s = tid; s < n; s += kCmBlock)
+    if ((key[s] >> kCmShift) == bin) cand[atomicAdd(&s_cnt, 1)] = (uint16_t)s;
+  __syncthreads();
+  // rank of each of the bin's samples among them by (key, s): the one of
+  // rank need - 1 is the last one in
+  const int cnt = s_cnt;
+  for (int c = tid; c < cnt; c += kCmBlock) {
+    const int s = cand[c];
+    const uint32_t k = key[s];
+    int rank = 0;
+    for (int d = 0; d < cnt; d++) {
+      const int t = cand[d];
+      const uint32_t kt = key[t];
+      rank += (kt < k || (kt == k && t < s)) ? 1 : 0;
+    }
+    if (rank == need - 1) {
+      s_T = k;
+      s_sT = s;
+    }
+  }
+  __syncthreads();
+  const uint32_t T = s_T;
+  const int sT = s_sT;
+  for (int s = tid; s < n; s += kCmBlock) {
+    const uint32_t k = key[s];
+    if (k < T || (k == T && s <= sT)) atomicOr(&mw[s >> 6], 1ull << (s & 63));
+  }
+  __syncthreads();
+  for (int w = tid; w < W; w += kCmBlock) out[w] = mw[w];
 }
 
 // ------------------------------------------------------------ k_pairs
@@ -1339,7 +1360,7 @@ __global__ void __launch_bounds__(256, 3) k_units(const __grid_constant__ SetDev
       });
 
   // ---- P6: unique count and status; the normalisation and JS follow in
-  // k_js (one warp per unit) from the fixed-point scores in dist
+  // k_js (32 units per warp) from the fixed-point scores in dist
   const int keep = bd.keep_slot ? bd.keep_slot[u] : -1;
   if (tid == 0) {
     bd.U[u] = U;
@@ -1385,96 +1406,136 @@ __global__ void __launch_bounds__(256, 3) k_units(const __grid_constant__ SetDev
 // the unit's scratch: per class min, max and mean of the scores,
 // likelihoods exp((d - mean) 10 / (max - min)) normalised to sum 1, then the
 // two KL terms of kool() (routines.cu:42-60), zeros skipped, in FP64.  A
-// unit k_units gave up on (U < 0) is left as it is.  One warp per unit
-// (kJsLanes lanes, so the FP64 chains of the unique networks run side by
-// side); the exponentials of the first kJsCache * kJsLanes networks are
-// kept in registers between the sum and the KL pass instead of being
-// computed twice (FP64 is slow on this part).
-constexpr int kJsLanes = 32, kJsCache = 1;
-__global__ void __launch_bounds__(256) k_js(const __grid_constant__ SetDev sd,
-                                            const __grid_constant__ BatchDev bd) {
-  const int u = (int)((blockIdx.x * blockDim.x + threadIdx.x) / kJsLanes);
-  const int sub = threadIdx.x & (kJsLanes - 1);
-  const int U = u < bd.B ? bd.U[u] : -1;
-  const bool act = U > 0;  // (inactive lanes join the shuffles with neutral values)
+// unit k_units gave up on (U < 0) is left as it is.
+//
+// One warp per 32 units.  Lane l holds unit 32 w + l's minimum, maximum and
+// mean (an exact integer sum); the warp then walks the units' unique
+// networks as one flattened list, 32 at a time, so that every lane runs an
+// FP64 exponential or logarithm whatever the units' sizes (units have ~8
+// unique networks, and FP64 is slow on this part: one warp per unit left
+// three lanes in four idle).  A unit's sums are formed in a fixed order: a
+// segmented tree sum within each 32-network pass, the passes added in turn.
+// Between the two passes a network's exponentials replace its scores in the
+// unit's dist array (the scores are not read after this kernel).
+constexpr int kJsWarps = 8;
+__global__ void __launch_bounds__(32 * kJsWarps) k_js(const __grid_constant__ SetDev sd,
+                                                      const __grid_constant__ BatchDev bd) {
+  __shared__ int pre[kJsWarps][33];
+  __shared__ double acc[kJsWarps][3][32];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int u0 = (blockIdx.x * kJsWarps + warp) * 32, u = u0 + lane;
+  const int Ur = u < bd.B ? bd.U[u] : 0;
+  const int U = Ur > 0 ? Ur : 0;
   const int S = sd.S;
   const UnitLayout L = unit_layout(sd.c, S, bd.kmax);
-  const long long *dist =
-      act ? (const long long *)(bd.scratch + (size_t)u * bd.unit_bytes + L.dist) : nullptr;
-  long long l0 = LLONG_MAX, h0 = LLONG_MIN, l1 = LLONG_MAX, h1 = LLONG_MIN;
-  for (int uu = sub; act && uu < U; uu += kJsLanes) {
-    const long long a = dist[uu], b = dist[S + uu];
-    l0 = a < l0 ? a : l0;
-    h0 = a > h0 ? a : h0;
-    l1 = b < l1 ? b : l1;
-    h1 = b > h1 ? b : h1;
-  }
-  for (int o = kJsLanes / 2; o > 0; o >>= 1) {
-    long long x;
-    x = __shfl_xor_sync(0xffffffffu, l0, o); l0 = x < l0 ? x : l0;
-    x = __shfl_xor_sync(0xffffffffu, h0, o); h0 = x > h0 ? x : h0;
-    x = __shfl_xor_sync(0xffffffffu, l1, o); l1 = x < l1 ? x : l1;
-    x = __shfl_xor_sync(0xffffffffu, h1, o); h1 = x > h1 ? x : h1;
-  }
-  double s0 = 0.0, s1 = 0.0;
-  for (int uu = sub; act && uu < U; uu += kJsLanes) {
-    s0 += (double)(dist[uu] - l0);
-    s1 += (double)(dist[S + uu] - l1);
-  }
-  for (int o = kJsLanes / 2; o > 0; o >>= 1) {
-    s0 += __shfl_xor_sync(0xffffffffu, s0, o);
-    s1 += __shfl_xor_sync(0xffffffffu, s1, o);
-  }
-  const double m0 = act ? s0 / (double)U : 0.0, m1 = act ? s1 / (double)U : 0.0;
-  const double sA = act ? 10.0 / (double)(h0 - l0) : 0.0, sB = act ? 10.0 / (double)(h1 - l1) : 0.0;
-  auto ea_of = [&](int uu) { return exp(((double)(dist[uu] - l0) - m0) * sA); };
-  auto eb_of = [&](int uu) { return exp(((double)(dist[S + uu] - l1) - m1) * sB); };
-  double ea[kJsCache], eb[kJsCache];
-  double e0 = 0.0, e1 = 0.0;
-#pragma unroll
-  for (int j = 0; j < kJsCache; j++) {
-    const int uu = sub + kJsLanes * j;
-    ea[j] = eb[j] = 0.0;
-    if (act && uu < U) {
-      ea[j] = ea_of(uu);
-      eb[j] = eb_of(uu);
-      e0 += ea[j];
-      e1 += eb[j];
-    }
-  }
-  for (int uu = sub + kJsLanes * kJsCache; act && uu < U; uu += kJsLanes) {
-    e0 += ea_of(uu);
-    e1 += eb_of(uu);
-  }
-  for (int o = kJsLanes / 2; o > 0; o >>= 1) {
-    e0 += __shfl_xor_sync(0xffffffffu, e0, o);
-    e1 += __shfl_xor_sync(0xffffffffu, e1, o);
-  }
-  const int keep = (act && bd.keep_slot) ? bd.keep_slot[u] : -1;
-  double ls = 0.0;
-  auto term = [&](int uu, double a, double b) {
-    const double Pu = a / e0;
-    const double Qu = b / e1;
-    const double M = (Pu + Qu) / 2;
-    if (M != 0) {
-      if (Pu != 0) ls += 0.5 * (Pu * log(Pu / M));
-      if (Qu != 0) ls += 0.5 * (Qu * log(Qu / M));
-    }
-    if (keep >= 0) {
-      bd.out_lval[((size_t)keep * 2 + 0) * S + uu] = Pu;
-      bd.out_lval[((size_t)keep * 2 + 1) * S + uu] = Qu;
-    }
+  auto dist_of = [&](int uid) {
+    return (long long *)(bd.scratch + (size_t)uid * bd.unit_bytes + L.dist);
   };
-#pragma unroll
-  for (int j = 0; j < kJsCache; j++) {
-    const int uu = sub + kJsLanes * j;
-    if (act && uu < U) term(uu, ea[j], eb[j]);
+  long long l0 = LLONG_MAX, h0 = LLONG_MIN, l1 = LLONG_MAX, h1 = LLONG_MIN;
+  double m0 = 0.0, m1 = 0.0, sA = 0.0, sB = 0.0;
+  if (U > 0) {
+    const long long *d = dist_of(u);
+    for (int uu = 0; uu < U; uu++) {
+      const long long a = d[uu], b = d[S + uu];
+      l0 = a < l0 ? a : l0;
+      h0 = a > h0 ? a : h0;
+      l1 = b < l1 ? b : l1;
+      h1 = b > h1 ? b : h1;
+    }
+    long long q0 = 0, q1 = 0;
+    for (int uu = 0; uu < U; uu++) {
+      q0 += d[uu] - l0;
+      q1 += d[S + uu] - l1;
+    }
+    m0 = (double)q0 / (double)U;
+    m1 = (double)q1 / (double)U;
+    sA = 10.0 / (double)(h0 - l0);
+    sB = 10.0 / (double)(h1 - l1);
   }
-  for (int uu = sub + kJsLanes * kJsCache; act && uu < U; uu += kJsLanes)
-    term(uu, ea_of(uu), eb_of(uu));
-  for (int o = kJsLanes / 2; o > 0; o >>= 1) ls += __shfl_xor_sync(0xffffffffu, ls, o);
-  if (act && sub == 0) {
-    double js = ls / log(2.0);
+  const int keep = (U > 0 && bd.keep_slot) ? bd.keep_slot[u] : -1;
+  // the warp's units as prefix intervals of the flattened list
+  int incl = U;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int y = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += y;
+  }
+  pre[warp][lane] = incl - U;
+  if (lane == 31) pre[warp][32] = incl;
+  acc[warp][0][lane] = acc[warp][1][lane] = acc[warp][2][lane] = 0.0;
+  __syncwarp();
+  const int total = pre[warp][32];
+  // owner of network i: the last unit whose interval starts at or before i
+  auto owner = [&](int i) {
+    int lo = 0, hi = 31;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (pre[warp][mid] <= i) lo = mid;
+      else hi = mid - 1;
+    }
+    return lo;
+  };
+  // sum of v over this lane's run of equal owners, added to dst[owner] by
+  // the run's last live lane
+  auto seg_add = [&](double v, int o, bool live, double *dst) {
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+      const double y = __shfl_up_sync(0xffffffffu, v, d);
+      const int oy = __shfl_up_sync(0xffffffffu, o, d);
+      if (lane >= d && oy == o) v += y;
+    }
+    const int on = __shfl_down_sync(0xffffffffu, o, 1);
+    const bool nlive = __shfl_down_sync(0xffffffffu, live ? 1 : 0, 1) != 0;
+    if (live && (lane == 31 || on != o || !nlive)) dst[o] += v;
+  };
+  // pass 1: the likelihoods, summed per unit and class
+  for (int i0 = 0; i0 < total; i0 += 32) {
+    const int i = i0 + lane;
+    const bool live = i < total;
+    const int o = live ? owner(i) : 31;
+    const long long ol0 = __shfl_sync(0xffffffffu, l0, o), ol1 = __shfl_sync(0xffffffffu, l1, o);
+    const double om0 = __shfl_sync(0xffffffffu, m0, o), om1 = __shfl_sync(0xffffffffu, m1, o);
+    const double osA = __shfl_sync(0xffffffffu, sA, o), osB = __shfl_sync(0xffffffffu, sB, o);
+    double ea = 0.0, eb = 0.0;
+    if (live) {
+      long long *d = dist_of(u0 + o);
+      const int uu = i - pre[warp][o];
+      ea = exp(((double)(d[uu] - ol0) - om0) * osA);
+      eb = exp(((double)(d[S + uu] - ol1) - om1) * osB);
+      d[uu] = __double_as_longlong(ea);
+      d[S + uu] = __double_as_longlong(eb);
+    }
+    seg_add(ea, o, live, acc[warp][0]);
+    seg_add(eb, o, live, acc[warp][1]);
+  }
+  __syncwarp();
+  // pass 2: the normalised likelihoods and the two KL terms
+  for (int i0 = 0; i0 < total; i0 += 32) {
+    const int i = i0 + lane;
+    const bool live = i < total;
+    const int o = live ? owner(i) : 31;
+    const int okeep = __shfl_sync(0xffffffffu, keep, o);
+    double t = 0.0;
+    if (live) {
+      const long long *d = dist_of(u0 + o);
+      const int uu = i - pre[warp][o];
+      const double Pu = __longlong_as_double(d[uu]) / acc[warp][0][o];
+      const double Qu = __longlong_as_double(d[S + uu]) / acc[warp][1][o];
+      const double M = (Pu + Qu) / 2;
+      if (M != 0) {
+        if (Pu != 0) t += 0.5 * (Pu * log(Pu / M));
+        if (Qu != 0) t += 0.5 * (Qu * log(Qu / M));
+      }
+      if (okeep >= 0) {
+        bd.out_lval[((size_t)okeep * 2 + 0) * S + uu] = Pu;
+        bd.out_lval[((size_t)okeep * 2 + 1) * S + uu] = Qu;
+      }
+    }
+    seg_add(t, o, live, acc[warp][2]);
+  }
+  __syncwarp();
+  if (U > 0) {
+    double js = acc[warp][2][lane] / log(2.0);
     if (h0 == l0 || h1 == l1) js = __longlong_as_double(0x7ff8000000000000ll);
     bd.js[u] = js;
   }
@@ -1493,15 +1554,16 @@ cudaError_t launch_prep(const int8_t *vals, int g, int n, int W, int c, uint64_t
 cudaError_t launch_counter_masks(int n, int nA, int W, uint64_t seed, const int32_t *unit_set,
                                  const int32_t *unit_perm, const uint64_t *mask0, uint64_t *masks,
                                  int B, cudaStream_t st) {
-  // keys [n] u32 (padded to 8 bytes), then the W mask words; 128-thread
-  // blocks (the select is barrier-bound: more blocks per SM hide it)
-  const size_t smem = sizeof(uint32_t) * (size_t)((n + 1) & ~1) + sizeof(uint64_t) * W;
+  // keys [n] u32 (padded to 8 bytes), the W mask words, then [n] u16
+  // sample indices; 128-thread blocks (more blocks per SM hide the barriers)
+  const size_t smem = sizeof(uint32_t) * (size_t)((n + 1) & ~1) + sizeof(uint64_t) * W +
+                      sizeof(uint16_t) * (size_t)n;
   if (smem > 48 * 1024) {
     cudaError_t e =
         cudaFuncSetAttribute(k_counter_masks, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
   }
-  k_counter_masks<<<B, 128, smem, st>>>(n, nA, W, seed, unit_set, unit_perm, mask0, masks);
+  k_counter_masks<<<B, kCmBlock, smem, st>>>(n, nA, W, seed, unit_set, unit_perm, mask0, masks);
   return cudaGetLastError();
 }
 
@@ -1521,7 +1583,7 @@ cudaError_t launch_units(const SetDev &sd, const BatchDev &bd, cudaStream_t st) 
   k_units<<<bd.B, threads, smem, st>>>(sd, bd);
   e = cudaGetLastError();
   if (e != cudaSuccess) return e;
-  k_js<<<(bd.B + 256 / kJsLanes - 1) / (256 / kJsLanes), 256, 0, st>>>(sd, bd);
+  k_js<<<(bd.B + 32 * kJsWarps - 1) / (32 * kJsWarps), 32 * kJsWarps, 0, st>>>(sd, bd);
   return cudaGetLastError();
 }
 

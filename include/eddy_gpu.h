@@ -37,7 +37,9 @@ extern "C" {
 
 /* Label-permutation streams.  GLIBC reproduces main.cu:538-573 exactly
  * (glibc rand(), never reseeded, one stream across all gene sets);
- * COUNTER uses Philox-4x32-10 keyed by (seed, set, permutation, sample);
+ * COUNTER uses Philox-4x32-10 keyed by seed: sample s's key is word s mod 4
+ * of the block with counter (s / 4, permutation, set, 0), and the n_A
+ * samples with the smallest (key, s) form class 0 of that permutation;
  * EXTERNAL takes caller-supplied labellings (eddy_set_labellings). */
 #define EDDY_RNG_GLIBC 0
 #define EDDY_RNG_COUNTER 1

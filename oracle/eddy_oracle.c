@@ -582,12 +582,14 @@ void or_counter_labels(uint64_t seed, int set_id, int n, int n_class1,
   uint32_t key[2] = {(uint32_t)seed, (uint32_t)(seed >> 32)};
   memcpy(out, labels0, n);
   for (int perm = 1; perm < R; perm++) {
-    for (int s = 0; s < n; s++) {
-      uint32_t ctr[4] = {(uint32_t)s, (uint32_t)perm, (uint32_t)set_id, 0u};
+    for (int s = 0; s < n; s += 4) {
+      uint32_t ctr[4] = {(uint32_t)(s / 4), (uint32_t)perm, (uint32_t)set_id, 0u};
       uint32_t o[4];
       or_philox4x32_10(ctr, key, o);
-      kv[s].key = o[0];
-      kv[s].idx = s;
+      for (int j = 0; j < 4 && s + j < n; j++) {
+        kv[s + j].key = o[j];
+        kv[s + j].idx = s + j;
+      }
     }
     qsort(kv, n, sizeof(kv_t), kv_cmp);
     uint8_t *row = out + (size_t)perm * n;

@@ -117,9 +117,10 @@ void or_glibc_labels(int n, int n_class1, const uint8_t *labels0, int R,
 /* Number of libc rand() calls one permutation consumes (for stream tests). */
 long long or_glibc_rand_calls(void);
 
-/* Counter-based labelling (Philox-4x32-10 keyed by seed; counter =
- * (sample, perm, set, 0)); the n_class1 samples with the smallest
- * (key, index) get label 0.  perm 0 = labels0. */
+/* Counter-based labelling: the key of sample s is word s mod 4 of
+ * Philox-4x32-10 keyed by seed with counter (s / 4, perm, set, 0); the
+ * n_class1 samples with the smallest (key, index) get label 0.  perm 0 =
+ * labels0. */
 void or_counter_labels(uint64_t seed, int set_id, int n, int n_class1,
                        const uint8_t *labels0, int R, uint8_t *out);
 void or_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2],
