@@ -21,6 +21,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <algorithm>
 #include <climits>
 
 #include "eddy_device.cuh"
@@ -1360,7 +1361,7 @@ __global__ void __launch_bounds__(256, 3) k_units(const __grid_constant__ SetDev
       });
 
   // ---- P6: unique count and status; the normalisation and JS follow in
-  // k_js (32 units per warp) from the fixed-point scores in dist
+  // k_js (up to 32 units per warp) from the fixed-point scores in dist
   const int keep = bd.keep_slot ? bd.keep_slot[u] : -1;
   if (tid == 0) {
     bd.U[u] = U;
@@ -1408,23 +1409,26 @@ __global__ void __launch_bounds__(256, 3) k_units(const __grid_constant__ SetDev
 // two KL terms of kool() (routines.cu:42-60), zeros skipped, in FP64.  A
 // unit k_units gave up on (U < 0) is left as it is.
 //
-// One warp per 32 units.  Lane l holds unit 32 w + l's minimum, maximum and
-// mean (an exact integer sum); the warp then walks the units' unique
-// networks as one flattened list, 32 at a time, so that every lane runs an
-// FP64 exponential or logarithm whatever the units' sizes (units have ~8
-// unique networks, and FP64 is slow on this part: one warp per unit left
-// three lanes in four idle).  A unit's sums are formed in a fixed order: a
-// segmented tree sum within each 32-network pass, the passes added in turn.
-// Between the two passes a network's exponentials replace its scores in the
-// unit's dist array (the scores are not read after this kernel).
+// One warp per upw <= 32 units.  Lane l < upw holds unit upw w + l's
+// minimum, maximum and mean (an exact integer sum); the warp then walks the
+// units' unique networks as one flattened list, 32 at a time, so that every
+// lane runs an FP64 exponential or logarithm whatever the units' sizes
+// (units have ~8 unique networks, and FP64 is slow on this part: one warp
+// per unit leaves three lanes in four idle).  upw is chosen so that the
+// grid still covers the GPU (one unit per warp for small batches).  A
+// unit's sums are formed in a fixed order: a segmented tree sum within each
+// 32-network pass, the passes added in turn.  Between the two passes a
+// network's exponentials replace its scores in the unit's dist array (the
+// scores are not read after this kernel).
 constexpr int kJsWarps = 8;
 __global__ void __launch_bounds__(32 * kJsWarps) k_js(const __grid_constant__ SetDev sd,
-                                                      const __grid_constant__ BatchDev bd) {
+                                                      const __grid_constant__ BatchDev bd,
+                                                      int upw) {
   __shared__ int pre[kJsWarps][33];
   __shared__ double acc[kJsWarps][3][32];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int u0 = (blockIdx.x * kJsWarps + warp) * 32, u = u0 + lane;
-  const int Ur = u < bd.B ? bd.U[u] : 0;
+  const int u0 = (blockIdx.x * kJsWarps + warp) * upw, u = u0 + lane;
+  const int Ur = (lane < upw && u < bd.B) ? bd.U[u] : 0;
   const int U = Ur > 0 ? Ur : 0;
   const int S = sd.S;
   const UnitLayout L = unit_layout(sd.c, S, bd.kmax);
@@ -1583,7 +1587,17 @@ cudaError_t launch_units(const SetDev &sd, const BatchDev &bd, cudaStream_t st) 
   k_units<<<bd.B, threads, smem, st>>>(sd, bd);
   e = cudaGetLastError();
   if (e != cudaSuccess) return e;
-  k_js<<<(bd.B + 32 * kJsWarps - 1) / (32 * kJsWarps), 32 * kJsWarps, 0, st>>>(sd, bd);
+  // units per warp: as many as keep about eight warps per SM busy
+  static int sms = 0;
+  if (sms == 0) {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+      sms = 148;
+  }
+  const int upw = std::max(1, std::min(32, bd.B / (sms * kJsWarps)));
+  const int warps = (bd.B + upw - 1) / upw;
+  k_js<<<(warps + kJsWarps - 1) / kJsWarps, 32 * kJsWarps, 0, st>>>(sd, bd, upw);
   return cudaGetLastError();
 }
 
