@@ -366,7 +366,7 @@ def run_ours(args, rank, world, local):
     cells = 4 if core else 9
     k1_ms = acc["ms_pairs"] / launches_per_kernel
     # algorithmic work of the contraction: 2 (3g)^2 n_A per unit (the class-A
-    # Gram matrix of the genes' state indicators); the GEMM this build runs
+    # Gram matrix of the genes' state indicators); the GEMM the kernel runs
     # is smaller: 2 x cells x c x n per unit
     nA = int((np.asarray(w.labels) == 0).sum())
     k1_flops = 2.0 * (3 * g) ** 2 * nA * B
