@@ -301,3 +301,41 @@ def test_normaliser_branches(oracle_lib):
     out = np.zeros(3)
     O.lib().or_normalise(3, np.full(3, -42.0), out)
     assert np.all(np.isnan(out))
+
+
+def test_counter_stream_definition(oracle_lib):
+    """The COUNTER labelling: sample s's key is word s mod 4 of
+    Philox-4x32-10 (key = seed) with counter (s / 4, permutation, set, 0);
+    the n_A samples with the smallest (key, s) form class 0; permutation 0
+    is the unpermuted labelling.  Recomputed here from single Philox calls
+    (n not a multiple of 4, ties broken by sample index)."""
+    O = oracle_lib
+    seed, set_id, n, nA = 0x1234_5678_9ABC_DEF0, 3, 103, 41
+    labels0 = np.concatenate([np.zeros(nA, np.uint8), np.ones(n - nA, np.uint8)])
+    R = 6
+    got = O.counter_labels(seed, set_id, labels0, R)
+    assert np.array_equal(got[0], labels0)
+    key = [seed & 0xFFFFFFFF, seed >> 32]
+    for perm in range(1, R):
+        keys = np.zeros(n, np.uint64)
+        for s4 in range((n + 3) // 4):
+            o = O.philox([s4, perm, set_id, 0], key)
+            for j in range(4):
+                if 4 * s4 + j < n:
+                    keys[4 * s4 + j] = o[j]
+        order = np.lexsort((np.arange(n), keys))  # by key, then sample
+        want = np.ones(n, np.uint8)
+        want[order[:nA]] = 0
+        assert np.array_equal(got[perm], want), perm
+        assert int((got[perm] == 0).sum()) == nA
+
+
+def test_philox_known_answers(oracle_lib):
+    """Philox-4x32-10 against the known-answer vectors published with
+    Random123 (Salmon, Moraes, Dror, Shaw, SC'11): counter, key -> output."""
+    kat = [([0, 0, 0, 0], [0, 0], [0x6627e8d5, 0xe169c58d, 0xbc57ac4c, 0x9b00dbd8]),
+           ([0xffffffff] * 4, [0xffffffff] * 2, [0x408f276d, 0x41c83b0e, 0xa20bc7c6, 0x6d5451fd]),
+           ([0x243f6a88, 0x85a308d3, 0x13198a2e, 0x03707344], [0xa4093822, 0x299f31d0],
+            [0xd16cfe09, 0x94fdcceb, 0x5001e420, 0x24126ea1])]
+    for ctr, key, want in kat:
+        assert [int(x) for x in oracle_lib.philox(ctr, key)] == want
