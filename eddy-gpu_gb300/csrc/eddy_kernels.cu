@@ -1587,14 +1587,15 @@ cudaError_t launch_units(const SetDev &sd, const BatchDev &bd, cudaStream_t st) 
   k_units<<<bd.B, threads, smem, st>>>(sd, bd);
   e = cudaGetLastError();
   if (e != cudaSuccess) return e;
-  // units per warp: as many as keep about eight warps per SM busy
-  static int sms = 0;
-  if (sms == 0) {
-    int dev = 0;
+  // units per warp: as many as keep about eight warps per SM busy (the SM
+  // count read once, thread-safely, from the current device)
+  static const int sms = [] {
+    int dev = 0, v = 0;
     if (cudaGetDevice(&dev) != cudaSuccess ||
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
-      sms = 148;
-  }
+        cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || v < 1)
+      v = 148;
+    return v;
+  }();
   const int upw = std::max(1, std::min(32, bd.B / (sms * kJsWarps)));
   const int warps = (bd.B + upw - 1) / upw;
   k_js<<<(warps + kJsWarps - 1) / kJsWarps, 32 * kJsWarps, 0, st>>>(sd, bd, upw);
