@@ -15,10 +15,11 @@
 // with cudaGetSymbolAddress while that device is current and caches it; make
 // that first call before any stream capture.  All calls share the array and
 // each call rewrites every region it reads, so nothing carries over from the
-// previous call.  Calls from one process are serialised by a lock (each call
-// ends with a stream synchronisation); calls whose GPU work overlaps (other
-// processes sharing the context, or work the caller enqueues on the array
-// by other means) race on it.
+// previous call.  Calls from one process are serialised by a lock, and each
+// call, including one that fails after it has queued work, waits for its
+// stream before it returns; calls whose GPU work overlaps (other processes
+// sharing the context, or work the caller enqueues on the array by other
+// means) race on it.
 #include <cuda_runtime.h>
 #include <math.h>
 #include <string.h>
@@ -74,11 +75,18 @@ std::mutex g_call;
 int64_t g_lg_host[kDivisors * (kNAMaxSamples + 1)];
 int8_t g_vals_host[kNAMaxGenes * kNAMaxSamples];
 
+// Once per device, with that device current: the array's device address
+// and the BDeu divisor map in constant memory (the map is the same for
+// every sample count, so later calls never rewrite it).
 int setup_device(int dev, unsigned char **out) {
   if (dev < 0 || dev >= 64) return EDDY_ERR_ARG;
   if (!g_slots[dev].ptr) {
     void *p = nullptr;
     if (cudaGetSymbolAddress(&p, g_noalloc) != cudaSuccess || p == nullptr) return EDDY_ERR_CUDA;
+    int shift = 0;
+    int8_t dmap[82];
+    bdeu_table_into(1, g_lg_host, shift, dmap);
+    if (set_divisor_map(dmap) != cudaSuccess) return EDDY_ERR_CUDA;
     g_slots[dev].ptr = (unsigned char *)p;
   }
   *out = g_slots[dev].ptr;
@@ -125,18 +133,25 @@ extern "C" int eddy_unit_noalloc(const eddy_opts *opts, const int8_t *vals, int 
   int shift = 0;
   int8_t dmap[82];
   bdeu_table_into(n, g_lg_host, shift, dmap);
+  // From the first enqueue on, an error return first waits for this call's
+  // work on the stream (ignoring that wait's own status): the lock must not
+  // be released while copies or kernels of this call may still use the
+  // shared array.
+  auto bail = [st](int code) {
+    cudaStreamSynchronize(st);
+    return code;
+  };
   if (cudaMemcpyAsync(base + kOffLg, g_lg_host, 8ull * kDivisors * (n + 1), cudaMemcpyHostToDevice,
                       st) != cudaSuccess)
-    return EDDY_ERR_CUDA;
-  if (set_divisor_map(dmap) != cudaSuccess) return EDDY_ERR_CUDA;
+    return bail(EDDY_ERR_CUDA);
   if (cudaMemcpyAsync(base + kOffVals, v8, (size_t)g * n, cudaMemcpyHostToDevice, st) != cudaSuccess ||
       cudaMemcpyAsync(base + kOffMask, mask, 8ull * W, cudaMemcpyHostToDevice, st) != cudaSuccess ||
       cudaMemcpyAsync(base + kOffPrior, pbits, (size_t)c, cudaMemcpyHostToDevice, st) != cudaSuccess)
-    return EDDY_ERR_CUDA;
+    return bail(EDDY_ERR_CUDA);
   if (launch_prep((const int8_t *)(base + kOffVals), g, n, W, c, (uint64_t *)(base + kOffPlanes),
                   (uint64_t *)(base + kOffValid), (uint16_t *)(base + kOffCtot),
                   (int8_t *)(base + kOffValsT), st) != cudaSuccess)
-    return EDDY_ERR_CUDA;
+    return bail(EDDY_ERR_CUDA);
 
   SetDev sd{};
   sd.g = g;
@@ -174,7 +189,7 @@ extern "C" int eddy_unit_noalloc(const eddy_opts *opts, const int8_t *vals, int 
     if (cudaMemsetAsync(base + kOffDmask, 0, dmask_bytes(1, c), st) != cudaSuccess ||
         launch_pairs(sd, (const uint64_t *)(base + kOffMask), (uint32_t *)(base + kOffDmask), 1,
                      nullptr, st) != cudaSuccess)
-      return EDDY_ERR_CUDA;
+      return bail(EDDY_ERR_CUDA);
     BatchDev bd{};
     bd.B = 1;
     bd.kmax = kNAKmax;
@@ -187,11 +202,11 @@ extern "C" int eddy_unit_noalloc(const eddy_opts *opts, const int8_t *vals, int 
     bd.status = d_status;
     bd.keep_slot = nullptr;
     bd.stats = nullptr;
-    if (launch_units(sd, bd, st) != cudaSuccess) return EDDY_ERR_CUDA;
+    if (launch_units(sd, bd, st) != cudaSuccess) return bail(EDDY_ERR_CUDA);
     unsigned char out[16];
-    if (cudaMemcpyAsync(out, base + kOffOut, 16, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
-        cudaStreamSynchronize(st) != cudaSuccess)
-      return EDDY_ERR_CUDA;
+    if (cudaMemcpyAsync(out, base + kOffOut, 16, cudaMemcpyDeviceToHost, st) != cudaSuccess)
+      return bail(EDDY_ERR_CUDA);
+    if (cudaStreamSynchronize(st) != cudaSuccess) return EDDY_ERR_CUDA;
     uint32_t status;
     memcpy(js, out, 8);
     memcpy(unique, out + 8, 4);

@@ -194,8 +194,9 @@ int eddy_write_edge_list(const char *path, const char *const *genes, int g, cons
  * NULL.  *js and *unique receive the JS (NaN when U == 1) and U.
  * The first call on a device looks up the array's device address (call it
  * once before any stream capture).  Calls share the array: one process's
- * calls are serialised by a lock and each call ends with a stream
- * synchronisation; GPU work that overlaps a call from elsewhere races. */
+ * calls are serialised by a lock and each call, also one that fails after
+ * queueing work, ends with a stream synchronisation; GPU work that
+ * overlaps a call from elsewhere races. */
 int eddy_unit_noalloc(const eddy_opts *opts, const int8_t *vals, int g, int n,
                       const uint8_t *labels, const uint8_t *prior, void *stream, double *js,
                       int32_t *unique);

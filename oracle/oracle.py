@@ -33,13 +33,18 @@ class UnitResult(C.Structure):
                 ("total_edges", C.c_int), ("uni_edges_total", C.c_int)]
 
 
-def build(ref: bool | None = None) -> None:
-    """Compile liboracle.so (and _ref/ when the reference sources exist)."""
+def build(ref: bool | None = None, ref_root: str | None = None) -> None:
+    """Compile liboracle.so, and _ref/ from the reference sources under
+    ref_root (or $EDDY_REFERENCE_ROOT) when that directory holds them."""
     subprocess.run(["make", "-s", "-C", HERE, "all"], check=True)
-    refroot = os.environ.get("EDDY_REFERENCE_ROOT", "/root/reference")
+    refroot = ref_root or os.environ.get("EDDY_REFERENCE_ROOT")
+    have = bool(refroot) and os.path.isfile(os.path.join(refroot, "kernel1.cu"))
     if ref is None:
-        ref = os.path.isfile(os.path.join(refroot, "kernel1.cu"))
+        ref = have
     if ref:
+        if not have:
+            raise FileNotFoundError("the reference sources were not found: pass ref_root "
+                                    "or set EDDY_REFERENCE_ROOT")
         subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF={refroot}"],
                        check=True)
 

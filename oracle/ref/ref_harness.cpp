@@ -1,7 +1,7 @@
 /*
  * ref_harness.cpp -- runs the reference's own kernels (kernel1.cu ..
  * kernel5.cu) and host routines (routines.cu) on the CPU, compiled from the
- * reference sources where they lie (see oracle/ref/Makefile), through a
+ * reference sources where they lie (the `ref` target of oracle/Makefile), through a
  * small CUDA-thread emulator.  TEST INFRASTRUCTURE ONLY: it produces the
  * golden vectors under tests/golden that pin the oracle restatement.
  *

@@ -5,7 +5,7 @@
  * kernel bodies run here as the strongest parity pin for the oracle.
  *
  * CUDA qualifiers become empty; blockIdx/threadIdx/blockDim/gridDim are
- * globals set by the emulator (ref_emu.cpp) before a simulated thread runs;
+ * globals set by the emulator (ref_harness.cpp) before a simulated thread runs;
  * __syncthreads() yields to the emulator's block scheduler, which runs every
  * simulated thread of the block up to the barrier before any goes on.
  * Device malloc/free/printf map to the C library; abs/min/lgamma/log/exp/pow

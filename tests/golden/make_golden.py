@@ -13,7 +13,7 @@ gammds.npz (the host AS 147 twin on a grid) and writers.json (output files
 of the reference's writers).  Only runnable where the reference sources
 exist; the fixtures it writes are committed.
 
-    python tests/golden/make_golden.py
+    EDDY_REFERENCE_ROOT=<reference root> python tests/golden/make_golden.py
 """
 import json
 import os

@@ -68,7 +68,7 @@ def _set(rng, G, pairs, extra):
 
 
 @pytest.mark.parametrize("rng_mode", ["counter", "glibc"])
-def test_many_sets_one_launch(eddy_lib, oracle_lib, rng_mode):
+def test_many_sets_in_one_run(eddy_lib, oracle_lib, rng_mode):
     rng = np.random.default_rng(41)
     G, n, nA = 60, 160, 70
     data, labels0 = _data(rng, G, n, nA)

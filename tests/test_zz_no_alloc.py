@@ -3,9 +3,10 @@ memory (a host application owning all device memory through its own pool,
 or a pipeline that must avoid cudaFree's device-wide synchronisation): it
 runs one labelling with every intermediate in a fixed array compiled into
 the library.  Its results must equal the allocating entry point's
-(eddy_run_labellings) on the same inputs, on two calls in a row; sizes past
-its limits (64 genes, 2048 samples) are refused.  This file is collected
-last so a stop-at-first-failure run has run everything else first."""
+(eddy_run_labellings) and the oracle's on the same inputs, on two calls in
+a row, up to its limit shape (64 genes x 2048 samples); sizes past that
+limit are refused.  This file is collected last so a stop-at-first-failure
+run has run everything else first."""
 import numpy as np
 import pytest
 
@@ -23,8 +24,10 @@ def _data(rng, g, n, nA):
 
 
 @pytest.mark.parametrize("g,n,nA,mp,bonf,npr", [(20, 200, 100, 3, False, 4),
-                                                 (48, 300, 120, 4, True, 0)])
-def test_noalloc_matches_allocating_entry_point(g, n, nA, mp, bonf, npr, eddy_lib):
+                                                 (48, 300, 120, 4, True, 0),
+                                                 (64, 2048, 900, 3, True, 6)])
+def test_noalloc_matches_allocating_entry_point(g, n, nA, mp, bonf, npr, eddy_lib,
+                                                oracle_lib):
     rng = np.random.default_rng(g * 31 + n)
     data = _data(rng, g, n, nA)
     labels0 = np.concatenate([np.zeros(nA, np.uint8), np.ones(n - nA, np.uint8)])
@@ -44,11 +47,17 @@ def test_noalloc_matches_allocating_entry_point(g, n, nA, mp, bonf, npr, eddy_li
         lab[rng.choice(n, nA, replace=False)] = 0
         labs.append(lab)
     ref_js, ref_U = ctx.run_labellings(sid, np.stack(labs))
+    prm = oracle_lib.params(mp=mp, pw=0.5, bonferroni=bonf)
+    o_js, o_U = oracle_lib.units(data, np.stack(labs), pr, prm)
+
+    def close(a, b):
+        return (np.isnan(a) and np.isnan(b)) or abs(a - b) <= JS_RTOL * abs(b) + JS_ATOL
+
     for t in range(2):  # two calls in a row share the fixed array
         js, U = eddy_lib.unit_noalloc(ctx.opts, data, labs[t], pr)
-        assert U == ref_U[t]
-        assert (np.isnan(js) and np.isnan(ref_js[t])) or \
-            abs(js - ref_js[t]) <= JS_RTOL * abs(ref_js[t]) + JS_ATOL, (js, ref_js[t])
+        assert U == ref_U[t] == o_U[t], (U, ref_U[t], o_U[t])
+        assert close(js, ref_js[t]), (js, ref_js[t])
+        assert close(js, o_js[t]), (js, o_js[t])
     ctx.close()
 
 
