@@ -96,6 +96,9 @@ struct SetHost {
   std::vector<int32_t> ids, nodes, epn, edges;
   std::vector<double> lval;
   std::vector<int32_t> el_nodes, el_epn, el_edges;
+  // changed-node records per network that the set's units needed so far
+  // (0: none beyond the default): later batches of the set start there
+  int kmax_hint = 0;
 };
 
 }  // namespace
@@ -465,12 +468,23 @@ int run_units(eddy_ctx *ctx, SetRun &sr, int nunits, const uint64_t *masks_host,
   // kmax: changed-node records per network (EDDY_KMAX lowers it, to test the
   // re-run of the units that overflow it)
   int kmax = 16;
-  if (const char *ek = getenv("EDDY_KMAX")) kmax = std::max(1, std::min(16, atoi(ek)));
+  const char *ek = getenv("EDDY_KMAX");
+  if (ek) kmax = std::max(1, std::min(16, atoi(ek)));
+  else if (sr.set_id >= 0) kmax = std::max(kmax, std::min(g + 1, ctx->sets[sr.set_id].kmax_hint));
   size_t per_unit = unit_scratch_bytes(c, S, kmax) + sizeof(uint32_t) * (size_t)c + 8 * W + 64;
   // (up to 16 GB and 16384 units per batch: the general-path queue holds
   // unit indices below 2^15)
   int Bmax = (int)std::max<size_t>(1, ((size_t)16 << 30) / std::max<size_t>(per_unit, 1));
   Bmax = std::min(Bmax, 16384);
+  // the general-path queue has room for every table of a batch, up to 2^28
+  // (near-threshold sets queue most of them); the units are then split into
+  // batches of equal size, which later calls of the same size replay
+  Bmax = (int)std::min<size_t>((size_t)Bmax,
+                               std::max<size_t>(1, ((size_t)1 << 28) / (2 * (size_t)std::max(c, 1))));
+  {
+    const int nb = std::max(1, (nunits + Bmax - 1) / Bmax);
+    Bmax = std::max(1, (nunits + nb - 1) / nb);
+  }
   std::vector<uint32_t> status;
   const int mpk = std::max(1, mpk_req);
   if (keeping) {
@@ -671,10 +685,12 @@ int run_units(eddy_ctx *ctx, SetRun &sr, int nunits, const uint64_t *masks_host,
       t_units += bms;
       std::vector<int> again;
       bool overflow = false, collision = false;
+      int need = 0;  // most changed nodes of a network in an overflowed unit
       for (int i = 0; i < Bt; i++) {
         const int u = b0 + todo[i];
         if (status[i] & kUnitKmaxOverflow) {
           overflow = true;
+          need = std::max(need, (int)(status[i] >> 16));
           again.push_back(todo[i]);
         } else if (status[i] & kUnitHashCollision) {
           collision = true;
@@ -717,7 +733,16 @@ int run_units(eddy_ctx *ctx, SetRun &sr, int nunits, const uint64_t *masks_host,
         memcpy(keep->lval.data(), hk + o_lval, b_dist);
         memcpy(keep->rows.data(), hk + o_rows, b_rows);
       }
-      if (overflow) kmax_run = g + 1;
+      if (overflow) {
+        // the re-run holds every record these units need (their networks do
+        // not change); the set's later batches start with a quarter more
+        const int want = std::max(need, kmax_run + 1);
+        kmax_run = std::min(g + 1, (want + 7) / 8 * 8);
+        if (!ek && sr.set_id >= 0) {
+          int &hint = ctx->sets[sr.set_id].kmax_hint;
+          hint = std::max(hint, std::min(g + 1, (want + want / 4 + 7) / 8 * 8));
+        }
+      }
       if (collision) {
         ctx->salt = ctx->salt * 6364136223846793005ull + 1442695040888963407ull;
         sd.salt = ctx->salt;

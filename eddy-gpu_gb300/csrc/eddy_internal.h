@@ -16,7 +16,9 @@ constexpr int kDofSlots = 3;        // dof 1, 2, 4 (dof 0 never gives an edge)
 constexpr int kMaxBdeuParents = 3;  // kernel5.cu:119-130 caps at 1 + 3
 constexpr int kDivisors = 15;       // distinct q and q*r of the BDeu terms
 constexpr uint32_t kUnitOk = 0;
-constexpr uint32_t kUnitKmaxOverflow = 1u;   // more changed nodes than kmax
+constexpr uint32_t kUnitKmaxOverflow = 1u;   // more changed nodes than kmax;
+                                             // bits 16-31 then hold the most
+                                             // changed nodes of its networks
 constexpr uint32_t kUnitHashCollision = 2u;  // equal hash, unequal networks
 constexpr uint32_t kUnitBadShape = 4u;
 

@@ -281,7 +281,7 @@ constexpr unsigned kSmProbes = 64;
 
 struct UnitLayout {
   size_t phi[2], pcol[2], rec, htk, htv, dist, uid, urep, sig;
-  size_t skey, sbits, srep, hsk, hsv, wl, total;
+  size_t skey, sbits, srep, hsk, hsv, wl, ksc, total;
   int HT, rec_words;  // rec_words: 64-bit words per network record
 };
 
@@ -325,6 +325,8 @@ __host__ __device__ inline UnitLayout unit_layout(int c, int S, int kmax) {
   o = al(o + sizeof(int32_t) * (size_t)HT);
   L.wl = o;  // work list of networks
   o = al(o + sizeof(int32_t) * (size_t)S);
+  L.ksc = o;  // scores of the distinct changed-node keys: [HT][2 classes]
+  o = al(o + 2 * sizeof(int64_t) * (size_t)HT);
   L.total = o;
   return L;
 }
@@ -369,6 +371,7 @@ struct UnitSmem {
   int firstB0;  // first class-2 network equal to the class-2 full network
   int firstE2;  // first class-2 network with an empty signature (S - 1: none)
   int ncand;    // candidates for unique networks
+  int maxchg;   // most changed nodes of a network past kmax (0: none)
   int scan[32];
   unsigned status;
   int U;
@@ -577,6 +580,7 @@ __global__ void __launch_bounds__(256, 3) k_units(const __grid_constant__ SetDev
     SM.nphi[0] = SM.nphi[1] = 0;
     SM.ndab = 0;
     SM.status = 0;
+    SM.maxchg = 0;
     for (int a = 0; a < 2; a++)
       for (int b = 0; b < 2; b++) SM.base[a][b] = 0;
   }
@@ -1045,13 +1049,18 @@ __global__ void __launch_bounds__(256, 3) k_units(const __grid_constant__ SetDev
     if (lane == 0) {
       R[0] = SM.HF[k] + dh;
       R[1] = (unsigned long long)nchg;
-      if (nchg > bd.kmax) atomicOr(&SM.status, kUnitKmaxOverflow);
+      if (nchg > bd.kmax) {
+        atomicOr(&SM.status, kUnitKmaxOverflow);
+        atomicMax(&SM.maxchg, nchg);
+      }
     }
   }
   __syncthreads();
   if (SM.status & kUnitKmaxOverflow) {
     if (tid == 0) {
-      bd.status[u] = SM.status;
+      // bits 16-31: the records the unit needs (the host re-runs it with
+      // room for them)
+      bd.status[u] = SM.status | ((unsigned)min(SM.maxchg, 0xFFFF) << 16);
       bd.js[u] = __longlong_as_double(0x7ff8000000000000ll);
       bd.U[u] = -1;
     }
@@ -1335,30 +1344,102 @@ __global__ void __launch_bounds__(256, 3) k_units(const __grid_constant__ SetDev
       if ((int)((e >> (16 + 16 * q)) & 0xFFFF) != (int)P.fps[(k * g + t) * 3 + q]) return true;
     return false;
   };
-  bdeu_items(
-      sd, P, SM.scan, nchg_all,
-      [&](int e) -> unsigned long long {
-        int uu, k;
-        unsigned long long rec;
-        item_of(e, uu, k, rec);
-        if (!differs(k, rec)) return ~0ull;
-        return rec;  // t | np << 14 | parents: the item key format
-      },
-      [&](int e, long long s1, long long s2) {
-        int uu, k;
-        unsigned long long rec;
-        item_of(e, uu, k, rec);
-        if (!differs(k, rec)) return;
-        const int t = (int)(rec & 0x3FFF), np = (int)((rec >> 14) & 3);
-        if (np == 0) {
-          s1 = bdeu_score0(sd, t, P.cnt3);
-          s2 = bdeu_score0(sd, t, P.cnt3 + 3 * g);
-        }
-        atomicAdd((unsigned long long *)&dist[uu],
-                  (unsigned long long)(s1 - P.fsc[(k * 2 + 0) * g + t]));
-        atomicAdd((unsigned long long *)&dist[S + uu],
-                  (unsigned long long)(s2 - P.fsc[(k * 2 + 1) * g + t]));
-      });
+  // the score delta of item e, given its key's scores in both classes
+  auto add_delta = [&](int uu, int k, unsigned long long rec, long long s1, long long s2) {
+    const int t = (int)(rec & 0x3FFF), np = (int)((rec >> 14) & 3);
+    if (np == 0) {
+      s1 = bdeu_score0(sd, t, P.cnt3);
+      s2 = bdeu_score0(sd, t, P.cnt3 + 3 * g);
+    }
+    atomicAdd((unsigned long long *)&dist[uu],
+              (unsigned long long)(s1 - P.fsc[(k * 2 + 0) * g + t]));
+    atomicAdd((unsigned long long *)&dist[S + uu],
+              (unsigned long long)(s2 - P.fsc[(k * 2 + 1) * g + t]));
+  };
+  // The leave-one-out networks of a unit share most of their changed nodes'
+  // lists (one flip near a threshold changes the same node in every network
+  // whose left-out sample triggers it), so the items hold few distinct keys
+  // (node, first three parents): ~260 among ~19500 items per unit when
+  // nearly every pair sits near the threshold.  Each distinct key is scored
+  // once, in a table of HT slots (the network table's, free after the dedup
+  // phase; the signature table's key array holds the list of keys), and
+  // every item adds its key's score.  More distinct keys than the table
+  // holds: every item is scored on its own.
+  unsigned long long *kslot = htk;
+  int *kidx = htv;
+  unsigned long long *klist = hsk;
+  long long *ksc = (long long *)(scr + L.ksc);
+  const unsigned kmask = (unsigned)HT - 1u;
+  for (int i = tid; i < HT; i += nt) kslot[i] = ~0ull;
+  if (tid == 0) SM.tfull = 0;
+  __syncthreads();
+  for (int e = tid; e < nchg_all; e += nt) {
+    int uu, k;
+    unsigned long long rc;
+    item_of(e, uu, k, rc);
+    if (!differs(k, rc)) continue;
+    unsigned slot = (unsigned)(mix64(rc) & kmask);
+    bool placed = false;
+    for (int pr = 0; pr < HT; pr++, slot = (slot + 1u) & kmask) {
+      const unsigned long long prev = atomicCAS(&kslot[slot], ~0ull, rc);
+      if (prev == ~0ull || prev == rc) {
+        placed = true;
+        break;
+      }
+    }
+    if (!placed) SM.tfull = 1;
+  }
+  __syncthreads();
+  if (!SM.tfull) {
+    // the keys in slot order: key list and slot -> list index
+    int nk = 0;
+    for (int i0 = 0; i0 < HT; i0 += nt) {
+      const int i = i0 + tid;
+      const bool has = i < HT && kslot[i] != ~0ull;
+      int total;
+      const int off = block_scan(has ? 1 : 0, total, SM.scan);
+      if (has) {
+        kidx[i] = nk + off;
+        klist[nk + off] = kslot[i];
+      }
+      nk += total;
+    }
+    __syncthreads();
+    bdeu_items(
+        sd, P, SM.scan, nk, [&](int i) -> unsigned long long { return klist[i]; },
+        [&](int i, long long s1, long long s2) {
+          ksc[2 * i] = s1;
+          ksc[2 * i + 1] = s2;
+        });
+    __syncthreads();
+    for (int e = tid; e < nchg_all; e += nt) {
+      int uu, k;
+      unsigned long long rc;
+      item_of(e, uu, k, rc);
+      if (!differs(k, rc)) continue;
+      unsigned slot = (unsigned)(mix64(rc) & kmask);
+      while (kslot[slot] != rc) slot = (slot + 1u) & kmask;
+      const int i = kidx[slot];
+      add_delta(uu, k, rc, ksc[2 * i], ksc[2 * i + 1]);
+    }
+  } else {
+    bdeu_items(
+        sd, P, SM.scan, nchg_all,
+        [&](int e) -> unsigned long long {
+          int uu, k;
+          unsigned long long rec;
+          item_of(e, uu, k, rec);
+          if (!differs(k, rec)) return ~0ull;
+          return rec;  // t | np << 14 | parents: the item key format
+        },
+        [&](int e, long long s1, long long s2) {
+          int uu, k;
+          unsigned long long rec;
+          item_of(e, uu, k, rec);
+          if (!differs(k, rec)) return;
+          add_delta(uu, k, rec, s1, s2);
+        });
+  }
 
   // ---- P6: unique count and status; the normalisation and JS follow in
   // k_js (up to 32 units per warp) from the fixed-point scores in dist

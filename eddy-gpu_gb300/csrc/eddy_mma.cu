@@ -1095,9 +1095,13 @@ size_t mma_y_bytes(const SetDev &sd) {
 int mma_bpad(int B) { return (B + kTM - 1) / kTM * kTM; }
 static size_t a_operand_bytes(int B, int n) { return (size_t)mma_bpad(B) * mma_npad(n); }
 // the A operand, then the general-path queue: a 16-byte counter and room
-// for 1/8 of the batch's tables (at least 65536)
+// for every table of the batch (near-threshold workloads send half of them
+// or more to the general path), at least 65536 and at most 2^28 items
+// (7.5 GB with the deferred list; the list's entries, item * 10 + slot,
+// stay below 2^32)
 static unsigned queue_cap(int B, int c) {
-  const size_t t = (size_t)B * (c > 0 ? c : 1) * 2 / 8;
+  const size_t all = (size_t)B * (c > 0 ? c : 1) * 2;
+  const size_t t = all < ((size_t)1 << 28) ? all : ((size_t)1 << 28);
   return (unsigned)(t < 65536 ? 65536 : t);
 }
 // EDDY_GENERAL_QUEUE_CAP lowers the queue's capacity (tests of the

@@ -265,7 +265,13 @@ int or_unique(int nets, int g, const int *pnodes, const int *edges_pn,
 
 /* --------------------------------------------------------------- K5 */
 
-/* kernel5.cu:4-236 (njLoop + bDeu3) for one (class, network, node). */
+/* kernel5.cu:4-236 (njLoop + bDeu3) for one (class, network, node).  The
+ * counts N_ijk of kernel5.cu:30-110 (parent configuration j in mixed radix
+ * over the parents' observed states, parent 1 fastest; child state k among
+ * the node's observed states) are tallied in one pass over the samples: a
+ * sample whose node or parent value is not an observed state (a value
+ * outside -1/0/1) matches no configuration, as in the reference's scan.
+ * The lgamma terms are then summed in the reference's order (j, then k). */
 double or_bdeu_node(int g, int ns, const int8_t *data, const int *ppn,
                     const int *stf, int node, int nparents,
                     const int *parents) {
@@ -275,45 +281,41 @@ double or_bdeu_node(int g, int ns, const int8_t *data, const int *ppn,
   int pa[4];
   pa[0] = node;
   for (int k = 0; k < noParents - 1; k++) pa[k + 1] = parents[k];
-  static const int stateSs[3] = {-1, 0, 1};
-  int stateVal[3];
-  int r = ppn[node], pos = 0;
-  for (int i = 0; i < 3; i++)
-    if (stf[3 * node + i] == 1) stateVal[pos++] = stateSs[i];
+  /* rank of each value -1/0/1 among a gene's observed states (-1 = none) */
+  int rank[4][3];
+  for (int i = 0; i < noParents; i++) {
+    int sc = 0;
+    for (int st = 0; st < 3; st++) rank[i][st] = stf[pa[i] * 3 + st] != 0 ? sc++ : -1;
+  }
+  const int r = ppn[node];
   int q = 1;
   for (int i = 1; i < noParents; i++) q *= ppn[pa[i]];
+  /* q <= 27 and r <= 3 (three observed states at most) */
+  int nijk[27][3];
+  memset(nijk, 0, sizeof nijk);
+  for (int s = 0; s < ns; s++) {
+    const int v0 = data[(size_t)node * ns + s];
+    if (v0 < -1 || v0 > 1 || rank[0][v0 + 1] < 0) continue;
+    int j = 0, div = 1, ok = 1;
+    for (int i = 1; i < noParents && ok; i++) {
+      const int v = data[(size_t)pa[i] * ns + s];
+      if (v < -1 || v > 1 || rank[i][v + 1] < 0) {
+        ok = 0;
+        break;
+      }
+      j += rank[i][v + 1] * div;
+      div *= ppn[pa[i]];
+    }
+    if (ok && rank[0][v0 + 1] < r) nijk[j][rank[0][v0 + 1]]++;
+  }
   const int nPrime = 4;
   double sum2 = 0.0;
   for (int j = 0; j < q; j++) {
-    int idx[4], val[4];
-    int div = 1;
-    for (int p2 = 1; p2 < noParents; p2++) {
-      idx[p2] = (j / div) % ppn[pa[p2]];
-      div *= ppn[pa[p2]];
-    }
-    for (int p3 = 1; p3 < noParents; p3++) {
-      int sc = 0;
-      for (int st = 0; st < 3; st++)
-        if (stf[pa[p3] * 3 + st] != 0) {
-          if (sc == idx[p3]) val[p3] = stateSs[st];
-          sc++;
-        }
-    }
-    int nijk[3] = {0, 0, 0}, nij = 0;
-    for (int k = 0; k < r; k++) {
-      int cnt = 0;
-      for (int s = 0; s < ns; s++) {
-        int ok = (data[(size_t)node * ns + s] == stateVal[k]);
-        for (int p3 = 1; p3 < noParents && ok; p3++)
-          ok = (data[(size_t)pa[p3] * ns + s] == val[p3]);
-        cnt += ok;
-      }
-      nijk[k] = cnt;
-      nij += cnt;
-    }
+    int nij = 0;
+    for (int k = 0; k < r; k++) nij += nijk[j][k];
     double sum1 = 0.0;
     for (int k = 0; k < r; k++)
-      sum1 += lgamma((double)nijk[k] + (double)nPrime / (double)(q * r)) -
+      sum1 += lgamma((double)nijk[j][k] + (double)nPrime / (double)(q * r)) -
               lgamma((double)nPrime / (double)(q * r));
     sum2 += lgamma((double)nPrime / (double)q) -
             lgamma((double)nij + (double)nPrime / (double)q) + sum1;
@@ -441,10 +443,12 @@ void or_unit(int g, int n, const int8_t *data, const uint8_t *labels,
 
   /* K5 per class / unique network / node, run4 (kernel5.cu:237-257) */
   double *out5 = (double *)malloc(sizeof(double) * 2 * (size_t)U * g);
-  for (int cls = 0; cls < 2; cls++) {
+#pragma omp parallel for schedule(dynamic, 8)
+  for (int cu = 0; cu < 2 * U; cu++) {
+    const int cls = cu / U, u = cu % U;
     const int8_t *d = cls ? dB : dA;
     int ns = cls ? nB : nA;
-    for (int u = 0; u < U; u++) {
+    {
       int Eu = uepn[u + 1] - uepn[u];
       for (int t = 0; t < g; t++) {
         int np = (t == g - 1) ? Eu - un[(size_t)u * g + t]
@@ -490,17 +494,30 @@ int or_units(int g, int n, const int8_t *data, int R, const uint8_t *labels,
 #ifdef _OPENMP
   int prev = omp_get_max_threads();
   if (threads > 0) omp_set_num_threads(threads);
-  /* parallel over labellings; the per-network loop inside runs serially */
+  /* parallel over labellings (one level: loops inside a unit then run
+   * serially), or inside each unit when labellings are fewer than threads */
   int nested = omp_get_max_active_levels();
   omp_set_max_active_levels(1);
 #endif
+  if (R >= omp_get_max_threads()) {
 #pragma omp parallel for schedule(dynamic, 1)
-  for (int r = 0; r < R; r++) {
-    or_unit_result res;
-    or_unit(g, n, data, labels + (size_t)r * n, prior, p, &res, NULL, NULL,
-            NULL, NULL, NULL, NULL, NULL);
-    js[r] = res.js;
-    U[r] = res.U;
+    for (int r = 0; r < R; r++) {
+      or_unit_result res;
+      or_unit(g, n, data, labels + (size_t)r * n, prior, p, &res, NULL, NULL,
+              NULL, NULL, NULL, NULL, NULL);
+      js[r] = res.js;
+      U[r] = res.U;
+    }
+  } else {
+    /* fewer labellings than threads: one at a time, each unit's network
+     * and BDeu loops parallel (the results do not depend on the split) */
+    for (int r = 0; r < R; r++) {
+      or_unit_result res;
+      or_unit(g, n, data, labels + (size_t)r * n, prior, p, &res, NULL, NULL,
+              NULL, NULL, NULL, NULL, NULL);
+      js[r] = res.js;
+      U[r] = res.U;
+    }
   }
 #ifdef _OPENMP
   omp_set_max_active_levels(nested);
