@@ -3,10 +3,11 @@ units per second, exact edges.
 
 Workload (one gene set, the largest single-GPU configuration the metric is
 quoted on): 200 genes x 1000 samples (classes 400/600), -mp 4, the -r 10000
-permutation test; synthetic seeded data with the shapes of the "precision
-stress" workload (eddy_gpu/synth.py config 4).  One step = one batch of
-`--units` permutations of that set (default 10000: the whole -r 10000 run,
-which the library decides as one batch).
+permutation test; synthetic seeded data of the "precision stress" workload
+(eddy_gpu/synth.py config 4: every gene loads on one latent factor, so the
+pair tests sit near the Bonferroni edge threshold; the measured near-threshold
+fractions are reported in `config`).  One step = `--units` permutations of
+that set (default 10000: the whole -r 10000 run).
 
   value  device time of the hot path with the set resident in HBM (CUDA
          events on the library's launching stream around K steps; labellings
@@ -16,7 +17,10 @@ which the library decides as one batch).
          (iteration 0 with its networks, the permutations, the beta fit) and
          the JS values read back.
   cpu_baseline  the oracle (CPU restatement of the reference kernels, FP64,
-         OpenMP over units) on a bounded sample of the same units.
+         OpenMP over units, or inside a unit when units are fewer than
+         threads) on a bounded sample of the same units.
+  precision  edge decisions of every network, node-summed BDeu, JS, U and
+         the pDDN of one eddy_run, against the FP64 oracle on that sample.
 
 `--impl reference` runs the reference's algorithm on the host cores (the
 oracle port: the reference's own hot path exists only as CUDA kernels; its
@@ -45,7 +49,8 @@ import numpy as np  # noqa: E402
 
 METRIC = "gene-set x permutations/sec, batched FP32 vs plain FP64 on one GB300, exact edges"
 UNIT = "units/s"
-WORKLOAD = "config 4: one 200-gene set x 1000 samples (400/600), -mp 4, permutations of -r 10000"
+WORKLOAD = ("config 4 (precision stress): one 200-gene set x 1000 samples (400/600), -mp 4, "
+            "permutations of -r 10000")
 
 
 def load_peaks():
@@ -57,16 +62,20 @@ def load_peaks():
     return 6800.0, 1900.0, "fallback"
 
 
-def algorithmic_bytes(g, n, mp):
-    """Per-unit algorithmic bytes of the network kernel (k_units) as the
-    fused design must move them: the c 4-byte leave-one-out decision masks
-    and the unit's class mask read, JS, U and status written.  (The unfused
-    stage-by-stage model, S x c edge bits written and read back plus S x g x
-    mp parent entries, would be ~4.5 MB per unit at 200 genes x 1000
-    samples; the kernel never materialises those.)"""
+def algorithmic_bytes(g, n, mp, U):
+    """Per-unit algorithmic bytes of the network stages (k_units + k_js:
+    network assembly, dedup, BDeu, normalisation and JS) when each stage reads
+    its inputs and writes its outputs once through HBM: the S x c edge bits
+    of the S leave-one-out networks read, S x g x mp 16-bit parent entries and
+    an 8-byte hash per network written, the U unique networks' parent sets
+    (16-bit) and the set's data (2 x g x n bytes) read by BDeu, two 8-byte
+    scores per unique network and node written, and the JS written.  U is
+    the measured mean of unique networks per unit.  The kernel keeps the edge
+    bits and lists on chip, so this is the work it stands for, not the bytes
+    it moves (those are `traffic`)."""
     c = g * (g - 1) // 2
-    W = (n + 63) // 64
-    return 4 * c + 8 * W + 16
+    S = n + 2
+    return S * c / 8 + S * g * mp * 2 + 8 * S + U * g * mp * 2 + 2 * g * n + 16 * U * g + 8
 
 
 class ClockSampler:
@@ -145,6 +154,52 @@ def cpu_sample(w, genes, seed, first, count, threads):
     return count / dt, dt, js, U
 
 
+def precision_vs_oracle(eddy_gpu, oracle, w, genes, seed, labs, ojs, oU):
+    """The GPU against the FP64 oracle on the sampled labellings: one
+    eddy_run over them (the unpermuted labelling and the permutations of
+    the counter stream) for JS, U and pDDN; every edge decision of every
+    network and the node-summed BDeu of every unique network for the first
+    two labellings."""
+    mp, pw = w.flags["mp"], w.flags["pw"]
+    prm = oracle.params(mp=mp, pw=pw)
+    R = labs.shape[0]
+    ctx = eddy_gpu.Context(max_parents=mp, prior_weight=pw, permutations=R,
+                           rng=eddy_gpu.RNG_COUNTER, seed=seed, keep_networks=True)
+    ctx.load_matrix(w.data, w.labels)
+    sid = ctx.add_set(genes)
+    ctx.run()
+    gjs, gU = ctx.js(sid)
+    summ = ctx.summary(sid)
+    rc, _, _, opd = oracle.pddn(ojs)
+    data = w.data[genes]
+    tests = agree = 0
+    bdeu_err = 0.0
+    ids_equal = True
+    for r in range(min(2, R)):
+        o = oracle.unit(data, labs[r], None, prm)
+        e = ctx.debug_edges(sid, labs[r])
+        tests += e.size
+        agree += int((e == o["edges"]).sum())
+        d = ctx.debug_unit(sid, labs[r], min(mp, 3))
+        ids_equal &= bool(np.array_equal(d["ids"], o["unique_ids"]))
+        od = o["out5"].sum(axis=2)
+        if d["dist"].shape == od.shape:
+            bdeu_err = max(bdeu_err, float(np.max(np.abs(d["dist"] - od) / np.abs(od))))
+        else:
+            bdeu_err = float("inf")
+    ctx.close()
+    rel = np.abs(gjs - ojs) / np.maximum(np.abs(ojs), 1e-300)
+    return {"oracle_units": int(R),
+            "edge_decisions_compared": int(tests),
+            "edge_decision_agreement": agree / max(tests, 1),
+            "unique_ids_equal": ids_equal,
+            "unique_networks_equal": bool(np.array_equal(gU, oU)),
+            "bdeu_max_rel_err": bdeu_err,
+            "js_max_rel_err": float(np.max(rel)),
+            "pddn": summ["pddn"], "pddn_oracle": opd,
+            "pddn_rel_err": (abs(summ["pddn"] - opd) / abs(opd)) if rc == 0 and opd else None}
+
+
 def run_reference(args, rank, world):
     """Reference arm: the reference's hot path on the host cores (oracle
     port), same workload and metric; rank 0 only."""
@@ -156,7 +211,7 @@ def run_reference(args, rank, world):
     w = synth.make(4, seed=0)
     genes = w.sets[0][1]
     threads = os.cpu_count() or 1
-    per_step = args.cpu_units
+    per_step = args.ref_units
     for i in range(args.warmup):
         cpu_sample(w, genes, 4242, 1 + i * per_step, per_step, threads)[:2]
     t0 = time.perf_counter()
@@ -251,8 +306,11 @@ def run_ours(args, rank, world, local):
     # each rank its own permutation indices
     base = 1 + rank * (args.warmup + args.steps + 1) * B
 
+    u_mean = []
+
     def step(i):
         js, U = ctx.run_permutations(sid, base + i * B, B)
+        u_mean.append(float(np.mean(U)))
         t = ctx.timing()
         return t
 
@@ -348,9 +406,15 @@ def run_ours(args, rank, world, local):
     if rank != 0:
         return
     hbm, bf16, peak_kind = load_peaks()
-    bu = algorithmic_bytes(g, n, mp)
+    U_mean = float(np.mean(u_mean[-args.steps:]))
+    bu = algorithmic_bytes(g, n, mp, U_mean)
     c = g * (g - 1) // 2
-    launches_per_kernel = args.steps  # one launch of each kernel per step (B units)
+    # a step's units run as equal batches of at most 2^28 / (2 c) units (the
+    # library's general-path queue holds every table of a batch): one launch
+    # of each kernel per batch
+    batches = -(-B // min(16384, (1 << 28) // (2 * c)))
+    launches_per_kernel = args.steps * batches
+    Bl = B / batches  # units per launch
     traffic_info = {}
     tf = os.path.join(ROOT, "profiles", "traffic_config4.json")
     if os.path.exists(tf):
@@ -369,8 +433,8 @@ def run_ours(args, rank, world, local):
     # Gram matrix of the genes' state indicators); the GEMM the kernel runs
     # is smaller: 2 x cells x c x n per unit
     nA = int((np.asarray(w.labels) == 0).sum())
-    k1_flops = 2.0 * (3 * g) ** 2 * nA * B
-    k1_gemm = 2.0 * cells * c * n * B
+    k1_flops = 2.0 * (3 * g) ** 2 * nA * Bl
+    k1_gemm = 2.0 * cells * c * n * Bl
     e4m3 = 2.0 * bf16
     k1 = {"kernel": "k_pairs_mma", "bound": "tensor", "achieved": k1_flops / (k1_ms / 1e3) / 1e12,
           "peak": e4m3, "unit": "TFLOP/s", "ms_per_launch": k1_ms,
@@ -378,17 +442,19 @@ def run_ours(args, rank, world, local):
           "layout": f"{cells} counted cells per table",
           "gemm_flops_per_launch": k1_gemm,
           "gemm_frac": k1_gemm / (k1_ms / 1e3) / 1e12 / e4m3,
-          "traffic": traffic_info.get("k_pairs_mma_bytes_per_unit", 0) * B or None,
+          "traffic": traffic_info.get("k_pairs_mma_bytes_per_unit", 0) * Bl or None,
+          "units_per_launch": Bl,
           "ncu_sm_throughput_pct": traffic_info.get("k_pairs_mma_sm_throughput_pct"),
           "ncu_tensor_pipe_pct": traffic_info.get("k_pairs_mma_tensor_pipe_pct")}
     k1["frac"] = k1["achieved"] / e4m3
     # network assembly, dedup, BDeu, JS: algorithmic bytes (each stage's
     # inputs and outputs once through HBM)
     k2_ms = acc["ms_units"] / launches_per_kernel
-    k2 = {"kernel": "k_units", "bound": "hbm", "achieved": bu * B / (k2_ms / 1e3) / 1e9,
+    k2 = {"kernel": "k_units", "bound": "hbm", "achieved": bu * Bl / (k2_ms / 1e3) / 1e9,
           "peak": hbm, "unit": "GB/s", "ms_per_launch": k2_ms,
-          "algorithmic_bytes_per_launch": bu * B,
-          "traffic": traffic_info.get("k_units_bytes_per_unit", 0) * B or None,
+          "algorithmic_bytes_per_launch": bu * Bl, "unique_networks_per_unit": U_mean,
+          "units_per_launch": Bl,
+          "traffic": traffic_info.get("k_units_bytes_per_unit", 0) * Bl or None,
           # the kernel is bound by SM issue and latency, not HBM: the SM
           # throughput share from ncu (2048-unit launch) goes with the HBM one
           "ncu_sm_throughput_pct": traffic_info.get("k_units_sm_throughput_pct"),
@@ -402,18 +468,19 @@ def run_ours(args, rank, world, local):
     cpu = None
     precision = {"tables": int(stats["tables"]), "filtered": int(stats["filtered"]),
                  "exact_rechecks": int(stats["exact_rechecks"])}
+    # near-threshold share of the pair tests: the unpermuted labelling and
+    # the sampled permutations (host numpy; a property of the workload)
+    import oracle
+    R_s = args.cpu_units + 1
+    labs = oracle.counter_labels(seed, 0, w.labels, R_s)
+    near = synth.near_threshold(w.data[genes], labs)
     if world == 1 and not args.no_cpu:
         try:
-            cu, cs, ojs, oU = cpu_sample(w, genes, seed, 1, args.cpu_units, os.cpu_count() or 1)
+            cu, cs, ojs, oU = cpu_sample(w, genes, seed, 0, R_s, os.cpu_count() or 1)
             cpu = {"value": cu, "unit": UNIT, "cores": os.cpu_count() or 1, "kind": "port",
-                   "sample": f"{args.cpu_units} permutations of the same set ({cs:.1f} s)"}
-            # the same permutations on the GPU, against the FP64 oracle
-            ctx.clear_sets()
-            gjs, gU = ctx.run_permutations(ctx.add_set(genes), 1, args.cpu_units)
-            precision.update({
-                "oracle_units": args.cpu_units,
-                "unique_networks_equal": bool(np.array_equal(gU, oU)),
-                "js_max_rel_err": float(np.max(np.abs(gjs - ojs) / np.maximum(np.abs(ojs), 1e-300)))})
+                   "sample": f"{R_s} labellings of the same set: the unpermuted one and "
+                             f"{args.cpu_units} permutations ({cs:.1f} s)"}
+            precision.update(precision_vs_oracle(eddy_gpu, oracle, w, genes, seed, labs, ojs, oU))
         except Exception as e:  # pragma: no cover - reported, not hidden
             cpu = {"value": None, "unit": UNIT, "cores": 0, "kind": "port", "sample": f"failed: {e}"}
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -422,8 +489,15 @@ def run_ours(args, rank, world, local):
             "data": "synthetic (seeded, shapes of the precision-stress workload)",
             "config": {"workload": WORKLOAD, "units_per_step": B, "genes": g, "samples": n,
                        "max_parents": mp, "rng": "counter (Philox-4x32-10, on device)",
+                       "near_threshold": {
+                           "p_band": near["p_band"], "chi2_band": near["chi2_band"],
+                           "tests": near["tests"],
+                           "definition": "share of (pair, class) tests of the unpermuted labelling "
+                                         "and the sampled permutations whose Bonferroni-adjusted p is "
+                                         "within +-20% of 0.05 (p_band), or whose chi-square is within "
+                                         "+-20% of the critical chi-square (chi2_band)"},
                        "l2": "per-step working set (decision masks + per-unit scratch) "
-                             f"~{(B * (19900 * 4 + 420e3)) / 1e9:.2f} GB > L2"},
+                             f"~{(B * (c * 4 + 600e3)) / 1e9:.2f} GB > L2"},
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h},
             "gpu_launches": acc["launches"],
@@ -443,11 +517,13 @@ def run_ours(args, rank, world, local):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--units", type=int, default=10000, help="permutations per step")
-    ap.add_argument("--cpu-units", type=int, default=16, help="permutations in the CPU sample")
+    ap.add_argument("--cpu-units", type=int, default=8, help="permutations in the CPU sample")
+    ap.add_argument("--ref-units", type=int, default=2,
+                    help="permutations per step of the reference arm")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--workload", type=int, default=4, choices=[3, 4, 5],

@@ -96,9 +96,6 @@ struct SetHost {
   std::vector<int32_t> ids, nodes, epn, edges;
   std::vector<double> lval;
   std::vector<int32_t> el_nodes, el_epn, el_edges;
-  // changed-node records per network that the set's units needed so far
-  // (0: none beyond the default): later batches of the set start there
-  int kmax_hint = 0;
 };
 
 }  // namespace
@@ -139,6 +136,10 @@ struct eddy_ctx {
     bool exact_all;
   };
   std::map<int, ThrSet> thr_cache;
+  // changed-node records per network that units of sets of g genes needed
+  // beyond the default (kept across sets and eddy_clear_sets): later
+  // batches start there
+  std::map<int, int> kmax_hint;
   int lg_shift = 0;
   bool lg_ready = false;
   int lg_n = -1;  // sample count the fixed-point lgamma table was built for
@@ -314,6 +315,11 @@ bool use_popc() {
   const char *e = getenv("EDDY_PAIRS_KERNEL");
   return e && strcmp(e, "popc") == 0;
 }
+// Sets whose every table goes through the exact FP64 formula (the plain
+// FP64 form, or alphas outside (0, 1]) are decided by the popcount kernel
+// in one pass: the tensor-core epilogue and its general path would settle
+// nothing and list ten FP64 decisions per table.
+bool use_popc(const SetDev &sd) { return use_popc() || sd.exact_all; }
 
 
 // Contingency-kernel choices for a batch: tile shape v % mma_variants(), in
@@ -396,7 +402,7 @@ int dmask_ready(eddy_ctx *ctx, int B, int c) {
 int launch_pairs_any(eddy_ctx *ctx, const SetDev &sd, const uint64_t *masks, int B, uint32_t *dmask,
                      unsigned long long *stats, bool force_popc = false) {
   if (sd.c == 0) return EDDY_OK;
-  if (use_popc() || force_popc) {
+  if (use_popc(sd) || force_popc) {
     CK(launch_pairs(sd, masks, dmask, B, stats, ctx->stream));
     ctx->launches += 1;
     return EDDY_OK;
@@ -448,8 +454,8 @@ int launch_pairs_any(eddy_ctx *ctx, const SetDev &sd, const uint64_t *masks, int
   return EDDY_OK;
 }
 
-int check_mma_error(eddy_ctx *ctx) {
-  if (use_popc() || ctx->d_err.p == nullptr) return EDDY_OK;
+int check_mma_error(eddy_ctx *ctx, const SetDev &sd) {
+  if (use_popc(sd) || ctx->d_err.p == nullptr) return EDDY_OK;
   unsigned e = 0;
   CK(cudaMemcpyAsync(&e, ctx->d_err.p, sizeof e, cudaMemcpyDeviceToHost, ctx->stream));
   CK(cudaStreamSynchronize(ctx->stream));
@@ -467,10 +473,16 @@ int run_units(eddy_ctx *ctx, SetRun &sr, int nunits, const uint64_t *masks_host,
   // batch size: bounded by memory (masks, decisions and scratch);
   // kmax: changed-node records per network (EDDY_KMAX lowers it, to test the
   // re-run of the units that overflow it)
-  int kmax = 16;
+  // (records are written only for changed nodes, so room for more costs
+  // memory, not time: 64 covers every network of sets whose pair tests all
+  // sit near the threshold, measured at 200 genes)
+  int kmax = std::min(g + 1, 64);
   const char *ek = getenv("EDDY_KMAX");
   if (ek) kmax = std::max(1, std::min(16, atoi(ek)));
-  else if (sr.set_id >= 0) kmax = std::max(kmax, std::min(g + 1, ctx->sets[sr.set_id].kmax_hint));
+  else {
+    auto it = ctx->kmax_hint.find(g);
+    if (it != ctx->kmax_hint.end()) kmax = std::max(kmax, std::min(g + 1, it->second));
+  }
   size_t per_unit = unit_scratch_bytes(c, S, kmax) + sizeof(uint32_t) * (size_t)c + 8 * W + 64;
   // (up to 16 GB and 16384 units per batch: the general-path queue holds
   // unit indices below 2^15)
@@ -526,7 +538,7 @@ int run_units(eddy_ctx *ctx, SetRun &sr, int nunits, const uint64_t *masks_host,
       // set's operand built): a batch that repeats the previous one's set /
       // shape / buffers is captured as one CUDA graph and later replayed (a
       // set that runs a single batch launches directly: no capture cost)
-      const bool graphable = !masks_host && !keeping && !popc_batch && !use_popc() && c > 0 &&
+      const bool graphable = !masks_host && !keeping && !popc_batch && !use_popc(sd) && c > 0 &&
                              ctx->y_ready && ctx->stream != nullptr &&
                              pick_variant(ctx, sd, Bt) >= 0;
       if (masks_host) {
@@ -662,7 +674,7 @@ int run_units(eddy_ctx *ctx, SetRun &sr, int nunits, const uint64_t *masks_host,
       CK(cudaMemcpyAsync(hjs, ctx->d_js.p, 8 * Bt, cudaMemcpyDeviceToHost, ctx->stream));
       CK(cudaMemcpyAsync(hU, ctx->d_U.p, 4 * Bt, cudaMemcpyDeviceToHost, ctx->stream));
       CK(cudaMemcpyAsync(hst, ctx->d_status.p, 4 * Bt, cudaMemcpyDeviceToHost, ctx->stream));
-      const bool mma_used = !use_popc() && !popc_batch && ctx->d_err.p != nullptr && c > 0;
+      const bool mma_used = !use_popc(sd) && !popc_batch && ctx->d_err.p != nullptr && c > 0;
       if (mma_used)
         CK(cudaMemcpyAsync(herr, ctx->d_err.p, sizeof(unsigned), cudaMemcpyDeviceToHost, ctx->stream));
       CK(cudaStreamSynchronize(ctx->stream));
@@ -738,8 +750,8 @@ int run_units(eddy_ctx *ctx, SetRun &sr, int nunits, const uint64_t *masks_host,
         // not change); the set's later batches start with a quarter more
         const int want = std::max(need, kmax_run + 1);
         kmax_run = std::min(g + 1, (want + 7) / 8 * 8);
-        if (!ek && sr.set_id >= 0) {
-          int &hint = ctx->sets[sr.set_id].kmax_hint;
+        if (!ek) {
+          int &hint = ctx->kmax_hint[g];
           hint = std::max(hint, std::min(g + 1, (want + want / 4 + 7) / 8 * 8));
         }
       }
@@ -1163,7 +1175,7 @@ int eddy_debug_edges(eddy_ctx *ctx, int set_id, const uint8_t *labels, uint8_t *
   CK(cudaMemcpyAsync(ctx->d_masks.p, m.data(), 8 * W, cudaMemcpyHostToDevice, ctx->stream));
   rc = launch_pairs_any(ctx, sd, ctx->d_masks.as<uint64_t>(), 1, ctx->d_dmask.as<uint32_t>(), nullptr);
   if (rc) return rc;
-  rc = check_mma_error(ctx);
+  rc = check_mma_error(ctx, sd);
   if (rc) return rc;
   std::vector<uint32_t> dm(c);
   CK(cudaMemcpyAsync(dm.data(), ctx->d_dmask.p, 4 * (size_t)c, cudaMemcpyDeviceToHost, ctx->stream));

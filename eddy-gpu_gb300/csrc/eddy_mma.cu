@@ -800,7 +800,7 @@ __global__ void __launch_bounds__(256) k_general(const __grid_constant__ SetDev 
 }
 
 // The listed decisions of k_general through the exact FP64 path, one lane
-// each, one warp per block (one per SM at the launch size used).
+// each, one warp per block.
 __global__ void __launch_bounds__(32) k_exact(const __grid_constant__ SetDev sd,
                                               const unsigned *queue, unsigned qcap, int B,
                                               uint32_t *dmask, unsigned long long *stats) {
@@ -1193,7 +1193,11 @@ static cudaError_t launch_variant(const SetDev &sd, const uint8_t *Afp8, const u
   k_general<<<sms * 8, 256, 0, st>>>(sd, gqueue, qcap, B, dmask, stats, err);
   e = cudaGetLastError();
   if (e != cudaSuccess) return e;
-  k_exact<<<sms, 32, 0, st>>>(sd, gqueue, qcap, B, dmask, stats);
+  // one-warp blocks: the first sms of them land one per SM, which is all a
+  // short list needs; near-threshold batches (hundreds of thousands of
+  // rechecks) fill eight per SM, whose independent FP64 chains keep the
+  // SM's FP64 pipe busy while each waits on its own dependent operations
+  k_exact<<<sms * 8, 32, 0, st>>>(sd, gqueue, qcap, B, dmask, stats);
   return cudaGetLastError();
 }
 
