@@ -1,7 +1,8 @@
 """The eddy CLI as a drop-in for the reference's ./eddy on a GB300: config 1
 and config 2 inputs written in the reference's file formats, the reference's
-glibc permutation stream, printed lines and output files checked against the
-oracle driven by the same stream."""
+glibc permutation stream, printed lines and output files (_Networks,
+_BDEU_SCORES and _EdgeList) checked against the oracle driven by the same
+stream."""
 import os
 import re
 import subprocess
@@ -69,4 +70,14 @@ def test_cli_matches_oracle(cfg, R, eddy_lib, oracle_lib, tmp_path):
     vals = np.array([[float(x) for x in ln.split("\t")[1:3]] for ln in b if ln.startswith("Network ")
                      and ln[8].isdigit()])
     assert np.allclose(vals, u["lval"].T, atol=2e-6)
-    assert os.path.exists(os.path.join(str(tmp_path), name + "_EdgeList.txt"))
+    # _EdgeList.txt: the oracle's uncapped parent lists of iteration 0's two
+    # full-data networks (main.cu:1530-1641) through the reference-format
+    # writer, byte for byte
+    e = u["edges"]
+    S = e.shape[0]
+    pn, epn, pe = O.parents(e[[0, S - 1]], len(genes), 1 << 30)
+    exp_el = os.path.join(str(tmp_path), "expected_edgelist.txt")
+    eddy_lib.write_edge_list(exp_el, gn, dict(nodes=pn, edges=pe, epn=epn), prior, "CLASS_A",
+                             "CLASS_B")
+    got_el = open(os.path.join(str(tmp_path), name + "_EdgeList.txt")).read()
+    assert got_el == open(exp_el).read()
