@@ -124,16 +124,20 @@ void GlibcRand::reseed(uint32_t seed) {
 void glibc_permutation(GlibcRand &rng, int n, int n_class1, bool relabel, uint8_t *labels,
                        std::vector<uint8_t> &seen, std::vector<int> &order) {
   const uint32_t un = (uint32_t)n;
+  // rand() % n without a division: Lemire, Kaser and Kurz, "Faster
+  // remainder by direct computation" (2019), exact for 32-bit operands
+  const uint64_t M = UINT64_C(0xFFFFFFFFFFFFFFFF) / un + 1;
   for (int c = 0; c < n; c++) (void)rng.next();
   seen.assign(n, 0);
-  order.resize(n);
+  order.resize((size_t)n + 1);
   int cnt = 0;
+  // the first n distinct values in draw order, branch-free: every draw is
+  // written at the end of the list, which grows only when it is new
   while (cnt < n) {
-    uint32_t r = rng.next() % un;
-    if (!seen[r]) {
-      seen[r] = 1;
-      order[cnt++] = (int)r;
-    }
+    const uint32_t r = (uint32_t)(((unsigned __int128)(M * rng.next()) * un) >> 64);
+    order[cnt] = (int)r;
+    cnt += !seen[r];
+    seen[r] = 1;
   }
   if (relabel) {
     for (int k = 0; k < n_class1; k++) labels[order[k]] = 0;

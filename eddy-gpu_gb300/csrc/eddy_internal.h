@@ -57,51 +57,86 @@ struct SetDev {
   uint64_t salt;          // network hash salt
 };
 
-// Per-batch pointers for the unit kernel.
-// Decision masks of a batch: [B][c] u32, followed by a bitmap per unit of
-// the 32-pair chunks that hold a nonzero mask ([B][chunk_words(c)] u32).
-// Between batches the whole buffer is zero: the decision kernels only set
-// bits (and a chunk's bit with every nonzero mask in it), and the unit
-// kernel clears each mask word and chunk bit it reads.
+// Decision masks of a batch, per set: [nb][c] u32 (class 1 in bits 0-9,
+// class 2 in bits 16-25), followed by a bitmap per unit of the 32-pair
+// chunks that hold a nonzero mask ([nb][chunk_words(c)] u32).  Between
+// batches the whole buffer is zero: the decision kernels only set bits
+// (and a chunk's bit with every nonzero mask in it), and the unit kernel
+// clears each mask word and chunk bit it reads.
 #ifdef __CUDACC__
 #define EDDY_HD __host__ __device__
 #else
 #define EDDY_HD
 #endif
 EDDY_HD constexpr int chunk_words(int c) { return ((c + 31) / 32 + 31) / 32; }
-EDDY_HD constexpr size_t dmask_bytes(int B, int c) {
-  const int cc = c > 0 ? c : 1;
-  return sizeof(uint32_t) * ((size_t)B * cc + (size_t)B * chunk_words(cc));
+// u32 words of one set's decision masks and chunk bitmaps for nb units
+EDDY_HD constexpr size_t dmask_words(int nb, int c) {
+  return (size_t)nb * (c > 0 ? c : 1) + (size_t)nb * chunk_words(c > 0 ? c : 1);
 }
+EDDY_HD constexpr size_t dmask_bytes(int B, int c) { return sizeof(uint32_t) * dmask_words(B, c); }
+
+// One gene set of a batch.  A batch holds the units (labellings) of one or
+// more sets of the same sample count: set k's units are [u0, u0 + nb) of
+// the batch, in order.  Its decision masks and per-unit scratch are its
+// slices of the batch's buffers; in the contingency GEMM its units are the
+// A-operand rows [128 mb0, 128 (mb0 + mblocks)) (the rest of the last
+// block is padding) and its pair groups the column groups [grp0, grp0 +
+// groups) of the batch's operand Y, full-sample tables and group table, and
+// its tiles are [tile0, tile0 + ntn * mblocks) of the launch.
+struct BatchSet {
+  SetDev sd;
+  int u0, nb;          // units
+  int mb0, mblocks;    // A-operand row blocks of 128 units
+  int tile0, ntn;      // contingency tiles (ntn column tiles per row block)
+  int grp0;            // first column group of the set in the batch's Y
+  int gc0;             // first gene of the set in the batch's gene counts
+  int marg_b0;         // first block of its class-count work (4-cell layout)
+  int pad_;
+  long long dm0;       // u32 words: its decision masks, then its chunk bitmap
+  long long sc0;       // bytes: its per-unit scratch, unit_bytes per unit
+  long long mg0;       // u32 words (4-cell layout): class counts [g][128
+                       // mblocks], then the class-1 sizes [128 mblocks]
+  long long unit_bytes;
+};
 #ifdef __CUDACC__
-__device__ __forceinline__ uint32_t *chunk_bits(uint32_t *dmask, int B, int c, int u) {
-  return dmask + (size_t)B * c + (size_t)u * chunk_words(c);
+__device__ __forceinline__ uint32_t *unit_dmask(uint32_t *dmask, const BatchSet &bs, int u) {
+  return dmask + bs.dm0 + (size_t)(u - bs.u0) * bs.sd.c;
 }
-__device__ __forceinline__ void mark_chunk(uint32_t *dmask, int B, int c, int u, int p) {
-  atomicOr(chunk_bits(dmask, B, c, u) + (p >> 10), 1u << ((p >> 5) & 31));
+__device__ __forceinline__ uint32_t *unit_chunks(uint32_t *dmask, const BatchSet &bs, int u) {
+  return dmask + bs.dm0 + (size_t)bs.nb * bs.sd.c + (size_t)(u - bs.u0) * chunk_words(bs.sd.c);
+}
+// marks the chunk of pair p in a unit's chunk bitmap
+__device__ __forceinline__ void mark_chunk(uint32_t *ucb, int p) {
+  atomicOr(ucb + (p >> 10), 1u << ((p >> 5) & 31));
 }
 #endif
 
+// Per-batch pointers for the unit kernel.
 struct BatchDev {
   int B;                       // units in the batch
+  int nsets;                   // sets in the batch
   int kmax;                    // changed-node records per network
+  const BatchSet *sets;        // [nsets]
+  const int32_t *uslot;        // [B] set of each unit (index into sets)
   const uint64_t *masks;       // [B][W] class-1 sample mask per unit
-  uint32_t *dmask;             // [B][c] decision masks (class 1 bits 0-9, class 2 bits 16-25)
-  uint8_t *scratch;            // per-unit scratch, unit_bytes each
-  size_t unit_bytes;
+  uint32_t *dmask;             // decision masks and chunk bitmaps (per set: dm0)
+  uint8_t *scratch;            // per-unit scratch (per set: sc0)
   double *js;                  // [B]
   int32_t *U;                  // [B]
   uint32_t *status;            // [B]
   int32_t *keep_slot;          // [B] -1 or slot of detailed output
-  // detailed outputs for kept units (one slot per kept unit):
+  // detailed outputs for kept units (one slot per kept unit; node arrays
+  // strided by keep_g nodes and rows by keep_gw words):
+  int keep_g, keep_gw;
   int32_t *out_ids;            // [slots][S]   unique network -> network id
-  int32_t *out_cnt;            // [slots][S][g] capped parent counts
-  int32_t *out_par;            // [slots][S][g][mpk] parent lists
+  int32_t *out_cnt;            // [slots][S][keep_g] capped parent counts
+  int32_t *out_par;            // [slots][S][keep_g][mpk] parent lists
   int mpk;                     // list capacity per node in out_par
   double *out_dist;            // [slots][2][S] node-summed BDeu (double)
   double *out_lval;            // [slots][2][S] normalised likelihoods
-  uint32_t *out_rows;          // [slots][2][g][GW] full-network edge rows
-  unsigned long long *stats;   // [4] exact rechecks, tables, filtered, verifications
+  uint32_t *out_rows;          // [slots][2][keep_g][keep_gw] full-network edge rows
+  unsigned long long *stats;   // [nsets][4] per set: exact rechecks, tables decided,
+                               // tables settled by a filter, duplicate networks
 };
 
 }  // namespace eddy

@@ -198,10 +198,14 @@ __global__ void __launch_bounds__(kCmBlock) k_counter_masks(int n, int nA, int W
 }
 
 // ------------------------------------------------------------ k_pairs
-__global__ void __launch_bounds__(128) k_pairs(const __grid_constant__ SetDev sd, const uint64_t *masks, uint32_t *dmask,
+__global__ void __launch_bounds__(128) k_pairs(const BatchSet *__restrict__ sets,
+                                               const int32_t *__restrict__ uslot,
+                                               const uint64_t *masks, uint32_t *dmask,
                                                unsigned long long *stats) {
   extern __shared__ uint64_t smask[];
   const int u = blockIdx.y;
+  const BatchSet &bs = sets[uslot[u]];
+  const SetDev &sd = bs.sd;
   const int W = sd.W;
   for (int w = threadIdx.x; w < W; w += blockDim.x) smask[w] = masks[(size_t)u * W + w];
   __syncthreads();
@@ -228,8 +232,8 @@ __global__ void __launch_bounds__(128) k_pairs(const __grid_constant__ SetDev sd
     const int prior = sd.prior[p] ? 1 : 0;
     uint32_t mA = pair_mask(tA, prior, sd, nexact, nfilt);
     uint32_t mB = pair_mask(tB, prior, sd, nexact, nfilt);
-    dmask[(size_t)u * sd.c + p] = mA | (mB << 16);
-    if (mA | mB) mark_chunk(dmask, gridDim.y, sd.c, u, p);
+    unit_dmask(dmask, bs, u)[p] = mA | (mB << 16);
+    if (mA | mB) mark_chunk(unit_chunks(dmask, bs, u), p);
     ntab = 2;
   }
   if (stats) {
@@ -240,9 +244,10 @@ __global__ void __launch_bounds__(128) k_pairs(const __grid_constant__ SetDev sd
       ntab += __shfl_down_sync(0xffffffffu, ntab, o);
     }
     if ((threadIdx.x & 31) == 0) {
-      if (nexact) atomicAdd(&stats[0], (unsigned long long)nexact);
-      if (ntab) atomicAdd(&stats[1], (unsigned long long)ntab);
-      if (nfilt) atomicAdd(&stats[2], (unsigned long long)nfilt);
+      unsigned long long *sk = stats + 4 * (size_t)uslot[u];  // the set's row
+      if (nexact) atomicAdd(&sk[0], (unsigned long long)nexact);
+      if (ntab) atomicAdd(&sk[1], (unsigned long long)ntab);
+      if (nfilt) atomicAdd(&sk[2], (unsigned long long)nfilt);
     }
   }
 }
@@ -360,6 +365,7 @@ __device__ __forceinline__ int block_scan(int v, int &total, int *sbuf) {
 
 struct UnitSmem {
   // fixed part; variable arrays follow in dynamic shared memory
+  SetDev sd;    // the unit's set (copied from the batch's set table)
   unsigned long long HF[2];
   long long base[2][2];  // [data class][full network of class]
   int nphi[2];
@@ -546,16 +552,28 @@ __device__ void bdeu_items(const SetDev &sd, const UnitPtrs &P, int *scan, int n
 
 
 
-__global__ void __launch_bounds__(256, 3) k_units(const __grid_constant__ SetDev sd,
-                                                 const __grid_constant__ BatchDev bd) {
+__global__ void __launch_bounds__(256, 3) k_units(const __grid_constant__ BatchDev bd) {
   extern __shared__ __align__(16) char smraw[];
   UnitSmem &SM = *reinterpret_cast<UnitSmem *>(smraw);
   const int nw = blockDim.x >> 5, lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int u = blockIdx.x;
+  // the unit's set: its descriptor into shared memory, its slices of the
+  // batch's masks and scratch
+  const BatchSet &bs = bd.sets[bd.uslot[u]];
+  const int ul = u - bs.u0, bs_nb = bs.nb;
+  const long long bs_dm0 = bs.dm0;
+  uint8_t *scr = bd.scratch + bs.sc0 + (size_t)ul * bs.unit_bytes;
+  {
+    const int *src = reinterpret_cast<const int *>(&bs.sd);
+    int *dst = reinterpret_cast<int *>(&SM.sd);
+    for (int i = threadIdx.x; i < (int)(sizeof(SetDev) / sizeof(int)); i += blockDim.x) dst[i] = src[i];
+  }
+  __syncthreads();
+  const SetDev &sd = SM.sd;
   const int g = sd.g, W = sd.W, GW = sd.GW, S = sd.S, c = sd.c;
   UnitPtrs P = carve(smraw, g, W, GW, nw);
-  const int u = blockIdx.x;
   const UnitLayout L = unit_layout(c, S, bd.kmax);
-  uint8_t *scr = bd.scratch + (size_t)u * bd.unit_bytes;
+  uint32_t *ucb = bd.dmask + bs_dm0 + (size_t)bs_nb * c + (size_t)ul * chunk_words(c);
   uint32_t *phi[2] = {(uint32_t *)(scr + L.phi[0]), (uint32_t *)(scr + L.phi[1])};
   uint16_t *pcol[2] = {(uint16_t *)(scr + L.pcol[0]), (uint16_t *)(scr + L.pcol[1])};
   unsigned long long *rec = (unsigned long long *)(scr + L.rec);
@@ -571,7 +589,7 @@ __global__ void __launch_bounds__(256, 3) k_units(const __grid_constant__ SetDev
   unsigned long long *hsk = (unsigned long long *)(scr + L.hsk);
   int *hsv = (int *)(scr + L.hsv);
   int *wl = (int *)(scr + L.wl);
-  uint32_t *dm = bd.dmask + (size_t)u * c;
+  uint32_t *dm = bd.dmask + bs_dm0 + (size_t)ul * c;
   const int tid = threadIdx.x, nt = blockDim.x;
 
   // ---- P0: masks, state counts, selection prefixes, init
@@ -662,7 +680,7 @@ __global__ void __launch_bounds__(256, 3) k_units(const __grid_constant__ SetDev
     const int pa = r0 * (r0 - 1) / 2, pb = r0 < r1 ? r1 * (r1 - 1) / 2 : pa;
     int wpos0 = pa, wpos1 = pa;
     const uint32_t below = (1u << lane) - 1u;
-    const uint32_t *cbits = chunk_bits(bd.dmask, bd.B, c, u);
+    const uint32_t *cbits = ucb;
     const int k0 = pa >> 5, k1 = (pb + 31) >> 5;  // chunks [k0, k1)
     auto chunk = [&](int k, uint32_t m) {
       const int p = 32 * k + lane;
@@ -721,8 +739,7 @@ __global__ void __launch_bounds__(256, 3) k_units(const __grid_constant__ SetDev
   __syncthreads();
   // every warp has read the unit's chunk bitmap: zero it for the next batch
   {
-    uint32_t *cb = chunk_bits(bd.dmask, bd.B, c, u);
-    for (int i = tid; i < chunk_words(c); i += nt) cb[i] = 0u;
+    for (int i = tid; i < chunk_words(c); i += nt) ucb[i] = 0u;
   }
 
   // rows holding flip entries, ascending, per class, and entry totals
@@ -1250,7 +1267,8 @@ __global__ void __launch_bounds__(256, 3) k_units(const __grid_constant__ SetDev
     __syncwarp();
   }
   __syncthreads();
-  if (bd.stats && tid == 0) atomicAdd(&bd.stats[3], (unsigned long long)(S - U));
+  if (bd.stats && tid == 0)
+    atomicAdd(&bd.stats[4 * (size_t)bd.uslot[u] + 3], (unsigned long long)(S - U));
 
   // ---- P5: BDeu.  Base node scores of the two full networks: nodes
   // without parents from the state counts, the others as flat tasks; a
@@ -1458,8 +1476,11 @@ __global__ void __launch_bounds__(256, 3) k_units(const __grid_constant__ SetDev
       bd.out_dist[((size_t)keep * 2 + 0) * S + uu] = (double)dist[uu] * fx;
       bd.out_dist[((size_t)keep * 2 + 1) * S + uu] = (double)dist[S + uu] * fx;
     }
-    for (int i = tid; i < 2 * g * GW; i += nt)
-      bd.out_rows[(size_t)keep * 2 * g * GW + i] = P.rows[i];
+    for (int i = tid; i < 2 * g * GW; i += nt) {
+      const int kt = i / GW, w = i - kt * GW;  // (class, node) row, word
+      bd.out_rows[((size_t)keep * 2 * bd.keep_g + (kt / g) * bd.keep_g + kt % g) * bd.keep_gw + w] =
+          P.rows[i];
+    }
     // full capped lists of every unique network: warp per network
     for (int uu = warp; uu < U; uu += nw) {
       const int s = urep[uu];
@@ -1473,10 +1494,10 @@ __global__ void __launch_bounds__(256, 3) k_units(const __grid_constant__ SetDev
         while (cnt < sd.mp) {
           int j = G.next();
           if (j < 0) break;
-          if (cnt < mpk) bd.out_par[(((size_t)keep * S + uu) * g + t) * mpk + cnt] = j;
+          if (cnt < mpk) bd.out_par[(((size_t)keep * S + uu) * bd.keep_g + t) * mpk + cnt] = j;
           cnt++;
         }
-        bd.out_cnt[((size_t)keep * S + uu) * g + t] = cnt;
+        bd.out_cnt[((size_t)keep * S + uu) * bd.keep_g + t] = cnt;
       }
       __syncwarp();
     }
@@ -1502,24 +1523,30 @@ __global__ void __launch_bounds__(256, 3) k_units(const __grid_constant__ SetDev
 // network's exponentials replace its scores in the unit's dist array (the
 // scores are not read after this kernel).
 constexpr int kJsWarps = 8;
-__global__ void __launch_bounds__(32 * kJsWarps) k_js(const __grid_constant__ SetDev sd,
-                                                      const __grid_constant__ BatchDev bd,
-                                                      int upw) {
+__global__ void __launch_bounds__(32 * kJsWarps) k_js(const __grid_constant__ BatchDev bd, int upw) {
   __shared__ int pre[kJsWarps][33];
   __shared__ double acc[kJsWarps][3][32];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int u0 = (blockIdx.x * kJsWarps + warp) * upw, u = u0 + lane;
-  const int Ur = (lane < upw && u < bd.B) ? bd.U[u] : 0;
+  const bool mine = lane < upw && u < bd.B;
+  const int Ur = mine ? bd.U[u] : 0;
   const int U = Ur > 0 ? Ur : 0;
-  const int S = sd.S;
-  const UnitLayout L = unit_layout(sd.c, S, bd.kmax);
-  auto dist_of = [&](int uid) {
-    return (long long *)(bd.scratch + (size_t)uid * bd.unit_bytes + L.dist);
+  const int S = bd.sets[0].sd.S;  // n + 2, the same for every set of a batch
+  // this lane's unit's scores (its set's slice of the scratch), shared with
+  // the warp through shuffles
+  unsigned long long dptr = 0ull;
+  if (mine) {
+    const BatchSet &bs = bd.sets[bd.uslot[u]];
+    const UnitLayout L = unit_layout(bs.sd.c, S, bd.kmax);
+    dptr = (unsigned long long)(bd.scratch + bs.sc0 + (size_t)(u - bs.u0) * bs.unit_bytes + L.dist);
+  }
+  auto dist_of = [&](int o) {
+    return (long long *)__shfl_sync(0xffffffffu, dptr, o);
   };
   long long l0 = LLONG_MAX, h0 = LLONG_MIN, l1 = LLONG_MAX, h1 = LLONG_MIN;
   double m0 = 0.0, m1 = 0.0, sA = 0.0, sB = 0.0;
   if (U > 0) {
-    const long long *d = dist_of(u);
+    const long long *d = (const long long *)dptr;
     for (int uu = 0; uu < U; uu++) {
       const long long a = d[uu], b = d[S + uu];
       l0 = a < l0 ? a : l0;
@@ -1581,9 +1608,9 @@ __global__ void __launch_bounds__(32 * kJsWarps) k_js(const __grid_constant__ Se
     const long long ol0 = __shfl_sync(0xffffffffu, l0, o), ol1 = __shfl_sync(0xffffffffu, l1, o);
     const double om0 = __shfl_sync(0xffffffffu, m0, o), om1 = __shfl_sync(0xffffffffu, m1, o);
     const double osA = __shfl_sync(0xffffffffu, sA, o), osB = __shfl_sync(0xffffffffu, sB, o);
+    long long *d = dist_of(o);
     double ea = 0.0, eb = 0.0;
     if (live) {
-      long long *d = dist_of(u0 + o);
       const int uu = i - pre[warp][o];
       ea = exp(((double)(d[uu] - ol0) - om0) * osA);
       eb = exp(((double)(d[S + uu] - ol1) - om1) * osB);
@@ -1600,9 +1627,9 @@ __global__ void __launch_bounds__(32 * kJsWarps) k_js(const __grid_constant__ Se
     const bool live = i < total;
     const int o = live ? owner(i) : 31;
     const int okeep = __shfl_sync(0xffffffffu, keep, o);
+    const long long *d = dist_of(o);
     double t = 0.0;
     if (live) {
-      const long long *d = dist_of(u0 + o);
       const int uu = i - pre[warp][o];
       const double Pu = __longlong_as_double(d[uu]) / acc[warp][0][o];
       const double Qu = __longlong_as_double(d[S + uu]) / acc[warp][1][o];
@@ -1652,20 +1679,21 @@ cudaError_t launch_counter_masks(int n, int nA, int W, uint64_t seed, const int3
   return cudaGetLastError();
 }
 
-cudaError_t launch_pairs(const SetDev &sd, const uint64_t *masks, uint32_t *dmask, int B,
-                         unsigned long long *stats, cudaStream_t st) {
-  if (sd.c == 0) return cudaSuccess;
-  dim3 grid((sd.c + 127) / 128, B);
-  k_pairs<<<grid, 128, sizeof(uint64_t) * sd.W, st>>>(sd, masks, dmask, stats);
+cudaError_t launch_pairs(const BatchSet *sets, const int32_t *uslot, const uint64_t *masks,
+                         uint32_t *dmask, int B, int W, int cmax, unsigned long long *stats,
+                         cudaStream_t st) {
+  if (cmax <= 0) return cudaSuccess;
+  dim3 grid((cmax + 127) / 128, B);
+  k_pairs<<<grid, 128, sizeof(uint64_t) * W, st>>>(sets, uslot, masks, dmask, stats);
   return cudaGetLastError();
 }
 
-cudaError_t launch_units(const SetDev &sd, const BatchDev &bd, cudaStream_t st) {
+cudaError_t launch_units(const BatchDev &bd, int gmax, int W, cudaStream_t st) {
   const int threads = 256;
-  size_t smem = unit_smem_bytes(sd.g, sd.W, sd.GW, threads / 32);
+  size_t smem = unit_smem_bytes(gmax, W, (gmax + 31) / 32, threads / 32);
   cudaError_t e = cudaFuncSetAttribute(k_units, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
-  k_units<<<bd.B, threads, smem, st>>>(sd, bd);
+  k_units<<<bd.B, threads, smem, st>>>(bd);
   e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   // units per warp: as many as keep about eight warps per SM busy (the SM
@@ -1679,7 +1707,7 @@ cudaError_t launch_units(const SetDev &sd, const BatchDev &bd, cudaStream_t st) 
   }();
   const int upw = std::max(1, std::min(32, bd.B / (sms * kJsWarps)));
   const int warps = (bd.B + upw - 1) / upw;
-  k_js<<<(warps + kJsWarps - 1) / kJsWarps, 32 * kJsWarps, 0, st>>>(sd, bd, upw);
+  k_js<<<(warps + kJsWarps - 1) / kJsWarps, 32 * kJsWarps, 0, st>>>(bd, upw);
   return cudaGetLastError();
 }
 

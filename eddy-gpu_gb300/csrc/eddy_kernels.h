@@ -14,8 +14,12 @@ cudaError_t launch_prep(const int8_t *vals, int g, int n, int W, int c, uint64_t
 cudaError_t launch_counter_masks(int n, int nA, int W, uint64_t seed, const int32_t *unit_set,
                                  const int32_t *unit_perm, const uint64_t *mask0, uint64_t *masks,
                                  int B, cudaStream_t st);
-cudaError_t launch_pairs(const SetDev &sd, const uint64_t *masks, uint32_t *dmask, int B,
-                         unsigned long long *stats, cudaStream_t st);
-cudaError_t launch_units(const SetDev &sd, const BatchDev &bd, cudaStream_t st);
+// Popcount contingency and decision kernel for a batch (sets: its device
+// set table, uslot: each unit's set; cmax: the largest pair count).
+cudaError_t launch_pairs(const BatchSet *sets, const int32_t *uslot, const uint64_t *masks,
+                         uint32_t *dmask, int B, int W, int cmax, unsigned long long *stats,
+                         cudaStream_t st);
+// Network, BDeu and JS kernels of a batch (gmax: the largest set).
+cudaError_t launch_units(const BatchDev &bd, int gmax, int W, cudaStream_t st);
 cudaError_t set_divisor_map(const int8_t *map82);
 }  // namespace eddy

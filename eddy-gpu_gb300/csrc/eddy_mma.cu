@@ -296,6 +296,22 @@ __device__ __forceinline__ void core_table(const uint32_t *r, int q, uint32_t wr
 
 }  // namespace
 
+// Tile t of a batch's launch: its set k (sets ordered by tile0), column
+// tile tn and 128-unit row block mb within the set.
+struct TileAt {
+  int k, tn, mb;
+};
+__device__ __forceinline__ TileAt tile_at(const BatchSet *sets, int nsets, int t) {
+  int lo = 0, hi = nsets - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (sets[mid].tile0 <= t) lo = mid;
+    else hi = mid - 1;
+  }
+  const int l = t - sets[lo].tile0, mbk = sets[lo].mblocks;
+  return {lo, l / mbk, l % mbk};
+}
+
 template <int kStages>
 struct MmaSmem {
   unsigned long long full[kStages], empty[kStages], accfull[2], accempty[2], ctfull[2], drain;
@@ -320,15 +336,13 @@ constexpr int max_regs() {
 template <int kStages, int kEpi, int kGroups, bool kCore>
 __global__ void __maxnreg__(max_regs<kEpi>())
     k_pairs_mma(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
-                const __grid_constant__ SetDev sd, const float *__restrict__ ctotf, int B, int nk,
-                int ntiles, int mblocks, unsigned long long *stats,
-                unsigned *err, unsigned *gqueue, unsigned qcap,
-                const uint32_t *__restrict__ margc, const float *__restrict__ nc1,
+                const BatchSet *__restrict__ sets, int nsets, const float *__restrict__ ctotf,
+                int nk, int ntot, unsigned long long *stats, unsigned *err, unsigned *gqueue,
+                unsigned qcap, const uint32_t *__restrict__ margc,
                 const float4 *__restrict__ gcnt, const uint32_t *__restrict__ gtab) {
   constexpr int kTN = 32 * kGroups;
   constexpr int kPPG = kCore ? kCorePairs : kPairsPerGroup;  // pairs per column group
   constexpr int kPairsPerTile = kGroups * kPPG;
-  const int Bp = mblocks * kTM;
   constexpr uint32_t kStageBytes = (kTM + kTN) * kKC;
   constexpr uint32_t kCtBytes = kGroups * kGroupCtBytes;
   constexpr uint32_t kTmemCols = 2 * kTN <= 256 ? 256u : 512u;
@@ -341,7 +355,6 @@ __global__ void __maxnreg__(max_regs<kEpi>())
   MmaSmem<kStages> &S = *reinterpret_cast<MmaSmem<kStages> *>(base + kStages * kStageBytes);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   volatile unsigned *verr = err;
-  const int ntot = ntiles * mblocks;
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < kStages; s++) {
@@ -363,11 +376,13 @@ __global__ void __maxnreg__(max_regs<kEpi>())
                  "n"(kTmemCols));
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
   }
-  // 4-cell layout: the genes' full-sample counts in shared memory, after
-  // the barrier block
+  // 4-cell layout: a batch of one set has its genes' full-sample counts in
+  // shared memory, after the barrier block (others read them from global
+  // memory, at the set's offset)
   float4 *sgcnt = reinterpret_cast<float4 *>(base + kStages * kStageBytes + kBarBytes);
   if constexpr (kCore)
-    for (int i = threadIdx.x; i < sd.g; i += blockDim.x) sgcnt[i] = gcnt[i];
+    if (nsets == 1)
+      for (int i = threadIdx.x; i < sets[0].sd.g; i += blockDim.x) sgcnt[i] = gcnt[i];
   tc_fence_before();
   __syncthreads();
   tc_fence_after();
@@ -380,7 +395,9 @@ __global__ void __maxnreg__(max_regs<kEpi>())
       long long nfill = 0;
       bool live = true;  // false after a wait gave up (the error word is set)
       for (int t = blockIdx.x; t < ntot && live; t += gridDim.x) {
-        const int tn = t / mblocks, mb = t % mblocks;
+        const TileAt ta = tile_at(sets, nsets, t);
+        const int arow = (sets[ta.k].mb0 + ta.mb) * kTM;
+        const int brow = (sets[ta.k].grp0 + ta.tn * kGroups) * 32;
         for (int kc = 0; kc < nk; kc++) {
           if (!mbar_wait(smem_u32(&S.empty[stage]), phase ^ 1u, verr)) {
             live = false;
@@ -389,8 +406,8 @@ __global__ void __maxnreg__(max_regs<kEpi>())
           const uint32_t fb = smem_u32(&S.full[stage]);
           mbar_expect_tx(fb, kStageBytes);
           const uint32_t sa = smem_u32(base + stage * kStageBytes);
-          tma_load_2d(sa, &tmA, kc * kKC, mb * kTM, fb);
-          tma_load_2d(sa + kTM * kKC, &tmB, kc * kKC, tn * kTN, fb);
+          tma_load_2d(sa, &tmA, kc * kKC, arow, fb);
+          tma_load_2d(sa + kTM * kKC, &tmB, kc * kKC, brow, fb);
           nfill++;
           if (++stage == kStages) {
             stage = 0;
@@ -412,11 +429,12 @@ __global__ void __maxnreg__(max_regs<kEpi>())
         tc_fence_after();
         {
           // the tile's full-sample tables into the slot's buffer
-          const int tn = t / mblocks;
+          const TileAt ta = tile_at(sets, nsets, t);
+          const int grp = sets[ta.k].grp0 + ta.tn * kGroups;
           const uint32_t cb = smem_u32(&S.ctfull[acc]);
           mbar_expect_tx(cb, kCtBytes);
           bulk_load(smem_u32(base + kStages * kStageBytes + kCtOff + acc * kCtBytes),
-                    ctotf + (size_t)tn * kGroups * (kGroupCtBytes / 4), kCtBytes, cb);
+                    ctotf + (size_t)grp * (kGroupCtBytes / 4), kCtBytes, cb);
           nct++;
         }
         const uint32_t dcol = tmem + (uint32_t)(acc * kTN);
@@ -459,29 +477,50 @@ __global__ void __maxnreg__(max_regs<kEpi>())
     int acc = 0;
     uint32_t accphase = 0;
     unsigned nexact = 0, nfilt = 0, ntab = 0;
-    // no-edge thresholds of dof 4 without / with a prior (quick_zero_f2)
-    const float thr0 = sd.exact_all ? -1.f : sd.thr[0][2].chiA;
-    const float thr1 = sd.exact_all ? -1.f : sd.thr[1][2].chiA;
+    // the counters go to their set's row of stats ([nsets][4]): added when
+    // the warp moves to a tile of another set, and at the end
+    int stat_k = -1;
+    auto flush_stats = [&](int k) {
+      if (!stats || k < 0) return;
+      for (int o = 16; o > 0; o >>= 1) {
+        nexact += __shfl_down_sync(0xffffffffu, nexact, o);
+        nfilt += __shfl_down_sync(0xffffffffu, nfilt, o);
+        ntab += __shfl_down_sync(0xffffffffu, ntab, o);
+      }
+      if (lane == 0) {
+        unsigned long long *sk = stats + 4 * (size_t)k;
+        if (nexact) atomicAdd(&sk[0], (unsigned long long)nexact);
+        if (ntab) atomicAdd(&sk[1], (unsigned long long)ntab);
+        if (nfilt) atomicAdd(&sk[2], (unsigned long long)nfilt);
+      }
+      nexact = nfilt = ntab = 0;
+    };
     unsigned *qitems = gqueue + 4;
     // 4-cell layout: the class-1 count words of a group for this thread's
     // unit (w[q] = column gene of pair q, w[8] = the row gene) and the
     // unit's class-1 size, fetched one group ahead so that their L2 latency
-    // passes while the previous group is decided
+    // passes while the previous group is decided (the next group may be in
+    // the next tile, of another set: class counts [g][Bp] at the set's mg0,
+    // then its class-1 sizes)
     uint32_t wcur[kCorePairs + 1], wnext[kCorePairs + 1];
     float n1next = 0.f;
     auto fetch = [&](int t2, int gi2) {
       if constexpr (kCore) {
-        const int u2 = (t2 % mblocks) * kTM + row;
-        const uint32_t e = t2 < ntot ? gtab[(t2 / mblocks) * kGroups + wq + gi2 * kPerQuad]
-                                     : 0xFFFF0000u;
+        if (t2 >= ntot) return;
+        const TileAt ta = tile_at(sets, nsets, t2);
+        const BatchSet &b2 = sets[ta.k];
+        const int u2 = ta.mb * kTM + row, Bp2 = b2.mblocks * kTM;
+        const uint32_t *mc = margc + b2.mg0;
+        const uint32_t e = gtab[b2.grp0 + ta.tn * kGroups + wq + gi2 * kPerQuad];
         const int r2 = (int)(e >> 16), c2 = (int)(e & 0xFFFFu);
         if (r2 != 0xFFFF) {
-          wnext[kCorePairs] = margc[(size_t)r2 * Bp + u2];
+          wnext[kCorePairs] = mc[(size_t)r2 * Bp2 + u2];
 #pragma unroll
           for (int q = 0; q < kCorePairs; q++)
-            wnext[q] = margc[(size_t)(c2 + q < r2 ? c2 + q : r2 - 1) * Bp + u2];
+            wnext[q] = mc[(size_t)(c2 + q < r2 ? c2 + q : r2 - 1) * Bp2 + u2];
         }
-        if (gi2 == 0 && t2 < ntot) n1next = nc1[u2];
+        if (gi2 == 0)
+          n1next = reinterpret_cast<const float *>(mc + (size_t)b2.sd.g * Bp2)[u2];
       }
     };
     // with 16 epilogue warps the warps themselves hide the latency and the
@@ -489,18 +528,37 @@ __global__ void __maxnreg__(max_regs<kEpi>())
     constexpr bool kAhead = kEpi <= 12;
     if (kAhead) fetch(blockIdx.x, 0);
     for (int t = blockIdx.x; t < ntot; t += gridDim.x) {
-      const int tn = t / mblocks, mb = t % mblocks;
+      const TileAt ta = tile_at(sets, nsets, t);
+      const int tn = ta.tn, mb = ta.mb;
+      const BatchSet &bs = sets[ta.k];
+      if (ta.k != stat_k) {
+        flush_stats(stat_k);
+        stat_k = ta.k;
+      }
+      const SetDev &sd = bs.sd;
       if (!mbar_wait(smem_u32(&S.accfull[acc]), accphase, verr)) break;
       if (!mbar_wait(smem_u32(&S.ctfull[acc]), accphase, verr)) break;
       tc_fence_after();
       const float *ctile =
           reinterpret_cast<const float *>(base + kStages * kStageBytes + kCtOff + acc * kCtBytes);
-      const int u = mb * kTM + row;
-      // 4-cell layout: the unit's class sizes {class 1, class 2}
+      // the unit: TMEM lane row of the set's row block mb (past nb: padding)
+      const int ul = mb * kTM + row;
+      const bool ulive = ul < bs.nb;
+      const int u = bs.u0 + ul;
+      // no-edge thresholds of dof 4 without / with a prior (quick_zero_f2)
+      const float thr0 = sd.exact_all ? -1.f : sd.thr[0][2].chiA;
+      const float thr1 = sd.exact_all ? -1.f : sd.thr[1][2].chiA;
+      const int cset = sd.c;
+      const int grp_base = bs.grp0 + tn * kGroups;
+      // 4-cell layout: the unit's class sizes {class 1, class 2} and the
+      // set's genes' full-sample counts
       f32x2 N = f2_pack(0.f, 0.f);
       CoreN NC{};
+      const float4 *gc4 = nsets == 1 ? sgcnt : gcnt + bs.gc0;
       if constexpr (kCore) {
-        const float n1 = kAhead ? n1next : nc1[u];
+        const float n1 = kAhead ? n1next
+                                : reinterpret_cast<const float *>(
+                                      margc + bs.mg0 + (size_t)sd.g * bs.mblocks * kTM)[ul];
         N = f2_pack(n1, (float)sd.n - n1);
         core_n(N, NC);
       }
@@ -526,7 +584,7 @@ __global__ void __maxnreg__(max_regs<kEpi>())
         // 4-cell layout: the group's row gene and first column gene
         int crow = 0, ccol0 = 0;
         if constexpr (kCore) {
-          const uint32_t e = gtab[tn * kGroups + grp];
+          const uint32_t e = gtab[grp_base + grp];
           crow = (int)(e >> 16);
           ccol0 = (int)(e & 0xFFFFu);
           if (!kAhead) fetch(t, gi);
@@ -545,7 +603,7 @@ __global__ void __maxnreg__(max_regs<kEpi>())
           const uint32_t pbits = __float_as_uint(gct[32]);
           if (crow != 0xFFFF) {
             CoreGene Rg;
-            core_gene(Rg, wcur[kCorePairs], sgcnt[crow], N);
+            core_gene(Rg, wcur[kCorePairs], gc4[crow], N);
 #pragma unroll
             for (int h = 0; h < 2; h++) {
               uint32_t rh[16];
@@ -557,7 +615,7 @@ __global__ void __maxnreg__(max_regs<kEpi>())
                 const bool live = ccol0 + q < crow;
                 const int col = live ? ccol0 + q : crow - 1;
                 CoreGene Cg;
-                core_gene(Cg, wcur[q], sgcnt[col], N);
+                core_gene(Cg, wcur[q], gc4[col], N);
                 const float4 F = reinterpret_cast<const float4 *>(gct)[q];
                 f32x2 o[9];
                 core_cells(rh + 4 * qq, F, Rg, Cg, o);
@@ -581,10 +639,10 @@ __global__ void __maxnreg__(max_regs<kEpi>())
             }
             const float chiA = (f[9] != 0.f) ? thr1 : thr0;
             qmask |= (~quick_zero_f2(o2, chiA) & 3u) << (2 * q);
-            vmask |= (p0 + q < sd.c ? 3u : 0u) << (2 * q);
+            vmask |= (p0 + q < cset ? 3u : 0u) << (2 * q);
           }
         }
-        if (u >= B) vmask = 0u;
+        if (!ulive) vmask = 0u;
         qmask &= vmask;
         ntab += (unsigned)__popc(vmask);
         nfilt += (unsigned)__popc(vmask & ~qmask);
@@ -639,7 +697,7 @@ __global__ void __maxnreg__(max_regs<kEpi>())
                 it[2] = o[4] | (o[5] << 16);
                 it[3] = o[6] | (o[7] << 16);
                 it[4] = o[8] | ((uint32_t)cls << 16) | ((uint32_t)prior << 17);
-                it[5] = (uint32_t)p | ((uint32_t)u << 17);  // pair < 2^17, unit < 2^15
+                it[5] = (uint32_t)p | ((uint32_t)u << 17);  // pair < 2^17, batch unit < 2^15
               } else {
                 atomicOr(err, 2u);
               }
@@ -656,18 +714,7 @@ __global__ void __maxnreg__(max_regs<kEpi>())
         accphase ^= 1u;
       }
     }
-    if (stats) {
-      for (int o = 16; o > 0; o >>= 1) {
-        nexact += __shfl_down_sync(0xffffffffu, nexact, o);
-        nfilt += __shfl_down_sync(0xffffffffu, nfilt, o);
-        ntab += __shfl_down_sync(0xffffffffu, ntab, o);
-      }
-      if (lane == 0) {
-        if (nexact) atomicAdd(&stats[0], (unsigned long long)nexact);
-        if (ntab) atomicAdd(&stats[1], (unsigned long long)ntab);
-        if (nfilt) atomicAdd(&stats[2], (unsigned long long)nfilt);
-      }
-    }
+    flush_stats(stat_k);
   }
   tc_fence_before();
   __syncthreads();
@@ -717,26 +764,36 @@ __device__ __forceinline__ int general_task(const unsigned *it, int slot, const 
   return bit;
 }
 
-__device__ __forceinline__ void set_decision(uint32_t *dmask, int B, const SetDev &sd,
+__device__ __forceinline__ void set_decision(uint32_t *dmask, const BatchSet &bs,
                                              const unsigned *it, int slot) {
   const int cls = (it[4] >> 16) & 1;
   const int p = (int)(it[5] & 0x1FFFFu), u = (int)(it[5] >> 17);
-  atomicOr(&dmask[(size_t)u * sd.c + p], 1u << (slot + 16 * cls));
-  mark_chunk(dmask, B, sd.c, u, p);
+  atomicOr(&unit_dmask(dmask, bs, u)[p], 1u << (slot + 16 * cls));
+  mark_chunk(unit_chunks(dmask, bs, u), p);
 }
 
-__device__ __forceinline__ void add_stats(unsigned long long *stats, unsigned nexact,
-                                          unsigned nfilt) {
-  if (!stats) return;
-  for (int o = 16; o > 0; o >>= 1) {
-    nexact += __shfl_down_sync(0xffffffffu, nexact, o);
-    nfilt += __shfl_down_sync(0xffffffffu, nfilt, o);
+// A thread's counters of the general and exact paths, per set: added to
+// the set's row of stats ([nsets][4]) when the thread's next table belongs
+// to another set, and at the end.
+struct SetStats {
+  unsigned long long *stats;
+  int k = -1;
+  unsigned nexact = 0, nfilt = 0;
+  __device__ explicit SetStats(unsigned long long *s) : stats(s) {}
+  __device__ void flush() {
+    if (stats && k >= 0) {
+      if (nexact) atomicAdd(&stats[4 * (size_t)k], (unsigned long long)nexact);
+      if (nfilt) atomicAdd(&stats[4 * (size_t)k + 2], (unsigned long long)nfilt);
+    }
+    nexact = nfilt = 0;
   }
-  if ((threadIdx.x & 31) == 0) {
-    if (nexact) atomicAdd(&stats[0], (unsigned long long)nexact);
-    if (nfilt) atomicAdd(&stats[2], (unsigned long long)nfilt);
+  __device__ void to(int k2) {
+    if (k2 != k) {
+      flush();
+      k = k2;
+    }
   }
-}
+};
 
 // The general path for the queued tables of a launch, one thread per
 // table: the full table's FP32 decision and its Minkowski leave-one-out
@@ -747,16 +804,21 @@ __device__ __forceinline__ void add_stats(unsigned long long *stats, unsigned ne
 // dependent FP64 operation costs ~128 cycles and an SM issues one FP64 warp
 // instruction per ~32 cycles, so rechecks spread one per warp over the grid
 // would share the SMs' FP64 units, while k_exact runs them 32 to a warp.
-__global__ void __launch_bounds__(256) k_general(const __grid_constant__ SetDev sd,
-                                                 unsigned *queue, unsigned qcap, int B,
+__global__ void __launch_bounds__(256) k_general(const BatchSet *__restrict__ sets,
+                                                 const int32_t *__restrict__ uslot,
+                                                 unsigned *queue, unsigned qcap,
                                                  uint32_t *dmask, unsigned long long *stats,
                                                  unsigned *err) {
   const unsigned cnt = queue[0] < qcap ? queue[0] : qcap;
   const unsigned *items = queue + 4;
   unsigned *elist = queue + 4 + (size_t)qcap * kQWords;
-  unsigned nexact = 0, nfilt = 0;
+  SetStats ss(stats);
   for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < cnt; i += gridDim.x * blockDim.x) {
     const unsigned *it = items + (size_t)i * kQWords;
+    const int k = uslot[it[5] >> 17];
+    const BatchSet &bs = sets[k];
+    const SetDev &sd = bs.sd;
+    ss.to(k);
     const int prior = (it[4] >> 17) & 1;
     int t[9] = {(int)(it[0] & 0xFFFFu), (int)(it[0] >> 16), (int)(it[1] & 0xFFFFu),
                 (int)(it[1] >> 16),     (int)(it[2] & 0xFFFFu), (int)(it[2] >> 16),
@@ -764,7 +826,7 @@ __global__ void __launch_bounds__(256) k_general(const __grid_constant__ SetDev 
     TabInfo ti;
     table_info(t, ti);
     const bool safe = loo_safe(ti, prior, sd);
-    if (safe) nfilt++;
+    if (safe) ss.nfilt++;
     const int bit0 = fast_decision(ti, prior, sd);
     uint32_t bits = 0u;
     auto put = [&](int slot, int bit) {
@@ -792,30 +854,34 @@ __global__ void __launch_bounds__(256) k_general(const __grid_constant__ SetDev 
     if (bits) {
       const int cls = (it[4] >> 16) & 1;
       const int p = (int)(it[5] & 0x1FFFFu), u = (int)(it[5] >> 17);
-      atomicOr(&dmask[(size_t)u * sd.c + p], bits << (16 * cls));
-      mark_chunk(dmask, B, sd.c, u, p);
+      atomicOr(&unit_dmask(dmask, bs, u)[p], bits << (16 * cls));
+      mark_chunk(unit_chunks(dmask, bs, u), p);
     }
   }
-  add_stats(stats, nexact, nfilt);
+  ss.flush();
 }
 
 // The listed decisions of k_general through the exact FP64 path, one lane
 // each, one warp per block.
-__global__ void __launch_bounds__(32) k_exact(const __grid_constant__ SetDev sd,
-                                              const unsigned *queue, unsigned qcap, int B,
+__global__ void __launch_bounds__(32) k_exact(const BatchSet *__restrict__ sets,
+                                              const int32_t *__restrict__ uslot,
+                                              const unsigned *queue, unsigned qcap,
                                               uint32_t *dmask, unsigned long long *stats) {
   const unsigned n = queue[1] < qcap ? queue[1] : qcap;
   const unsigned *items = queue + 4;
   const unsigned *elist = queue + 4 + (size_t)qcap * kQWords;
-  unsigned nexact = 0, nfilt = 0;
+  SetStats ss(stats);
   for (unsigned k = blockIdx.x * 32u + threadIdx.x; k < n; k += gridDim.x * 32u) {
     const unsigned task = elist[k];
     const unsigned *it = items + (size_t)(task / 10) * kQWords;
     const int slot = (int)(task % 10);
     unsigned nf = 0;
-    if (general_task(it, slot, sd, true, nexact, nf)) set_decision(dmask, B, sd, it, slot);
+    const int ks = uslot[it[5] >> 17];
+    const BatchSet &bs = sets[ks];
+    ss.to(ks);
+    if (general_task(it, slot, bs.sd, true, ss.nexact, nf)) set_decision(dmask, bs, it, slot);
   }
-  add_stats(stats, nexact, nfilt);
+  ss.flush();
 }
 
 // -------------------------------------------------------------- operands
@@ -976,18 +1042,6 @@ __global__ void __launch_bounds__(128) k_setup(const __grid_constant__ SetupArgs
   }
 }
 
-// A: row u = class-1 mask of unit u over the samples, e4m3 0/1; rows >= B
-// zero.  Work item = one 16-sample chunk of one row.
-__device__ __forceinline__ void masks_fp8_chunk(const uint64_t *masks, int B, int W, int n_pad,
-                                                long long idx, uint8_t *A) {
-  const int chunks = n_pad / 16;
-  const int u = (int)(idx / chunks), ch = (int)(idx % chunks);
-  uint32_t bits = 0;
-  const int s0 = ch * 16, w = s0 >> 6, sh = s0 & 63;
-  if (u < B && w < W) bits = (uint32_t)(masks[(size_t)u * W + w] >> sh) & 0xFFFFu;
-  store_e4m3_16(A + (size_t)u * n_pad + ch * 16, bits);
-}
-
 // Class-1 counts of kMargGenes genes' states -1 and 0 for unit u (4-cell
 // layout): margc[i * Bp + u] = count(-1) | count(0) << 16 over the unit's
 // class-1 samples, and (for the first gene block) nc1[u] = its class-1
@@ -1018,22 +1072,50 @@ __device__ __forceinline__ void margins_unit(const uint64_t *masks, const uint64
   if (i0 == 0) nc1[u] = (float)tot;
 }
 
-// The per-batch operands in one launch of 128-thread blocks: blocks
-// [0, bA) the A operand, then (4-cell layout) Bp / 128 x ceil(g / 8) blocks
-// of class counts; block 0 also zeroes the general-path queue's header.
+// The per-batch operands in one launch of 128-thread blocks.  Blocks
+// [0, bA): the A operand, one 16-sample chunk of one row per thread; row r
+// of set k (128 mb0 <= r < 128 (mb0 + mblocks)) is the class-1 mask of its
+// unit r - 128 mb0, e4m3 0/1, and zero past the set's nb units.  Then, in
+// the 4-cell layout, each set's mblocks x ceil(g / 8) blocks of class
+// counts (from its marg_b0).  Block 0 also zeroes the general-path queue's
+// header.
 __global__ void __launch_bounds__(128)
-    k_operands(const uint64_t *masks, const uint64_t *planes, int B, int Bp, int g, int W,
-               int n_pad, int bA, uint8_t *A, uint32_t *margc, float *nc1, unsigned *gqueue) {
+    k_operands(const BatchSet *__restrict__ sets, int nsets, const uint64_t *masks, int W,
+               int n_pad, int rowsA, int bA, uint8_t *A, uint32_t *margc, unsigned *gqueue) {
   const int blk = blockIdx.x;
   if (blk == 0 && threadIdx.x < 4) gqueue[threadIdx.x] = 0u;  // the queue header
   if (blk < bA) {
+    const int chunks = n_pad / 16;
     const long long idx = (long long)blk * 128 + threadIdx.x;
-    if (idx < (long long)Bp * (n_pad / 16)) masks_fp8_chunk(masks, B, W, n_pad, idx, A);
+    if (idx >= (long long)rowsA * chunks) return;
+    const int r = (int)(idx / chunks), ch = (int)(idx % chunks);
+    int lo = 0, hi = nsets - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (sets[mid].mb0 * 128 <= r) lo = mid;
+      else hi = mid - 1;
+    }
+    const BatchSet &bs = sets[lo];
+    const int ul = r - bs.mb0 * 128;
+    const int s0 = ch * 16, w = s0 >> 6, sh = s0 & 63;
+    uint32_t bits = 0;
+    if (ul < bs.nb && w < W) bits = (uint32_t)(masks[(size_t)(bs.u0 + ul) * W + w] >> sh) & 0xFFFFu;
+    store_e4m3_16(A + (size_t)r * n_pad + ch * 16, bits);
     return;
   }
-  const int ub = Bp / 128, m = blk - bA;
-  const int u = (m % ub) * 128 + threadIdx.x, i0 = (m / ub) * kMargGenes;
-  margins_unit(masks, planes, B, Bp, g, W, u, i0, margc, nc1);
+  const int m = blk - bA;
+  int lo = 0, hi = nsets - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (sets[mid].marg_b0 <= m) lo = mid;
+    else hi = mid - 1;
+  }
+  const BatchSet &bs = sets[lo];
+  const int mm = m - bs.marg_b0, ub = bs.mblocks, Bp = ub * 128;
+  const int ul = (mm % ub) * 128 + threadIdx.x, i0 = (mm / ub) * kMargGenes;
+  uint32_t *mc = margc + bs.mg0;
+  margins_unit(masks + (size_t)bs.u0 * W, bs.sd.planes, bs.nb, Bp, bs.sd.g, W, ul, i0, mc,
+               reinterpret_cast<float *>(mc + (size_t)bs.sd.g * Bp));
 }
 
 // ------------------------------------------------------------ host side
@@ -1076,57 +1158,91 @@ int mma_ngroups_pad(const SetDev &sd, bool core) {
   return (g > 0 ? (g + kGroupPad - 1) / kGroupPad : 1) * kGroupPad;
 }
 int mma_npad(int n) { return (n + kKC - 1) / kKC * kKC; }
-// the operand Y, then the FP32 full-sample tables (a multiple of 128 bytes
-// in), then in the 4-cell layout the genes' full-sample state counts
-static size_t y_operand_bytes(const SetDev &sd) {
-  return (size_t)mma_ngroups_pad(sd, sd.core) * 32 * mma_npad(sd.n);
+// The Y arena: the operand Y (G x 32 rows of n_pad samples), the FP32
+// full-sample tables (a multiple of 128 bytes in, kGroupCtBytes per group),
+// the group table (4 bytes per group) and, 16-byte aligned, the genes'
+// full-sample state counts (16 bytes per gene).
+static size_t y_ct_offset(const YArena &y) { return (size_t)y.G * 32 * mma_npad(y.n); }
+static size_t y_gt_offset(const YArena &y) { return y_ct_offset(y) + (size_t)kGroupCtBytes * y.G; }
+static size_t y_gc_offset(const YArena &y) {
+  return (y_gt_offset(y) + sizeof(uint32_t) * (size_t)y.G + 15) & ~(size_t)15;
 }
-static size_t gene_counts_offset(const SetDev &sd) {
-  return y_operand_bytes(sd) + (size_t)kGroupCtBytes * mma_ngroups_pad(sd, sd.core);
+size_t mma_y_bytes(int G, int genes, int n) {
+  const YArena y{nullptr, G, genes, n};
+  return y_gc_offset(y) + sizeof(float4) * (size_t)genes;
 }
-// (4-cell layout) then the column-group table
-static size_t group_table_offset(const SetDev &sd) {
-  return gene_counts_offset(sd) + sizeof(float4) * (size_t)sd.g;
-}
-size_t mma_y_bytes(const SetDev &sd) {
-  if (!sd.core) return gene_counts_offset(sd);
-  return group_table_offset(sd) + sizeof(uint32_t) * (size_t)mma_ngroups_pad(sd, true);
-}
-int mma_bpad(int B) { return (B + kTM - 1) / kTM * kTM; }
-static size_t a_operand_bytes(int B, int n) { return (size_t)mma_bpad(B) * mma_npad(n); }
 // the A operand, then the general-path queue: a 16-byte counter and room
 // for every table of the batch (near-threshold workloads send half of them
 // or more to the general path), at least 65536 and at most 2^28 items
 // (7.5 GB with the deferred list; the list's entries, item * 10 + slot,
 // stay below 2^32)
-static unsigned queue_cap(int B, int c) {
-  const size_t all = (size_t)B * (c > 0 ? c : 1) * 2;
-  const size_t t = all < ((size_t)1 << 28) ? all : ((size_t)1 << 28);
+static size_t a_operand_bytes(int rowsA, int n) { return (size_t)rowsA * mma_npad(n); }
+static unsigned queue_cap(long long tables) {
+  const long long t = tables < (1ll << 28) ? tables : (1ll << 28);
   return (unsigned)(t < 65536 ? 65536 : t);
 }
 // EDDY_GENERAL_QUEUE_CAP lowers the queue's capacity (tests of the
 // overflow path: the batch is then decided by the popcount kernel)
-static unsigned queue_cap_used(int B, int c) {
-  const unsigned cap = queue_cap(B, c);
+static unsigned queue_cap_used(long long tables) {
+  const unsigned cap = queue_cap(tables);
   const char *e = getenv("EDDY_GENERAL_QUEUE_CAP");
   if (!e) return cap;
   const long v = atol(e);
   return (v >= 1 && (unsigned long)v < cap) ? (unsigned)v : cap;
 }
 // operand, queue header, items and the list of exact decisions, then (4-cell
-// layout, 256-byte aligned) the units' class counts [g][Bp] and class sizes
-static size_t margins_offset(int B, int n, int c) {
-  const size_t q = a_operand_bytes(B, n) + 16 + (size_t)queue_cap(B, c) * (kQWords + 1) * sizeof(uint32_t);
+// layout, 256-byte aligned) the sets' class counts and class sizes
+static size_t margins_offset(const MmaPlan &p, int n) {
+  const size_t q = a_operand_bytes(p.rowsA, n) + 16 +
+                   (size_t)queue_cap(p.tables) * (kQWords + 1) * sizeof(uint32_t);
   return (q + 255) & ~(size_t)255;
 }
-size_t mma_a_bytes(const SetDev &sd, int B) {
-  if (!sd.core)
-    return a_operand_bytes(B, sd.n) + 16 + (size_t)queue_cap(B, sd.c) * (kQWords + 1) * sizeof(uint32_t);
-  return margins_offset(B, sd.n, sd.c) + sizeof(uint32_t) * (size_t)mma_bpad(B) * (sd.g + 1);
+size_t mma_a_bytes(const MmaPlan &p, int n, bool core) {
+  if (!core)
+    return a_operand_bytes(p.rowsA, n) + 16 +
+           (size_t)queue_cap(p.tables) * (kQWords + 1) * sizeof(uint32_t);
+  return margins_offset(p, n) + sizeof(uint32_t) * (size_t)p.marg_words;
 }
 
-cudaError_t launch_build_y(const SetDev &sd, uint8_t *Y, cudaStream_t st) {
-  const int ng = mma_ngroups_pad(sd, sd.core), np = mma_npad(sd.n);
+// column groups per tile of each variant (see launch_shape)
+static int groups_of_variant(int v) {
+  static const int kg[5] = {4, 4, 6, 8, 8};
+  return kg[v % 5];
+}
+
+MmaPlan mma_plan(BatchSet *sets, int nsets, int variant, bool core) {
+  const int kg = groups_of_variant(variant);
+  MmaPlan p{};
+  int mb = 0, tile = 0, bm = 0;
+  long long mg = 0, tables = 0;
+  for (int k = 0; k < nsets; k++) {
+    BatchSet &b = sets[k];
+    b.mblocks = (b.nb + kTM - 1) / kTM;
+    b.mb0 = mb;
+    mb += b.mblocks;
+    const int ng = ngroups_of(b.sd, core);
+    b.ntn = ng > 0 ? (ng + kg - 1) / kg : 1;
+    b.tile0 = tile;
+    tile += b.ntn * b.mblocks;
+    b.marg_b0 = bm;
+    b.mg0 = mg;
+    if (core) {
+      bm += b.mblocks * ((b.sd.g + kMargGenes - 1) / kMargGenes);
+      mg += (long long)(b.sd.g + 1) * kTM * b.mblocks;
+    }
+    tables += 2ll * b.nb * (b.sd.c > 0 ? b.sd.c : 1);
+  }
+  p.rowsA = mb * kTM;
+  p.ntot = tile;
+  p.bM = bm;
+  p.marg_words = mg;
+  p.tables = tables;
+  return p;
+}
+
+cudaError_t launch_build_y(const SetDev &sd, bool core, const YArena &y, int grp0, int gc0,
+                           cudaStream_t st) {
+  const int ng = mma_ngroups_pad(sd, core), np = mma_npad(sd.n);
   const long long work = (long long)ng * 32 * (np / 16);
   SetupArgs a{};
   a.planes = sd.planes;
@@ -1137,16 +1253,16 @@ cudaError_t launch_build_y(const SetDev &sd, uint8_t *Y, cudaStream_t st) {
   a.c = sd.c;
   a.n_pad = np;
   a.ngroups = ng;
-  a.core = sd.core;
-  a.Y = Y;
-  a.ctf = (float *)(Y + y_operand_bytes(sd));
+  a.core = core ? 1 : 0;
+  a.Y = y.base + (size_t)grp0 * 32 * np;
+  a.ctf = reinterpret_cast<float *>(y.base + y_ct_offset(y)) + (size_t)grp0 * (kGroupCtBytes / 4);
   a.b[0] = (int)((work + 127) / 128);
-  a.b[1] = a.b[0] + (sd.core ? (ng + 127) / 128 : (ng * kPairsPerGroup + 127) / 128);
+  a.b[1] = a.b[0] + (core ? (ng + 127) / 128 : (ng * kPairsPerGroup + 127) / 128);
   a.b[2] = a.b[1];
   a.b[3] = a.b[1];
-  if (sd.core) {
-    a.gtab = (uint32_t *)(Y + group_table_offset(sd));
-    a.gcnt = (float4 *)(Y + gene_counts_offset(sd));
+  if (core) {
+    a.gtab = reinterpret_cast<uint32_t *>(y.base + y_gt_offset(y)) + grp0;
+    a.gcnt = reinterpret_cast<float4 *>(y.base + y_gc_offset(y)) + gc0;
     a.b[2] = a.b[1] + (ng + 127) / 128;
     a.b[3] = a.b[2] + (sd.g + 127) / 128;
   }
@@ -1156,48 +1272,44 @@ cudaError_t launch_build_y(const SetDev &sd, uint8_t *Y, cudaStream_t st) {
 int mma_build_launches(const SetDev &) { return 1; }
 
 template <int kStages, int kEpi, int kGroups, bool kCore>
-static cudaError_t launch_variant(const SetDev &sd, const uint8_t *Afp8, const uint8_t *Y,
-                                  unsigned *gqueue, unsigned qcap, int B, uint32_t *dmask,
-                                  unsigned long long *stats, unsigned *err, int sms,
-                                  cudaStream_t st) {
+static cudaError_t launch_variant(const BatchSet *sets, int nsets, const MmaPlan &plan,
+                                  const int32_t *uslot, int n, const uint8_t *Afp8,
+                                  const YArena &y, unsigned *gqueue, unsigned qcap,
+                                  uint32_t *dmask, unsigned long long *stats, unsigned *err,
+                                  int sms, cudaStream_t st, int g_single) {
   constexpr int kTN = 32 * kGroups;
-  const int np = mma_npad(sd.n), Bp = mma_bpad(B);
-  const int ng = ngroups_of(sd, kCore), nt = (ng + kGroups - 1) / kGroups;
+  const int np = mma_npad(n);
   CUtensorMap ma, mb;
-  if (!make_map(&ma, (void *)Afp8, np, Bp, kTM) ||
-      !make_map(&mb, (void *)Y, np, mma_ngroups_pad(sd, kCore) * 32, kTN))
+  if (!make_map(&ma, (void *)Afp8, np, plan.rowsA, kTM) ||
+      !make_map(&mb, (void *)y.base, np, y.G * 32, kTN))
     return cudaErrorNotSupported;
-  const int mblocks = Bp / kTM;
-  const float *ctotf = (const float *)(Y + y_operand_bytes(sd));
+  const float *ctotf = reinterpret_cast<const float *>(y.base + y_ct_offset(y));
   const uint32_t *margc = nullptr;
-  const float *nc1 = nullptr;
   const float4 *gcnt = nullptr;
   const uint32_t *gtab = nullptr;
   if (kCore) {
-    margc = (const uint32_t *)(Afp8 + margins_offset(B, sd.n, sd.c));
-    nc1 = (const float *)(margc + (size_t)Bp * sd.g);
-    gcnt = (const float4 *)(Y + gene_counts_offset(sd));
-    gtab = (const uint32_t *)(Y + group_table_offset(sd));
+    margc = reinterpret_cast<const uint32_t *>(Afp8 + margins_offset(plan, n));
+    gcnt = reinterpret_cast<const float4 *>(y.base + y_gc_offset(y));
+    gtab = reinterpret_cast<const uint32_t *>(y.base + y_gt_offset(y));
   }
   const size_t smem = 1024 + (size_t)kStages * (kTM + kTN) * kKC + kBarBytes +
-                      (kCore ? sizeof(float4) * (size_t)sd.g : 0);
+                      (kCore && nsets == 1 ? sizeof(float4) * (size_t)g_single : 0);
   auto kern = k_pairs_mma<kStages, kEpi, kGroups, kCore>;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
-  const int ntot = nt * mblocks;
-  const int grid = ntot < sms ? ntot : sms;
-  kern<<<grid, 32 * (2 + kEpi), smem, st>>>(ma, mb, sd, ctotf, B, np / kKC, nt, mblocks,
-                                            stats, err, gqueue, qcap, margc, nc1, gcnt, gtab);
+  const int grid = plan.ntot < sms ? plan.ntot : sms;
+  kern<<<grid, 32 * (2 + kEpi), smem, st>>>(ma, mb, sets, nsets, ctotf, np / kKC, plan.ntot,
+                                            stats, err, gqueue, qcap, margc, gcnt, gtab);
   e = cudaGetLastError();
   if (e != cudaSuccess) return e;
-  k_general<<<sms * 8, 256, 0, st>>>(sd, gqueue, qcap, B, dmask, stats, err);
+  k_general<<<sms * 8, 256, 0, st>>>(sets, uslot, gqueue, qcap, dmask, stats, err);
   e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   // one-warp blocks: the first sms of them land one per SM, which is all a
   // short list needs; near-threshold batches (hundreds of thousands of
   // rechecks) fill eight per SM, whose independent FP64 chains keep the
   // SM's FP64 pipe busy while each waits on its own dependent operations
-  k_exact<<<sms * 8, 32, 0, st>>>(sd, gqueue, qcap, B, dmask, stats);
+  k_exact<<<sms * 8, 32, 0, st>>>(sets, uslot, gqueue, qcap, dmask, stats);
   return cudaGetLastError();
 }
 
@@ -1205,45 +1317,47 @@ static cudaError_t launch_variant(const SetDev &sd, const uint8_t *Afp8, const u
 // 3: N=256, 8 warps; 4: N=256, 16 warps (ring depths fill the shared memory)
 int mma_variants() { return 5; }
 // operands (and class counts), GEMM + epilogue, general path, exact path
-int mma_launches(const SetDev &) { return 4; }
+int mma_launches() { return 4; }
 
 template <bool kCore>
-static cudaError_t launch_shape(const SetDev &sd, uint8_t *Afp8, const uint8_t *Y,
-                                unsigned *gqueue, unsigned qcap, int B, uint32_t *dmask,
-                                unsigned long long *stats, unsigned *err, int sms,
-                                cudaStream_t st, int variant) {
+static cudaError_t launch_shape(const BatchSet *sets, int nsets, const MmaPlan &plan,
+                                const int32_t *uslot, int n, const uint8_t *Afp8,
+                                const YArena &y, unsigned *gqueue, unsigned qcap,
+                                uint32_t *dmask, unsigned long long *stats, unsigned *err,
+                                int sms, cudaStream_t st, int variant, int g_single) {
+#define EDDY_VARIANT(S_, E_, G_)                                                              \
+  return launch_variant<S_, E_, G_, kCore>(sets, nsets, plan, uslot, n, Afp8, y, gqueue, qcap, \
+                                           dmask, stats, err, sms, st, g_single)
   switch (variant) {
-    case 1:
-      return launch_variant<6, 8, 4, kCore>(sd, Afp8, Y, gqueue, qcap, B, dmask, stats, err, sms, st);
-    case 2:
-      return launch_variant<5, 12, 6, kCore>(sd, Afp8, Y, gqueue, qcap, B, dmask, stats, err, sms, st);
-    case 3:
-      return launch_variant<4, 8, 8, kCore>(sd, Afp8, Y, gqueue, qcap, B, dmask, stats, err, sms, st);
-    case 4:
-      return launch_variant<4, 16, 8, kCore>(sd, Afp8, Y, gqueue, qcap, B, dmask, stats, err, sms, st);
-    default:
-      return launch_variant<6, 16, 4, kCore>(sd, Afp8, Y, gqueue, qcap, B, dmask, stats, err, sms, st);
+    case 1: EDDY_VARIANT(6, 8, 4);
+    case 2: EDDY_VARIANT(5, 12, 6);
+    case 3: EDDY_VARIANT(4, 8, 8);
+    case 4: EDDY_VARIANT(4, 16, 8);
+    default: EDDY_VARIANT(6, 16, 4);
   }
+#undef EDDY_VARIANT
 }
 
-cudaError_t launch_pairs_mma(const SetDev &sd, const uint64_t *masks, int B, uint8_t *Afp8,
-                             const uint8_t *Y, uint32_t *dmask, unsigned long long *stats,
-                             unsigned *err, int sms, cudaStream_t st, int variant) {
-  const int np = mma_npad(sd.n), Bp = mma_bpad(B);
-  const long long work = (long long)Bp * (np / 16);
+cudaError_t launch_pairs_mma(const BatchSet *sets, int nsets, const MmaPlan &plan,
+                             const uint64_t *masks, const int32_t *uslot, int n, int W,
+                             uint8_t *Afp8, const YArena &y, uint32_t *dmask,
+                             unsigned long long *stats, unsigned *err, int sms, cudaStream_t st,
+                             int variant, bool core, int g_single) {
+  const int np = mma_npad(n);
+  const long long work = (long long)plan.rowsA * (np / 16);
   const int bA = (int)((work + 127) / 128);
-  const int bM = sd.core ? (Bp / 128) * ((sd.g + kMargGenes - 1) / kMargGenes) : 0;
-  unsigned *gqueue = reinterpret_cast<unsigned *>(Afp8 + a_operand_bytes(B, sd.n));
-  uint32_t *margc = sd.core ? (uint32_t *)(Afp8 + margins_offset(B, sd.n, sd.c)) : nullptr;
-  k_operands<<<bA + bM, 128, 0, st>>>(masks, sd.planes, B, Bp, sd.g, sd.W, np, bA, Afp8, margc,
-                                       margc ? (float *)(margc + (size_t)Bp * sd.g) : nullptr,
-                                       gqueue);
+  unsigned *gqueue = reinterpret_cast<unsigned *>(Afp8 + a_operand_bytes(plan.rowsA, n));
+  uint32_t *margc = core ? reinterpret_cast<uint32_t *>(Afp8 + margins_offset(plan, n)) : nullptr;
+  k_operands<<<bA + (core ? plan.bM : 0), 128, 0, st>>>(sets, nsets, masks, W, np, plan.rowsA, bA,
+                                                        Afp8, margc, gqueue);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
-  const unsigned qcap = queue_cap_used(B, sd.c);
-  if (sd.core)
-    return launch_shape<true>(sd, Afp8, Y, gqueue, qcap, B, dmask, stats, err, sms, st, variant);
-  return launch_shape<false>(sd, Afp8, Y, gqueue, qcap, B, dmask, stats, err, sms, st, variant);
+  const unsigned qcap = queue_cap_used(plan.tables);
+  if (core)
+    return launch_shape<true>(sets, nsets, plan, uslot, n, Afp8, y, gqueue, qcap, dmask, stats,
+                              err, sms, st, variant % mma_variants(), g_single);
+  return launch_shape<false>(sets, nsets, plan, uslot, n, Afp8, y, gqueue, qcap, dmask, stats,
+                             err, sms, st, variant % mma_variants(), g_single);
 }
 
 }  // namespace eddy

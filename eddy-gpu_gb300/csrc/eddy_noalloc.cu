@@ -53,7 +53,9 @@ constexpr size_t kOffMask = kOffPrior + al256((size_t)kNAPairs);
 constexpr size_t kOffLg = kOffMask + al256(8ull * kNAW);
 constexpr size_t kOffDmask = kOffLg + al256(8ull * kDivisors * (kNAMaxSamples + 1));
 constexpr size_t kOffOut = kOffDmask + al256(dmask_bytes(1, kNAPairs));  // js, U, status
-constexpr size_t kOffUnit = kOffOut + 256;
+constexpr size_t kOffSets = kOffOut + 256;  // the one-set table and the unit's slot (0)
+constexpr size_t kOffSlot = kOffSets + al256(sizeof(BatchSet));
+constexpr size_t kOffUnit = kOffSlot + 256;
 
 }  // namespace
 
@@ -181,28 +183,41 @@ extern "C" int eddy_unit_noalloc(const eddy_opts *opts, const int8_t *vals, int 
   double *d_js = (double *)(base + kOffOut);
   int32_t *d_U = (int32_t *)(base + kOffOut + 8);
   uint32_t *d_status = (uint32_t *)(base + kOffOut + 12);
+  const BatchSet *d_sets = (const BatchSet *)(base + kOffSets);
+  const int32_t *d_slot = (const int32_t *)(base + kOffSlot);
+  if (cudaMemsetAsync(base + kOffSlot, 0, sizeof(int32_t), st) != cudaSuccess)
+    return bail(EDDY_ERR_CUDA);
   uint64_t salt = 0x5EED5EEDull;
   for (int attempt = 0; attempt < 4; attempt++) {
     sd.salt = salt;
+    // the batch's set table: this one set, its unit 0, its masks and
+    // scratch at the start of their regions (a host copy on the stack)
+    BatchSet bs{};
+    bs.sd = sd;
+    bs.nb = 1;
+    bs.unit_bytes = (long long)unit_scratch_bytes(c, S, kNAKmax);
     // decisions (the unit kernel zeroes the masks it reads, so every attempt
     // decides again), from masks and a chunk bitmap that start at zero
-    if (cudaMemsetAsync(base + kOffDmask, 0, dmask_bytes(1, c), st) != cudaSuccess ||
-        launch_pairs(sd, (const uint64_t *)(base + kOffMask), (uint32_t *)(base + kOffDmask), 1,
-                     nullptr, st) != cudaSuccess)
+    if (cudaMemcpyAsync(base + kOffSets, &bs, sizeof bs, cudaMemcpyHostToDevice, st) != cudaSuccess ||
+        cudaMemsetAsync(base + kOffDmask, 0, dmask_bytes(1, c), st) != cudaSuccess ||
+        launch_pairs(d_sets, d_slot, (const uint64_t *)(base + kOffMask),
+                     (uint32_t *)(base + kOffDmask), 1, W, c, nullptr, st) != cudaSuccess)
       return bail(EDDY_ERR_CUDA);
     BatchDev bd{};
     bd.B = 1;
+    bd.nsets = 1;
     bd.kmax = kNAKmax;
+    bd.sets = d_sets;
+    bd.uslot = d_slot;
     bd.masks = (const uint64_t *)(base + kOffMask);
     bd.dmask = (uint32_t *)(base + kOffDmask);
     bd.scratch = base + kOffUnit;
-    bd.unit_bytes = unit_scratch_bytes(c, S, kNAKmax);
     bd.js = d_js;
     bd.U = d_U;
     bd.status = d_status;
     bd.keep_slot = nullptr;
     bd.stats = nullptr;
-    if (launch_units(sd, bd, st) != cudaSuccess) return bail(EDDY_ERR_CUDA);
+    if (launch_units(bd, g, W, st) != cudaSuccess) return bail(EDDY_ERR_CUDA);
     unsigned char out[16];
     if (cudaMemcpyAsync(out, base + kOffOut, 16, cudaMemcpyDeviceToHost, st) != cudaSuccess)
       return bail(EDDY_ERR_CUDA);
