@@ -742,6 +742,46 @@ __global__ void __launch_bounds__(256, 3) k_units(const __grid_constant__ BatchD
     for (int i = tid; i < chunk_words(c); i += nt) ucb[i] = 0u;
   }
 
+  // ---- P1b: only flip entries that can change a capped list are kept.
+  // Node t's capped list is its first mp parents.  If R of the row's
+  // entries are edges of the full network (the flips that can remove an
+  // edge), every network of the class has at least mp edges in the columns
+  // up to the (mp + R)-th edge of the full row, so its capped list lies
+  // there: entries at later columns change no list and no network, and are
+  // dropped (networks that differ only in them are the same network).  A
+  // row's entries are contiguous and in column order.
+  for (int i = tid; i < 2 * g; i += nt) {
+    const int e0 = P.phs[i], e1 = P.phe[i];
+    if (e0 >= e1) continue;
+    const int k = i / g, t = i - k * g;
+    const uint32_t *row = P.rows + (size_t)i * GW;
+    int R = 0;
+    for (int e = e0; e < e1; e++) {
+      const int j = pcol[k][e];
+      R += (row[j >> 5] >> (j & 31)) & 1u;
+    }
+    int need = sd.mp + R, reach = t;  // t: every column of the row
+    for (int w = 0; w < GW; w++) {
+      uint32_t x = row[w];
+      const int pc = __popc(x);
+      if (pc >= need) {
+        for (int q = 1; q < need; q++) x &= x - 1;
+        reach = 32 * w + __ffs(x) - 1;
+        break;
+      }
+      need -= pc;
+    }
+    int e = e0;
+    while (e < e1 && pcol[k][e] <= reach) e++;
+    if (e == e0) {
+      P.phs[i] = 0x7fffffff;
+      P.phe[i] = 0;
+    } else {
+      P.phe[i] = e;
+    }
+  }
+  __syncthreads();
+
   // rows holding flip entries, ascending, per class, and entry totals
   if (tid == 0) SM.nent[0] = SM.nent[1] = 0;
   for (int k = 0; k < 2; k++) {
