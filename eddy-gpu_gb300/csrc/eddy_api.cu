@@ -464,7 +464,12 @@ int prepare_y(eddy_ctx *ctx, bool core) {
 // A decision buffer of `bytes` that holds only zeros: cleared in full
 // after an allocation or a batch that did not finish.
 int dmask_ready(eddy_ctx *ctx, size_t bytes) {
+  const void *p0 = ctx->d_dmask.p;
+  const size_t n0 = ctx->d_dmask.n;
   CK(ctx->d_dmask.ensure(bytes));
+  // a new allocation can start at the freed one's address: any change of
+  // the buffer means unknown contents
+  if (ctx->d_dmask.p != p0 || ctx->d_dmask.n != n0) ctx->dmask_clean = nullptr;
   if (ctx->dmask_clean != ctx->d_dmask.p) {
     CK(cudaMemsetAsync(ctx->d_dmask.p, 0, ctx->d_dmask.n, ctx->stream));
     ctx->dmask_clean = ctx->d_dmask.p;

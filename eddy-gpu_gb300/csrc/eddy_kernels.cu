@@ -286,9 +286,21 @@ constexpr unsigned kSmProbes = 64;
 
 struct UnitLayout {
   size_t phi[2], pcol[2], rec, htk, htv, dist, uid, urep, sig;
-  size_t skey, sbits, srep, hsk, hsv, wl, ksc, total;
+  size_t skey, sbits, srep, hsk, hsv, wl, ksc, memo, total;
   int HT, rec_words;  // rec_words: 64-bit words per network record
 };
+// Rows with at most kMemoE kept flip entries have their capped list under
+// every non-empty subset of those entries tabulated once per unit:
+// [2 g rows][kMemoSub subsets][2 words] (record entry or ~0 when the list
+// is the full network's, and the list's hash).
+constexpr int kMemoE = 4, kMemoSub = (1 << kMemoE) - 1;
+// genes of a set of c pairs (c = g (g - 1) / 2, so 1 + 8 c = (2 g - 1)^2)
+__host__ __device__ inline int genes_of_pairs(int c) {
+  int r = (int)sqrt((double)(1 + 8 * (long long)c));
+  while ((long long)r * r > 1 + 8 * (long long)c) r--;
+  while ((long long)(r + 1) * (r + 1) <= 1 + 8 * (long long)c) r++;
+  return (r + 1) / 2;
+}
 
 __host__ __device__ inline UnitLayout unit_layout(int c, int S, int kmax) {
   UnitLayout L;
@@ -332,6 +344,8 @@ __host__ __device__ inline UnitLayout unit_layout(int c, int S, int kmax) {
   o = al(o + sizeof(int32_t) * (size_t)S);
   L.ksc = o;  // scores of the distinct changed-node keys: [HT][2 classes]
   o = al(o + 2 * sizeof(int64_t) * (size_t)HT);
+  L.memo = o;  // per-row capped lists under each subset of the row's entries
+  o = al(o + 2 * sizeof(uint64_t) * kMemoSub * 2 * (size_t)genes_of_pairs(c));
   L.total = o;
   return L;
 }
@@ -405,7 +419,11 @@ struct UnitPtrs {
   int *tq;                   // [2 kItems + 1] task prefix per (item, class)
   int8_t *dmap;              // [96] divisor map (copy of the constant one)
   long long *fsc;            // [2 full][2 data][g] base node scores
+  uint32_t *ephi;            // [kEntCache] the kept flip entries, compacted
+  uint16_t *epcol;           // [kEntCache] their columns
 };
+// flip entries a unit keeps in shared memory (more stay in its scratch)
+constexpr int kEntCache = 1536;
 
 __host__ __device__ inline size_t unit_smem_bytes(int g, int W, int GW, int nwarps) {
   size_t o = sizeof(UnitSmem);
@@ -426,6 +444,8 @@ __host__ __device__ inline size_t unit_smem_bytes(int g, int W, int GW, int nwar
   o = al(o) + sizeof(int) * (2 * kItems + 1);
   o = al(o) + 96;
   o = al(o) + 4 * sizeof(long long) * g;
+  o = al(o) + sizeof(uint32_t) * kEntCache;
+  o = al(o) + sizeof(uint16_t) * kEntCache;
   return al(o);
 }
 
@@ -450,7 +470,9 @@ __device__ inline UnitPtrs carve(char *base, int g, int W, int GW, int nwarps) {
   o = al(o); P.acc = (long long *)(base + o); o += 2 * sizeof(long long) * kItems;
   o = al(o); P.tq = (int *)(base + o); o += sizeof(int) * (2 * kItems + 1);
   o = al(o); P.dmap = (int8_t *)(base + o); o += 96;
-  o = al(o); P.fsc = (long long *)(base + o);
+  o = al(o); P.fsc = (long long *)(base + o); o += 4 * sizeof(long long) * g;
+  o = al(o); P.ephi = (uint32_t *)(base + o); o += sizeof(uint32_t) * kEntCache;
+  o = al(o); P.epcol = (uint16_t *)(base + o);
   return P;
 }
 
@@ -781,6 +803,41 @@ __global__ void __launch_bounds__(256, 3) k_units(const __grid_constant__ BatchD
     }
   }
   __syncthreads();
+  // ---- P1c: the kept entries, when they fit, compacted into shared memory
+  // (rows in (class, node) order), where every later phase reads them
+  {
+    int kept = 0;
+    for (int i0 = 0; i0 < 2 * g; i0 += nt) {
+      const int i = i0 + tid;
+      const int cnt = (i < 2 * g && P.phs[i] < P.phe[i]) ? P.phe[i] - P.phs[i] : 0;
+      int total;
+      block_scan(cnt, total, SM.scan);
+      kept += total;
+    }
+    if (kept <= kEntCache) {
+      int running = 0;
+      for (int i0 = 0; i0 < 2 * g; i0 += nt) {
+        const int i = i0 + tid;
+        const int e0 = i < 2 * g ? P.phs[i] : 0, e1 = i < 2 * g ? P.phe[i] : 0;
+        const int cnt = e0 < e1 ? e1 - e0 : 0;
+        int total;
+        const int off = running + block_scan(cnt, total, SM.scan);
+        if (cnt) {
+          const int k = i / g;
+          for (int q = 0; q < cnt; q++) {
+            P.ephi[off + q] = phi[k][e0 + q];
+            P.epcol[off + q] = pcol[k][e0 + q];
+          }
+          P.phs[i] = off;
+          P.phe[i] = off + cnt;
+        }
+        running += total;
+      }
+      phi[0] = phi[1] = P.ephi;
+      pcol[0] = pcol[1] = P.epcol;
+      __syncthreads();
+    }
+  }
 
   // rows holding flip entries, ascending, per class, and entry totals
   if (tid == 0) SM.nent[0] = SM.nent[1] = 0;
@@ -1041,6 +1098,49 @@ __global__ void __launch_bounds__(256, 3) k_units(const __grid_constant__ BatchD
     R1[1] = 0;
   }
   __syncthreads();
+  // the capped list of each row with 1..kMemoE kept entries under every
+  // non-empty subset of them (the entries a left-out sample triggers):
+  // the record entry (t, first three parents) when it differs from the
+  // full network's list, and its hash; one thread per (row, subset)
+  unsigned long long *memo = (unsigned long long *)(scr + L.memo);
+  for (int task = tid; task < 2 * g * kMemoSub; task += nt) {
+    const int i = task / kMemoSub, msub = task - i * kMemoSub + 1;
+    const int e0 = P.phs[i], e1 = P.phe[i];
+    if (e0 >= e1 || e1 - e0 > kMemoE || msub >= (1 << (e1 - e0))) continue;
+    const int k = i / g, t = i - k * g;
+    const uint32_t *row = P.rows + (size_t)i * GW;
+    ListGen Go;
+    gen_for(Go, sd, P, phi[k], pcol[k], k, t, nullptr);
+    uint64_t h = node_hash_init(sd.salt, t);
+    int cnt = 0, ps[3] = {0xFFFF, 0xFFFF, 0xFFFF};
+    bool diff = false;
+    for (int w = 0; w < GW && cnt < sd.mp; w++) {
+      uint32_t x = row[w];
+      for (int q = 0; q < e1 - e0; q++) {
+        const int j = pcol[k][e0 + q];
+        if (((msub >> q) & 1) && (j >> 5) == w) x ^= 1u << (j & 31);
+      }
+      while (x && cnt < sd.mp) {
+        const int j = 32 * w + __ffs(x) - 1;
+        x &= x - 1;
+        if (Go.next() != j) diff = true;
+        if (cnt < 3) ps[cnt] = j;
+        h = node_hash_step(h, j);
+        cnt++;
+      }
+    }
+    // a shorter list than the full network's differs too
+    if (cnt < sd.mp && Go.next() >= 0) diff = true;
+    unsigned long long *M = memo + ((size_t)i * kMemoSub + (msub - 1)) * 2;
+    M[0] = diff ? ((unsigned long long)t | ((unsigned long long)(cnt < 3 ? cnt : 3) << 14) |
+                   ((unsigned long long)(ps[0] & 0xFFFF) << 16) |
+                   ((unsigned long long)(ps[1] & 0xFFFF) << 32) |
+                   ((unsigned long long)(ps[2] & 0xFFFF) << 48))
+                : ~0ull;
+    M[1] = h;
+  }
+  __syncthreads();
+
   // one record per distinct signature: changed nodes (capped list differs
   // from the full network's) with their lists, and the network hash
   int8_t *myst = P.stsig + (size_t)warp * g;
@@ -1057,16 +1157,33 @@ __global__ void __launch_bounds__(256, 3) k_units(const __grid_constant__ BatchD
     for (int t0 = 0; t0 < nrk; t0 += 32) {
       const int t = (t0 + lane < nrk) ? (int)P.rphi[k * g + t0 + lane] : -1;
       bool changed = false;
-      unsigned long long hn = 0;
+      unsigned long long hn = 0, ent = 0;
       int ps[3] = {0xFFFF, 0xFFFF, 0xFFFF};
       int cnt = 0;
       bool flips = false;
       if (t >= 0 && myst[t] <= 2) {
-        // does sample sigma trigger any flip entry of row t?
+        // the entries of row t that sample sigma triggers
         const int sr = myst[t] * 3;
-        for (int i = P.phs[k * g + t], e = P.phe[k * g + t]; i < e && !flips; i++) {
-          const int sc = myst[pcol[k][i]];
-          flips = sc <= 2 && (((phi[k][i] & 0x1FFu) >> (sr + sc)) & 1u);
+        const int e0 = P.phs[k * g + t], e1 = P.phe[k * g + t];
+        if (e1 - e0 <= kMemoE) {
+          int msub = 0;
+          for (int q = 0; q < e1 - e0; q++) {
+            const int sc = myst[pcol[k][e0 + q]];
+            if (sc <= 2 && (((phi[k][e0 + q] & 0x1FFu) >> (sr + sc)) & 1u)) msub |= 1 << q;
+          }
+          if (msub) {
+            const unsigned long long *M = memo + ((size_t)(k * g + t) * kMemoSub + (msub - 1)) * 2;
+            if (M[0] != ~0ull) {
+              changed = true;
+              ent = M[0];
+              hn = M[1];
+            }
+          }
+        } else {
+          for (int i = e0; i < e1 && !flips; i++) {
+            const int sc = myst[pcol[k][i]];
+            flips = sc <= 2 && (((phi[k][i] & 0x1FFu) >> (sr + sc)) & 1u);
+          }
         }
       }
       if (flips) {
@@ -1086,19 +1203,17 @@ __global__ void __launch_bounds__(256, 3) k_units(const __grid_constant__ BatchD
         if (diff) {
           changed = true;
           hn = h;
+          ent = (unsigned long long)t | ((unsigned long long)(cnt < 3 ? cnt : 3) << 14) |
+                ((unsigned long long)(ps[0] & 0xFFFF) << 16) |
+                ((unsigned long long)(ps[1] & 0xFFFF) << 32) |
+                ((unsigned long long)(ps[2] & 0xFFFF) << 48);
         }
       }
       unsigned bal = __ballot_sync(0xffffffffu, changed);
       if (changed) {
         int pos = nchg + __popc(bal & ((1u << lane) - 1u));
         dh += hn - P.fh[k * g + t];
-        if (pos < bd.kmax) {
-          unsigned long long e = (unsigned long long)t | ((unsigned long long)(cnt < 3 ? cnt : 3) << 14) |
-                                 ((unsigned long long)(ps[0] & 0xFFFF) << 16) |
-                                 ((unsigned long long)(ps[1] & 0xFFFF) << 32) |
-                                 ((unsigned long long)(ps[2] & 0xFFFF) << 48);
-          R[2 + pos] = e;
-        }
+        if (pos < bd.kmax) R[2 + pos] = ent;
       }
       nchg += __popc(bal);
     }
@@ -1431,21 +1546,30 @@ __global__ void __launch_bounds__(256, 3) k_units(const __grid_constant__ BatchD
   for (int i = tid; i < HT; i += nt) kslot[i] = ~0ull;
   if (tid == 0) SM.tfull = 0;
   __syncthreads();
-  for (int e = tid; e < nchg_all; e += nt) {
-    int uu, k;
-    unsigned long long rc;
-    item_of(e, uu, k, rc);
-    if (!differs(k, rc)) continue;
-    unsigned slot = (unsigned)(mix64(rc) & kmask);
-    bool placed = false;
-    for (int pr = 0; pr < HT; pr++, slot = (slot + 1u) & kmask) {
-      const unsigned long long prev = atomicCAS(&kslot[slot], ~0ull, rc);
-      if (prev == ~0ull || prev == rc) {
-        placed = true;
-        break;
+  // items network by network: a thread per unique network walks its
+  // changed-node records
+  for (int uu = tid; uu < U; uu += nt) {
+    const unsigned long long *R = rec_of(urep[uu]);
+    const int nrec = (int)R[1];
+    const int k = class_of(urep[uu]);
+    for (int e = 0; e < nrec; e++) {
+      const unsigned long long rc = R[2 + e];
+      if (!differs(k, rc)) continue;
+      unsigned slot = (unsigned)(mix64(rc) & kmask);
+      bool placed = false;
+      for (int pr = 0; pr < HT; pr++, slot = (slot + 1u) & kmask) {
+        // most items find their key already there: a read first (a slot
+        // only ever goes from empty to its final key), the atomic only on
+        // an empty slot
+        unsigned long long cur = __ldcg(&kslot[slot]);
+        if (cur == ~0ull) cur = atomicCAS(&kslot[slot], ~0ull, rc);
+        if (cur == ~0ull || cur == rc) {
+          placed = true;
+          break;
+        }
       }
+      if (!placed) SM.tfull = 1;
     }
-    if (!placed) SM.tfull = 1;
   }
   __syncthreads();
   if (!SM.tfull) {
@@ -1453,12 +1577,13 @@ __global__ void __launch_bounds__(256, 3) k_units(const __grid_constant__ BatchD
     int nk = 0;
     for (int i0 = 0; i0 < HT; i0 += nt) {
       const int i = i0 + tid;
-      const bool has = i < HT && kslot[i] != ~0ull;
+      const unsigned long long key = i < HT ? __ldcg(&kslot[i]) : ~0ull;
+      const bool has = key != ~0ull;
       int total;
       const int off = block_scan(has ? 1 : 0, total, SM.scan);
       if (has) {
         kidx[i] = nk + off;
-        klist[nk + off] = kslot[i];
+        klist[nk + off] = key;
       }
       nk += total;
     }
@@ -1470,16 +1595,36 @@ __global__ void __launch_bounds__(256, 3) k_units(const __grid_constant__ BatchD
           ksc[2 * i + 1] = s2;
         });
     __syncthreads();
-    for (int e = tid; e < nchg_all; e += nt) {
-      int uu, k;
-      unsigned long long rc;
-      item_of(e, uu, k, rc);
-      if (!differs(k, rc)) continue;
-      unsigned slot = (unsigned)(mix64(rc) & kmask);
-      while (kslot[slot] != rc) slot = (slot + 1u) & kmask;
-      const int i = kidx[slot];
-      add_delta(uu, k, rc, ksc[2 * i], ksc[2 * i + 1]);
+    // each network's deltas summed by its thread (exact integer sums)
+    for (int uu = tid; uu < U; uu += nt) {
+      const unsigned long long *R = rec_of(urep[uu]);
+      const int nrec = (int)R[1];
+      const int k = class_of(urep[uu]);
+      long long d1 = 0, d2 = 0;
+      for (int e = 0; e < nrec; e++) {
+        const unsigned long long rc = R[2 + e];
+        if (!differs(k, rc)) continue;
+        unsigned slot = (unsigned)(mix64(rc) & kmask);
+        int pr = 0;
+        while (__ldcg(&kslot[slot]) != rc && ++pr < HT) slot = (slot + 1u) & kmask;
+        if (pr >= HT) {  // not found: cannot happen; the unit is re-run
+          atomicOr(&SM.status, kUnitHashCollision);
+          continue;
+        }
+        const int i = kidx[slot];
+        const int t = (int)(rc & 0x3FFF), np = (int)((rc >> 14) & 3);
+        long long s1 = ksc[2 * i], s2 = ksc[2 * i + 1];
+        if (np == 0) {
+          s1 = bdeu_score0(sd, t, P.cnt3);
+          s2 = bdeu_score0(sd, t, P.cnt3 + 3 * g);
+        }
+        d1 += s1 - P.fsc[(k * 2 + 0) * g + t];
+        d2 += s2 - P.fsc[(k * 2 + 1) * g + t];
+      }
+      dist[uu] += d1;
+      dist[S + uu] += d2;
     }
+    __syncthreads();  // every network's score is complete before it is read
   } else {
     bdeu_items(
         sd, P, SM.scan, nchg_all,
