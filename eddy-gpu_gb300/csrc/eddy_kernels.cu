@@ -293,7 +293,7 @@ struct UnitLayout {
 // every non-empty subset of those entries tabulated once per unit:
 // [2 g rows][kMemoSub subsets][2 words] (record entry or ~0 when the list
 // is the full network's, and the list's hash).
-constexpr int kMemoE = 4, kMemoSub = (1 << kMemoE) - 1;
+constexpr int kMemoE = 6, kMemoSub = (1 << kMemoE) - 1;
 // genes of a set of c pairs (c = g (g - 1) / 2, so 1 + 8 c = (2 g - 1)^2)
 __host__ __device__ inline int genes_of_pairs(int c) {
   int r = (int)sqrt((double)(1 + 8 * (long long)c));
@@ -424,6 +424,12 @@ struct UnitPtrs {
 };
 // flip entries a unit keeps in shared memory (more stay in its scratch)
 constexpr int kEntCache = 1536;
+// slots of the shared table of distinct changed-node keys, which takes the
+// place of the flip-entry cache (ephi, then epcol) once the records are made
+constexpr int kKeyT = 1024;
+static_assert(kKeyT * sizeof(unsigned long long) <=
+                  kEntCache * (sizeof(uint32_t) + sizeof(uint16_t)),
+              "key table larger than the flip-entry cache");
 
 __host__ __device__ inline size_t unit_smem_bytes(int g, int W, int GW, int nwarps) {
   size_t o = sizeof(UnitSmem);
@@ -489,6 +495,8 @@ __device__ __forceinline__ void net_of(int s, const SetDev &sd, const int *sig, 
 
 __device__ __forceinline__ void load_stsig(const SetDev &sd, int sigma, int8_t *dst, int lane) {
   const int8_t *src = sd.valsT + (size_t)(sigma >= 0 ? sigma : 0) * sd.g;
+  // unrolled: the loads of a row's bytes are all in flight at once
+#pragma unroll 8
   for (int i = lane; i < sd.g; i += 32) dst[i] = (int8_t)(sigma >= 0 ? st_of(src[i]) : 3);
   __syncwarp();
 }
@@ -551,20 +559,38 @@ __device__ void bdeu_items(const SetDev &sd, const UnitPtrs &P, int *scan, int n
       running += total;
     }
     __syncthreads();
-    for (int task = tid; task < running; task += nt) {
-      int lo = 0, hi = 2 * m - 1;
-      while (lo < hi) {
-        const int mid = (lo + hi + 1) >> 1;
-        if (P.tq[mid] <= task) lo = mid;
-        else hi = mid - 1;
+    // tasks in (item, class) order: a warp's consecutive lanes mostly share
+    // one score, so their terms are summed in the warp (segmented) and each
+    // score takes one atomic per warp
+    const int lane = tid & 31;
+    for (int base = tid - lane; base < running; base += nt) {
+      const int task = base + lane;
+      int seg = -1;
+      long long term = 0;
+      if (task < running) {
+        int lo = 0, hi = 2 * m - 1;
+        while (lo < hi) {
+          const int mid = (lo + hi + 1) >> 1;
+          if (P.tq[mid] <= task) lo = mid;
+          else hi = mid - 1;
+        }
+        const int i = lo >> 1, cls = lo & 1, j = task - P.tq[lo];
+        const unsigned long long key = P.itk[i];
+        const int t = (int)(key & 0x3FFF), np = (int)((key >> 14) & 3);
+        term = bdeu_config_term(sd, t, np, (int)((key >> 16) & 0xFFFF),
+                                (int)((key >> 32) & 0xFFFF), (int)((key >> 48) & 0xFFFF),
+                                cls ? P.mB : P.mA, P.cnt3 + 3 * g * cls, j, P.dmap);
+        seg = lo;
       }
-      const int i = lo >> 1, cls = lo & 1, j = task - P.tq[lo];
-      const unsigned long long key = P.itk[i];
-      const int t = (int)(key & 0x3FFF), np = (int)((key >> 14) & 3);
-      const long long term = bdeu_config_term(
-          sd, t, np, (int)((key >> 16) & 0xFFFF), (int)((key >> 32) & 0xFFFF),
-          (int)((key >> 48) & 0xFFFF), cls ? P.mB : P.mA, P.cnt3 + 3 * g * cls, j, P.dmap);
-      atomicAdd((unsigned long long *)&P.acc[2 * i + cls], (unsigned long long)term);
+#pragma unroll
+      for (int d = 1; d < 32; d <<= 1) {
+        const long long y = __shfl_up_sync(0xffffffffu, term, d);
+        const int sy = __shfl_up_sync(0xffffffffu, seg, d);
+        if (lane >= d && sy == seg) term += y;
+      }
+      const int sn = __shfl_down_sync(0xffffffffu, seg, 1);
+      if (seg >= 0 && (lane == 31 || sn != seg))
+        atomicAdd((unsigned long long *)&P.acc[seg], (unsigned long long)term);
     }
     __syncthreads();
     for (int i = tid; i < m; i += nt) emit(b0 + i, P.acc[2 * i], P.acc[2 * i + 1]);
@@ -805,6 +831,7 @@ __global__ void __launch_bounds__(256, 3) k_units(const __grid_constant__ BatchD
   __syncthreads();
   // ---- P1c: the kept entries, when they fit, compacted into shared memory
   // (rows in (class, node) order), where every later phase reads them
+  bool compacted = false;
   {
     int kept = 0;
     for (int i0 = 0; i0 < 2 * g; i0 += nt) {
@@ -835,6 +862,7 @@ __global__ void __launch_bounds__(256, 3) k_units(const __grid_constant__ BatchD
       }
       phi[0] = phi[1] = P.ephi;
       pcol[0] = pcol[1] = P.epcol;
+      compacted = true;
       __syncthreads();
     }
   }
@@ -1532,57 +1560,85 @@ __global__ void __launch_bounds__(256, 3) k_units(const __grid_constant__ BatchD
   // The leave-one-out networks of a unit share most of their changed nodes'
   // lists (one flip near a threshold changes the same node in every network
   // whose left-out sample triggers it), so the items hold few distinct keys
-  // (node, first three parents): ~260 among ~19500 items per unit when
+  // (node, first three parents): ~240 among ~19500 items per unit when
   // nearly every pair sits near the threshold.  Each distinct key is scored
-  // once, in a table of HT slots (the network table's, free after the dedup
-  // phase; the signature table's key array holds the list of keys), and
-  // every item adds its key's score.  More distinct keys than the table
-  // holds: every item is scored on its own.
-  unsigned long long *kslot = htk;
-  int *kidx = htv;
+  // once, in a shared-memory table of KT slots, and every item adds its
+  // key's score.  A key that finds no slot within kKeyProbes probes: every
+  // item is scored on its own.
+  constexpr int kKeyProbes = 64;
+  const int KT = HT < kKeyT ? HT : kKeyT;  // slot-indexed scores fit ksc ([HT][2])
+  unsigned long long *kt = (unsigned long long *)P.ephi;
+  int *kpos = htv;  // key list index -> slot
   unsigned long long *klist = hsk;
   long long *ksc = (long long *)(scr + L.ksc);
-  const unsigned kmask = (unsigned)HT - 1u;
-  for (int i = tid; i < HT; i += nt) kslot[i] = ~0ull;
+  const unsigned kmask = (unsigned)KT - 1u;
+  if (compacted && bd.keep_slot && bd.keep_slot[u] >= 0) {
+    // the detailed outputs still read the flip entries: back to the
+    // unit's scratch, each class's (nent[k] <= c) to its own arrays, the
+    // class-2 row ranges shifted to start at 0
+    const int ne0 = SM.nent[0], ne = ne0 + SM.nent[1];
+    for (int k = 0; k < 2; k++) {
+      uint32_t *gphi = (uint32_t *)(scr + L.phi[k]);
+      uint16_t *gpcol = (uint16_t *)(scr + L.pcol[k]);
+      const int e0 = k ? ne0 : 0, e1 = k ? ne : ne0;
+      for (int i = e0 + tid; i < e1; i += nt) {
+        gphi[i - e0] = P.ephi[i];
+        gpcol[i - e0] = P.epcol[i];
+      }
+      phi[k] = gphi;
+      pcol[k] = gpcol;
+    }
+    for (int t = tid; t < g; t += nt)
+      if (P.phs[g + t] < P.phe[g + t]) {
+        P.phs[g + t] -= ne0;
+        P.phe[g + t] -= ne0;
+      }
+    __syncthreads();
+  }
+  for (int i = tid; i < KT; i += nt) kt[i] = ~0ull;
   if (tid == 0) SM.tfull = 0;
   __syncthreads();
-  // items network by network: a thread per unique network walks its
-  // changed-node records
-  for (int uu = tid; uu < U; uu += nt) {
+  // the items of unique network uu whose list differs from the full
+  // network's, in record order, read four records at a time
+  auto for_items = [&](int uu, auto &&fn) {
+    constexpr int kRecBatch = 4;
     const unsigned long long *R = rec_of(urep[uu]);
     const int nrec = (int)R[1];
     const int k = class_of(urep[uu]);
-    for (int e = 0; e < nrec; e++) {
-      const unsigned long long rc = R[2 + e];
-      if (!differs(k, rc)) continue;
-      unsigned slot = (unsigned)(mix64(rc) & kmask);
-      bool placed = false;
-      for (int pr = 0; pr < HT; pr++, slot = (slot + 1u) & kmask) {
-        // most items find their key already there: a read first (a slot
-        // only ever goes from empty to its final key), the atomic only on
-        // an empty slot
-        unsigned long long cur = __ldcg(&kslot[slot]);
-        if (cur == ~0ull) cur = atomicCAS(&kslot[slot], ~0ull, rc);
-        if (cur == ~0ull || cur == rc) {
-          placed = true;
-          break;
-        }
-      }
-      if (!placed) SM.tfull = 1;
+    for (int e0 = 0; e0 < nrec; e0 += kRecBatch) {
+      unsigned long long rb[kRecBatch];
+#pragma unroll
+      for (int q = 0; q < kRecBatch; q++) rb[q] = e0 + q < nrec ? R[2 + e0 + q] : ~0ull;
+#pragma unroll
+      for (int q = 0; q < kRecBatch; q++)
+        if (rb[q] != ~0ull && differs(k, rb[q])) fn(k, rb[q]);
     }
-  }
+  };
+  // a thread per unique network inserts its items' keys
+  for (int uu = tid; uu < U; uu += nt)
+    for_items(uu, [&](int, unsigned long long rc) {
+      unsigned slot = (unsigned)(mix64(rc) & kmask);
+      for (int pr = 0; pr < kKeyProbes; pr++, slot = (slot + 1u) & kmask) {
+        // a slot only ever goes from empty to its final key: a read first,
+        // the atomic only on an empty slot
+        unsigned long long cur = kt[slot];
+        if (cur == ~0ull) cur = atomicCAS(&kt[slot], ~0ull, rc);
+        if (cur == ~0ull || cur == rc) return;
+      }
+      SM.tfull = 1;
+    });
   __syncthreads();
   if (!SM.tfull) {
     // the keys in slot order: key list and slot -> list index
     int nk = 0;
-    for (int i0 = 0; i0 < HT; i0 += nt) {
+    for (int i0 = 0; i0 < KT; i0 += nt) {
       const int i = i0 + tid;
-      const unsigned long long key = i < HT ? __ldcg(&kslot[i]) : ~0ull;
+      const unsigned long long key = i < KT ? kt[i] : ~0ull;
       const bool has = key != ~0ull;
       int total;
       const int off = block_scan(has ? 1 : 0, total, SM.scan);
       if (has) {
-        kidx[i] = nk + off;
+        kpos[nk + off] = i;
         klist[nk + off] = key;
       }
       nk += total;
@@ -1591,36 +1647,30 @@ __global__ void __launch_bounds__(256, 3) k_units(const __grid_constant__ BatchD
     bdeu_items(
         sd, P, SM.scan, nk, [&](int i) -> unsigned long long { return klist[i]; },
         [&](int i, long long s1, long long s2) {
-          ksc[2 * i] = s1;
-          ksc[2 * i + 1] = s2;
+          ksc[2 * kpos[i]] = s1;
+          ksc[2 * kpos[i] + 1] = s2;
         });
     __syncthreads();
     // each network's deltas summed by its thread (exact integer sums)
     for (int uu = tid; uu < U; uu += nt) {
-      const unsigned long long *R = rec_of(urep[uu]);
-      const int nrec = (int)R[1];
-      const int k = class_of(urep[uu]);
       long long d1 = 0, d2 = 0;
-      for (int e = 0; e < nrec; e++) {
-        const unsigned long long rc = R[2 + e];
-        if (!differs(k, rc)) continue;
+      for_items(uu, [&](int k, unsigned long long rc) {
         unsigned slot = (unsigned)(mix64(rc) & kmask);
         int pr = 0;
-        while (__ldcg(&kslot[slot]) != rc && ++pr < HT) slot = (slot + 1u) & kmask;
-        if (pr >= HT) {  // not found: cannot happen; the unit is re-run
+        while (kt[slot] != rc && ++pr < kKeyProbes) slot = (slot + 1u) & kmask;
+        if (pr >= kKeyProbes) {  // not found: cannot happen; the unit is re-run
           atomicOr(&SM.status, kUnitHashCollision);
-          continue;
+          return;
         }
-        const int i = kidx[slot];
         const int t = (int)(rc & 0x3FFF), np = (int)((rc >> 14) & 3);
-        long long s1 = ksc[2 * i], s2 = ksc[2 * i + 1];
+        long long s1 = ksc[2 * slot], s2 = ksc[2 * slot + 1];
         if (np == 0) {
           s1 = bdeu_score0(sd, t, P.cnt3);
           s2 = bdeu_score0(sd, t, P.cnt3 + 3 * g);
         }
         d1 += s1 - P.fsc[(k * 2 + 0) * g + t];
         d2 += s2 - P.fsc[(k * 2 + 1) * g + t];
-      }
+      });
       dist[uu] += d1;
       dist[S + uu] += d2;
     }
