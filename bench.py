@@ -291,7 +291,8 @@ def run_multiset(args, rank, world, local):
                         f"{max(sizes)}, median {int(np.median(sizes))}) x {R} iterations "
                         f"(counter stream), {w.data.shape[0]} genes x {w.data.shape[1]} samples",
             "wall_units_per_s": units / wall, "units": units, "launches": t["launches"],
-            "stage_ms": {"pairs": t["ms_pairs"], "units": t["ms_units"]},
+            "stage_ms": {"k_operands+k_pairs_mma": t["ms_gemm"], "k_general+k_exact": t["ms_decide"],
+                         "k_units": t["ms_networks"], "k_js": t["ms_js"]},
             "sets_failed_at_iteration0": failed,
             "per_set_value": units / (ms_per_set / 1e3),
             "batching_speedup": ms_per_set / ms}
@@ -343,15 +344,15 @@ def run_ours(args, rank, world, local):
     if world > 1:
         dist.barrier()
     torch.cuda.synchronize()
-    acc = {"ms_pairs": 0.0, "ms_units": 0.0, "launches": 0}
+    acc = {"ms_pairs": 0.0, "ms_units": 0.0, "launches": 0, "ms_gemm": 0.0, "ms_decide": 0.0,
+           "ms_networks": 0.0, "ms_js": 0.0}
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     h0 = time.perf_counter()
     e0.record(stream)
     for i in range(args.steps):
         t = step(args.warmup + i)
-        acc["ms_pairs"] += t["ms_pairs"]
-        acc["ms_units"] += t["ms_units"]
-        acc["launches"] += t["launches"]
+        for k in acc:
+            acc[k] += t[k]
     e1.record(stream)
     torch.cuda.synchronize()
     clk.mark(h0, time.perf_counter())
@@ -449,7 +450,10 @@ def run_ours(args, rank, world, local):
     core = bool(np.isin(w.data[np.asarray(genes)], (-1, 0, 1)).all()) and \
         os.environ.get("EDDY_PAIR_LAYOUT") != "full"
     cells = 4 if core else 9
-    k1_ms = acc["ms_pairs"] / launches_per_kernel
+    # each kernel's own device time (CUDA events between the launches on
+    # the library's stream): operands + contraction; then the decisions the
+    # epilogue's bound leaves (k_general + k_exact) apart
+    k1_ms = acc["ms_gemm"] / launches_per_kernel
     # algorithmic work of the contraction: 2 (3g)^2 n_A per unit (the class-A
     # Gram matrix of the genes' state indicators); the GEMM the kernel runs
     # is smaller: 2 x cells x c x n per unit
@@ -470,7 +474,7 @@ def run_ours(args, rank, world, local):
     k1["frac"] = k1["achieved"] / e4m3
     # network assembly, dedup, BDeu, JS: algorithmic bytes (each stage's
     # inputs and outputs once through HBM)
-    k2_ms = acc["ms_units"] / launches_per_kernel
+    k2_ms = acc["ms_networks"] / launches_per_kernel
     k2 = {"kernel": "k_units", "bound": "hbm", "achieved": bu * Bl / (k2_ms / 1e3) / 1e9,
           "peak": hbm, "unit": "GB/s", "ms_per_launch": k2_ms,
           "algorithmic_bytes_per_launch": bu * Bl, "unique_networks_per_unit": U_mean,
@@ -522,7 +526,9 @@ def run_ours(args, rank, world, local):
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h},
             "gpu_launches": acc["launches"],
-            "stage_ms": {"k_pairs": acc["ms_pairs"], "k_units": acc["ms_units"]},
+            "stage_ms": {"k_operands+k_pairs_mma": acc["ms_gemm"],
+                         "k_general+k_exact": acc["ms_decide"], "k_units": acc["ms_networks"],
+                         "k_js": acc["ms_js"], "steps": args.steps},
             "roofline": roofline,
             "kernels": {"k_pairs_mma": k1, "k_units": k2},
             "clocks": clk.summary(),

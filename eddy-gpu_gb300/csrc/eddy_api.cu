@@ -114,7 +114,10 @@ struct eddy_ctx {
   std::vector<uint8_t> labels0;
   std::vector<SetHost> sets;
   cudaStream_t stream = nullptr;
-  cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+  // batch boundaries: 0 before the decisions, 4 after the contraction, 1
+  // after the decisions, 5 after the networks, 2 after the JS; 2 and 3 also
+  // time the autotuner's choices
+  cudaEvent_t ev[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
   GlibcRand rng{1};
   std::vector<uint8_t> seen;
   std::vector<int> order;
@@ -155,6 +158,9 @@ struct eddy_ctx {
   unsigned long long last_stats[4] = {0, 0, 0, 0};
   // timing of the last run
   double ms_total = 0, ms_pairs = 0, ms_units = 0;
+  // the same split by kernel: operands + contraction, general + exact
+  // decisions, networks, normalisation + JS
+  double ms_stage[4] = {0, 0, 0, 0};
   long long launches = 0;
   uint64_t salt = 0x5EED5EEDull;
   cudaStream_t own_stream = nullptr;
@@ -267,7 +273,7 @@ int prepare_sets(eddy_ctx *ctx, const std::vector<int> &ids) {
     const int g = (int)ctx->sets[ids[k]].genes.size(), c = g * (g - 1) / 2;
     o = al(o);
     ovt[k] = o;
-    o += (size_t)g * n + 16;
+    o += (size_t)st_stride(g) * n + 16;
     o = al(o);
     opl[k] = o;  // planes, then their word-major copy
     o += 2 * sizeof(uint64_t) * (size_t)g * 3 * W;
@@ -512,9 +518,19 @@ int upload_table(eddy_ctx *ctx, const BatchPlan &bp, size_t off) {
 // variant picked (tuning it on this batch when it is the first of its shape
 // with >= 512 units: every choice is timed once, same results, the fastest
 // kept).  The table is uploaded from the staging at byte offset toff.
+// ev_mid, when given, is recorded where the contraction ends and the
+// general-path decisions begin (right after the pair kernel on the popcount
+// path, which has no separate decision kernels).
 int launch_pairs_any(eddy_ctx *ctx, BatchPlan &bp, const uint64_t *masks, uint32_t *dmask,
-                     unsigned long long *stats, size_t toff, bool force_popc = false) {
-  if (bp.cmax == 0) return upload_table(ctx, bp, toff);
+                     unsigned long long *stats, size_t toff, bool force_popc = false,
+                     cudaEvent_t ev_mid = nullptr) {
+  auto mark = [&]() -> cudaError_t { return ev_mid ? cudaEventRecord(ev_mid, ctx->stream) : cudaSuccess; };
+  if (bp.cmax == 0) {
+    int rc = upload_table(ctx, bp, toff);
+    if (rc) return rc;
+    CK(mark());
+    return EDDY_OK;
+  }
   const int ns = (int)bp.sets.size();
   if (use_popc() || bp.fp64 || force_popc) {
     {
@@ -523,6 +539,7 @@ int launch_pairs_any(eddy_ctx *ctx, BatchPlan &bp, const uint64_t *masks, uint32
     }
     CK(launch_pairs(ctx->d_sets.as<BatchSet>(), ctx->d_uslot.as<int32_t>(), masks, dmask, bp.B,
                     ctx->W, bp.cmax, stats, ctx->stream));
+    CK(mark());
     ctx->launches += 1;
     return EDDY_OK;
   }
@@ -531,7 +548,7 @@ int launch_pairs_any(eddy_ctx *ctx, BatchPlan &bp, const uint64_t *masks, uint32
   Shape sh{bp.sets[0].sd.g, bp.sets[0].sd.c, shape_of(ctx, ctx->res_ids[0]).core};
   int variant = pick_variant(ctx, sh, bp.B);
   const int g_single = ns == 1 ? bp.sets[0].sd.g : 0;
-  auto run = [&](int v, unsigned long long *st) -> int {
+  auto run = [&](int v, unsigned long long *st, cudaEvent_t evm) -> int {
     {
       int rc = prepare_y(ctx, layout_core(v));
       if (rc) return rc;
@@ -545,7 +562,7 @@ int launch_pairs_any(eddy_ctx *ctx, BatchPlan &bp, const uint64_t *masks, uint32
     CK(launch_pairs_mma(ctx->d_sets.as<BatchSet>(), ns, mp, masks, ctx->d_uslot.as<int32_t>(),
                         ctx->samples, ctx->W, ctx->d_afp8.as<uint8_t>(), ctx->y, dmask, st,
                         ctx->d_err.as<unsigned>(), ctx->sms, ctx->stream, v, layout_core(v),
-                        g_single));
+                        g_single, evm));
     ctx->launches += mma_launches();
     return EDDY_OK;
   };
@@ -563,7 +580,7 @@ int launch_pairs_any(eddy_ctx *ctx, BatchPlan &bp, const uint64_t *masks, uint32
       if (ci > 0) CK(cudaStreamSynchronize(ctx->stream));
       CK(cudaEventRecord(ctx->ev[2], ctx->stream));
       {
-        int rc = run(v, nullptr);
+        int rc = run(v, nullptr, nullptr);
         if (rc) return rc;
       }
       CK(cudaEventRecord(ctx->ev[3], ctx->stream));
@@ -581,7 +598,7 @@ int launch_pairs_any(eddy_ctx *ctx, BatchPlan &bp, const uint64_t *masks, uint32
     CK(cudaStreamSynchronize(ctx->stream));
   }
   ctx->tuned_variant = variant;
-  return run(variant, stats);
+  return run(variant, stats, ev_mid);
 }
 
 int check_mma_error(eddy_ctx *ctx, const BatchPlan &bp) {
@@ -768,11 +785,12 @@ int run_batch(eddy_ctx *ctx, std::vector<Job> &jobs, const std::vector<UnitRef> 
     }
     CK(record(ctx->ev[0], capturing));
     {
-      int rc = launch_pairs_any(ctx, bp, bd.masks, bd.dmask, bd.stats, o_tab, popc_batch);
+      int rc = launch_pairs_any(ctx, bp, bd.masks, bd.dmask, bd.stats, o_tab, popc_batch,
+                                ctx->ev[4]);
       if (rc) return rc;
     }
     CK(record(ctx->ev[1], capturing));
-    CK(launch_units(bd, bp.gmax, W, ctx->stream));
+    CK(launch_units(bd, bp.gmax, W, ctx->stream, ctx->ev[5], capturing));
     CK(record(ctx->ev[2], capturing));
     ctx->launches += 2;  // networks, then normalisation and JS
     return EDDY_OK;
@@ -841,9 +859,10 @@ int run_batch(eddy_ctx *ctx, std::vector<Job> &jobs, const std::vector<UnitRef> 
           cap_ck(launch_pairs_mma(ctx->d_sets.as<BatchSet>(), ns, mp, bd.masks, bd.uslot, n, W,
                                   ctx->d_afp8.as<uint8_t>(), ctx->y, bd.dmask, bd.stats,
                                   ctx->d_err.as<unsigned>(), ctx->sms, ctx->stream, v,
-                                  layout_core(v), ns == 1 ? bp.sets[0].sd.g : 0));
+                                  layout_core(v), ns == 1 ? bp.sets[0].sd.g : 0, ctx->ev[4],
+                                  true));
           cap_ck(record(ctx->ev[1], true));
-          cap_ck(launch_units(bd, bp.gmax, W, ctx->stream));
+          cap_ck(launch_units(bd, bp.gmax, W, ctx->stream, ctx->ev[5], true));
           cap_ck(record(ctx->ev[2], true));
           ctx->launches += 1 + mma_launches() + 2;
         }
@@ -899,6 +918,14 @@ int run_batch(eddy_ctx *ctx, std::vector<Job> &jobs, const std::vector<UnitRef> 
   cudaEventElapsedTime(&bms, ctx->ev[1], ctx->ev[2]);
   *t_pairs += a;
   *t_units += bms;
+  {
+    const int cut[5] = {0, 4, 1, 5, 2};
+    for (int q = 0; q < 4; q++) {
+      float m = 0;
+      if (cudaEventElapsedTime(&m, ctx->ev[cut[q]], ctx->ev[cut[q + 1]]) == cudaSuccess)
+        ctx->ms_stage[q] += m;
+    }
+  }
   for (int k = 0; k < ns; k++) {
     for (int q = 0; q < 4; q++) ctx->last_stats[q] += hst4[4 * k + q];
     jobs[slot_job[k]].exact += hst4[4 * k];
@@ -1507,6 +1534,7 @@ int eddy_run(eddy_ctx *ctx) {
   if (!ctx) return EDDY_ERR_ARG;
   if (ctx->samples == 0) return fail(ctx, EDDY_ERR_STATE, "no matrix loaded");
   ctx->ms_total = ctx->ms_pairs = ctx->ms_units = 0;
+  for (double &m : ctx->ms_stage) m = 0;
   ctx->launches = 0;
   if (ctx->o.rng == EDDY_RNG_COUNTER && ctx->samples <= 4096) {
     // the counter stream's sets (labellings drawn on the device, independent
@@ -1597,6 +1625,7 @@ int eddy_run_labellings(eddy_ctx *ctx, int set_id, const uint8_t *labels, int R,
     if (a != ctx->nA) return fail(ctx, EDDY_ERR_ARG, "labelling %d has %d class-0 samples, expected %d", r, a, ctx->nA);
   }
   ctx->ms_total = ctx->ms_pairs = ctx->ms_units = 0;
+  for (double &m : ctx->ms_stage) m = 0;
   ctx->launches = 0;
   if (ctx->sets[set_id].genes.size() < 2) {
     for (int r = 0; r < R; r++) {
@@ -1713,6 +1742,7 @@ int eddy_run_permutations(eddy_ctx *ctx, int set_id, int first, int count, doubl
   SetHost &S = ctx->sets[set_id];
   const int n = ctx->samples, W = ctx->W;
   ctx->ms_total = ctx->ms_pairs = ctx->ms_units = 0;
+  for (double &m : ctx->ms_stage) m = 0;
   ctx->launches = 0;
   if (S.genes.size() < 2) {
     for (int i = 0; i < count; i++) {
@@ -1786,6 +1816,12 @@ int eddy_last_timing(const eddy_ctx *ctx, double *ms_kernels, double *ms_pairs, 
   if (ms_pairs) *ms_pairs = ctx->ms_pairs;
   if (ms_units) *ms_units = ctx->ms_units;
   if (launches) *launches = ctx->launches;
+  return EDDY_OK;
+}
+
+int eddy_last_stage_timing(const eddy_ctx *ctx, double *ms4) {
+  if (!ctx || !ms4) return EDDY_ERR_ARG;
+  for (int q = 0; q < 4; q++) ms4[q] = ctx->ms_stage[q];
   return EDDY_OK;
 }
 

@@ -48,7 +48,8 @@ struct SetDev {
   const uint64_t *planesT; // [W][g][3] the same planes word-major (follows planes)
   const uint64_t *valid;  // [W] all-sample mask
   const int8_t *vals;     // [g][n]  -1/0/1, 2 = any other value
-  const int8_t *valsT;    // [n][g]  the same, sample-major
+  const int8_t *valsT;    // [n][st_stride(g)] states 0-3 (st_of) of the same,
+                          // sample-major, rows padded with 3 to 16 bytes
   const uint16_t *ctot;   // [c][9]  permutation-invariant full-sample table
   const uint8_t *prior;   // [c]     prior bit of pair p
   const int64_t *lg;      // [kDivisors][n+1] fixed-point lgamma(m+4/d)-lgamma(4/d)
@@ -68,6 +69,9 @@ struct SetDev {
 #else
 #define EDDY_HD
 #endif
+// Row stride of the sample-major state matrix: genes rounded up to 16, so
+// that every row starts on a 16-byte boundary.
+EDDY_HD constexpr int st_stride(int g) { return (g + 15) & ~15; }
 EDDY_HD constexpr int chunk_words(int c) { return ((c + 31) / 32 + 31) / 32; }
 // u32 words of one set's decision masks and chunk bitmaps for nb units
 EDDY_HD constexpr size_t dmask_words(int nb, int c) {

@@ -56,11 +56,14 @@ __global__ void k_planes(const int8_t *vals, int g, int n, int W, uint64_t *plan
   if (i == 0) valid[w] = v;
 }
 
+// Sample-major states: valsT[s][i] = st_of(vals[i][s]), rows of
+// st_stride(g) bytes padded with state 3 (no value).
 __global__ void k_transpose(const int8_t *vals, int g, int n, int8_t *valsT) {
-  int idx = blockIdx.x * blockDim.x + threadIdx.x;
-  if (idx >= g * n) return;
-  int s = idx / g, i = idx % g;
-  valsT[idx] = vals[(size_t)i * n + s];
+  const int gp = st_stride(g);
+  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= gp * n) return;
+  const int s = idx / gp, i = idx % gp;
+  valsT[idx] = (int8_t)(i < g ? st_of(vals[(size_t)i * n + s]) : 3);
 }
 
 __global__ void k_ctot(const uint64_t *planes, int g, int W, int c, uint16_t *ctot) {
@@ -444,7 +447,7 @@ __host__ __device__ inline size_t unit_smem_bytes(int g, int W, int GW, int nwar
   o = al(o) + 4 * sizeof(int) * g;
   o = al(o) + sizeof(uint16_t) * g;
   o = al(o) + 2 * sizeof(uint16_t) * g;
-  o = al(o) + (size_t)nwarps * g;
+  o = al(o) + (size_t)nwarps * st_stride(g);
   o = al(o) + sizeof(unsigned long long) * kItems;
   o = al(o) + 2 * sizeof(long long) * kItems;
   o = al(o) + sizeof(int) * (2 * kItems + 1);
@@ -471,7 +474,7 @@ __device__ inline UnitPtrs carve(char *base, int g, int W, int GW, int nwarps) {
   o = al(o); P.phs = (int *)(base + o); P.phe = P.phs + 2 * g; o += 4 * sizeof(int) * g;
   o = al(o); P.dab = (uint16_t *)(base + o); o += sizeof(uint16_t) * g;
   o = al(o); P.rphi = (uint16_t *)(base + o); o += 2 * sizeof(uint16_t) * g;
-  o = al(o); P.stsig = (int8_t *)(base + o); o += (size_t)nwarps * g;
+  o = al(o); P.stsig = (int8_t *)(base + o); o += (size_t)nwarps * st_stride(g);
   o = al(o); P.itk = (unsigned long long *)(base + o); o += sizeof(unsigned long long) * kItems;
   o = al(o); P.acc = (long long *)(base + o); o += 2 * sizeof(long long) * kItems;
   o = al(o); P.tq = (int *)(base + o); o += sizeof(int) * (2 * kItems + 1);
@@ -493,11 +496,14 @@ __device__ __forceinline__ void net_of(int s, const SetDev &sd, const int *sig, 
   sigma = sig[s - 1];
 }
 
+// The states of every gene at sample sigma (3 for all when sigma < 0) into a
+// warp's row of st_stride(g) bytes (16-byte aligned), 16 bytes per lane.
 __device__ __forceinline__ void load_stsig(const SetDev &sd, int sigma, int8_t *dst, int lane) {
-  const int8_t *src = sd.valsT + (size_t)(sigma >= 0 ? sigma : 0) * sd.g;
-  // unrolled: the loads of a row's bytes are all in flight at once
-#pragma unroll 8
-  for (int i = lane; i < sd.g; i += 32) dst[i] = (int8_t)(sigma >= 0 ? st_of(src[i]) : 3);
+  const int nv = st_stride(sd.g) / 16;
+  const uint4 *src = reinterpret_cast<const uint4 *>(sd.valsT + (size_t)(sigma >= 0 ? sigma : 0) * st_stride(sd.g));
+  uint4 *d = reinterpret_cast<uint4 *>(dst);
+  for (int i = lane; i < nv; i += 32)
+    d[i] = sigma >= 0 ? __ldg(src + i) : make_uint4(0x03030303u, 0x03030303u, 0x03030303u, 0x03030303u);
   __syncwarp();
 }
 
@@ -1171,7 +1177,7 @@ __global__ void __launch_bounds__(256, 3) k_units(const __grid_constant__ BatchD
 
   // one record per distinct signature: changed nodes (capped list differs
   // from the full network's) with their lists, and the network hash
-  int8_t *myst = P.stsig + (size_t)warp * g;
+  int8_t *myst = P.stsig + (size_t)warp * st_stride(g);
   const int nwl = SM.nwl;
   for (int wi = warp; wi < nwl; wi += nw) {
     const int s = wl[wi];
@@ -1408,8 +1414,8 @@ __global__ void __launch_bounds__(256, 3) k_units(const __grid_constant__ BatchD
         ListGen a;
         gen_for(a, sd, P, phi[ks], pcol[ks], ks, t, ss >= 0 ? myst : nullptr);
         const int GWl = sd.GW;
-        const int8_t *rT = sd.valsT + (size_t)(sr >= 0 ? sr : 0) * sd.g;
-        const int strow_r = (sr >= 0) ? st_of(rT[t]) : 3;
+        const int8_t *rT = sd.valsT + (size_t)(sr >= 0 ? sr : 0) * st_stride(sd.g);
+        const int strow_r = (sr >= 0) ? rT[t] : 3;
         const uint32_t *rowr = P.rows + ((size_t)kr * g + t) * GWl;
         int fi = P.phs[kr * g + t], fe = P.phe[kr * g + t];
         int w = 0;
@@ -1420,7 +1426,7 @@ __global__ void __launch_bounds__(256, 3) k_units(const __grid_constant__ BatchD
           while (fi < fe) {
             int col = pcol[kr][fi];
             if (col >= hi) break;
-            int sc = st_of(rT[col]);
+            int sc = rT[col];
             if (sc <= 2 && ((phi[kr][fi] & 0x1FFu) >> (strow_r * 3 + sc)) & 1u) mm |= 1u << (col - 32 * ww);
             fi++;
           }
@@ -1893,7 +1899,7 @@ cudaError_t launch_prep(const int8_t *vals, int g, int n, int W, int c, uint64_t
                         uint64_t *valid, uint16_t *ctot, int8_t *valsT, cudaStream_t st) {
   int tot = g * W;
   k_planes<<<(tot + 127) / 128, 128, 0, st>>>(vals, g, n, W, planes, valid);
-  k_transpose<<<(g * n + 255) / 256, 256, 0, st>>>(vals, g, n, valsT);
+  k_transpose<<<(st_stride(g) * n + 255) / 256, 256, 0, st>>>(vals, g, n, valsT);
   if (c > 0) k_ctot<<<(c + 127) / 128, 128, 0, st>>>(planes, g, W, c, ctot);
   return cudaGetLastError();
 }
@@ -1923,7 +1929,8 @@ cudaError_t launch_pairs(const BatchSet *sets, const int32_t *uslot, const uint6
   return cudaGetLastError();
 }
 
-cudaError_t launch_units(const BatchDev &bd, int gmax, int W, cudaStream_t st) {
+cudaError_t launch_units(const BatchDev &bd, int gmax, int W, cudaStream_t st, cudaEvent_t ev_mid,
+                         bool ev_external) {
   const int threads = 256;
   size_t smem = unit_smem_bytes(gmax, W, (gmax + 31) / 32, threads / 32);
   cudaError_t e = cudaFuncSetAttribute(k_units, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -1931,6 +1938,11 @@ cudaError_t launch_units(const BatchDev &bd, int gmax, int W, cudaStream_t st) {
   k_units<<<bd.B, threads, smem, st>>>(bd);
   e = cudaGetLastError();
   if (e != cudaSuccess) return e;
+  if (ev_mid) {
+    e = ev_external ? cudaEventRecordWithFlags(ev_mid, st, cudaEventRecordExternal)
+                    : cudaEventRecord(ev_mid, st);
+    if (e != cudaSuccess) return e;
+  }
   // units per warp: as many as keep about eight warps per SM busy (the SM
   // count read once, thread-safely, from the current device)
   static const int sms = [] {

@@ -19,7 +19,9 @@ cudaError_t launch_counter_masks(int n, int nA, int W, uint64_t seed, const int3
 cudaError_t launch_pairs(const BatchSet *sets, const int32_t *uslot, const uint64_t *masks,
                          uint32_t *dmask, int B, int W, int cmax, unsigned long long *stats,
                          cudaStream_t st);
-// Network, BDeu and JS kernels of a batch (gmax: the largest set).
-cudaError_t launch_units(const BatchDev &bd, int gmax, int W, cudaStream_t st);
+// Network, BDeu and JS kernels of a batch (gmax: the largest set); ev_mid,
+// when given, is recorded between the network kernel and the JS kernel.
+cudaError_t launch_units(const BatchDev &bd, int gmax, int W, cudaStream_t st,
+                         cudaEvent_t ev_mid = nullptr, bool ev_external = false);
 cudaError_t set_divisor_map(const int8_t *map82);
 }  // namespace eddy

@@ -1300,16 +1300,6 @@ static cudaError_t launch_variant(const BatchSet *sets, int nsets, const MmaPlan
   const int grid = plan.ntot < sms ? plan.ntot : sms;
   kern<<<grid, 32 * (2 + kEpi), smem, st>>>(ma, mb, sets, nsets, ctotf, np / kKC, plan.ntot,
                                             stats, err, gqueue, qcap, margc, gcnt, gtab);
-  e = cudaGetLastError();
-  if (e != cudaSuccess) return e;
-  k_general<<<sms * 8, 256, 0, st>>>(sets, uslot, gqueue, qcap, dmask, stats, err);
-  e = cudaGetLastError();
-  if (e != cudaSuccess) return e;
-  // one-warp blocks: the first sms of them land one per SM, which is all a
-  // short list needs; near-threshold batches (hundreds of thousands of
-  // rechecks) fill eight per SM, whose independent FP64 chains keep the
-  // SM's FP64 pipe busy while each waits on its own dependent operations
-  k_exact<<<sms * 8, 32, 0, st>>>(sets, uslot, gqueue, qcap, dmask, stats);
   return cudaGetLastError();
 }
 
@@ -1342,7 +1332,8 @@ cudaError_t launch_pairs_mma(const BatchSet *sets, int nsets, const MmaPlan &pla
                              const uint64_t *masks, const int32_t *uslot, int n, int W,
                              uint8_t *Afp8, const YArena &y, uint32_t *dmask,
                              unsigned long long *stats, unsigned *err, int sms, cudaStream_t st,
-                             int variant, bool core, int g_single) {
+                             int variant, bool core, int g_single, cudaEvent_t ev_mid,
+                             bool ev_external) {
   const int np = mma_npad(n);
   const long long work = (long long)plan.rowsA * (np / 16);
   const int bA = (int)((work + 127) / 128);
@@ -1353,11 +1344,26 @@ cudaError_t launch_pairs_mma(const BatchSet *sets, int nsets, const MmaPlan &pla
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   const unsigned qcap = queue_cap_used(plan.tables);
-  if (core)
-    return launch_shape<true>(sets, nsets, plan, uslot, n, Afp8, y, gqueue, qcap, dmask, stats,
-                              err, sms, st, variant % mma_variants(), g_single);
-  return launch_shape<false>(sets, nsets, plan, uslot, n, Afp8, y, gqueue, qcap, dmask, stats,
-                             err, sms, st, variant % mma_variants(), g_single);
+  e = core ? launch_shape<true>(sets, nsets, plan, uslot, n, Afp8, y, gqueue, qcap, dmask, stats,
+                                err, sms, st, variant % mma_variants(), g_single)
+           : launch_shape<false>(sets, nsets, plan, uslot, n, Afp8, y, gqueue, qcap, dmask, stats,
+                                 err, sms, st, variant % mma_variants(), g_single);
+  if (e != cudaSuccess) return e;
+  // the end of the contraction (a record node when the stream is captured)
+  if (ev_mid) {
+    e = ev_external ? cudaEventRecordWithFlags(ev_mid, st, cudaEventRecordExternal)
+                    : cudaEventRecord(ev_mid, st);
+    if (e != cudaSuccess) return e;
+  }
+  k_general<<<sms * 8, 256, 0, st>>>(sets, uslot, gqueue, qcap, dmask, stats, err);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  // one-warp blocks: the first sms of them land one per SM, which is all a
+  // short list needs; near-threshold batches (hundreds of thousands of
+  // rechecks) fill eight per SM, whose independent FP64 chains keep the
+  // SM's FP64 pipe busy while each waits on its own dependent operations
+  k_exact<<<sms * 8, 32, 0, st>>>(sets, uslot, gqueue, qcap, dmask, stats);
+  return cudaGetLastError();
 }
 
 }  // namespace eddy

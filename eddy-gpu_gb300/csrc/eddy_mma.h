@@ -58,5 +58,6 @@ cudaError_t launch_pairs_mma(const BatchSet *sets, int nsets, const MmaPlan &pla
                              const uint64_t *masks, const int32_t *uslot, int n, int W,
                              uint8_t *Afp8, const YArena &y, uint32_t *dmask,
                              unsigned long long *stats, unsigned *err, int sms, cudaStream_t st,
-                             int variant, bool core, int g_single);
+                             int variant, bool core, int g_single, cudaEvent_t ev_mid = nullptr,
+                             bool ev_external = false);
 }  // namespace eddy

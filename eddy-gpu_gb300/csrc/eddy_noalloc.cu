@@ -45,7 +45,7 @@ __host__ __device__ constexpr size_t al256(size_t x) { return (x + 255) & ~(size
 // region sizes at the maximum shape
 constexpr size_t kOffVals = 0;
 constexpr size_t kOffValsT = kOffVals + al256((size_t)kNAMaxGenes * kNAMaxSamples);
-constexpr size_t kOffPlanes = kOffValsT + al256((size_t)kNAMaxGenes * kNAMaxSamples);
+constexpr size_t kOffPlanes = kOffValsT + al256((size_t)st_stride(kNAMaxGenes) * kNAMaxSamples);
 constexpr size_t kOffValid = kOffPlanes + al256(2 * 8ull * kNAMaxGenes * 3 * kNAW);  // + word-major
 constexpr size_t kOffCtot = kOffValid + al256(8ull * kNAW);
 constexpr size_t kOffPrior = kOffCtot + al256(2ull * 9 * kNAPairs);

@@ -29,7 +29,7 @@ EXPORTS = ["eddy_ctx_create", "eddy_ctx_destroy", "eddy_last_error", "eddy_load_
            "eddy_debug_edges", "eddy_debug_unit", "eddy_run_permutations",
            "eddy_set_stream", "eddy_clear_sets", "eddy_write_networks", "eddy_write_bdeu",
            "eddy_write_edge_list", "eddy_unit_noalloc", "eddy_last_stats", "eddy_device_info",
-           "eddy_last_timing"]
+           "eddy_last_timing", "eddy_last_stage_timing"]
 
 
 class Opts(C.Structure):
@@ -93,6 +93,7 @@ def library(path: str | None = None):
     L.eddy_last_stats.argtypes = [vp, vp, C.POINTER(C.c_int)]
     L.eddy_last_timing.argtypes = [vp, C.POINTER(C.c_double), C.POINTER(C.c_double),
                                    C.POINTER(C.c_double), C.POINTER(C.c_longlong)]
+    L.eddy_last_stage_timing.argtypes = [vp, C.POINTER(C.c_double)]
     _lib = L
     return L
 
@@ -315,4 +316,7 @@ class Context:
         a, b, c = C.c_double(), C.c_double(), C.c_double()
         n = C.c_longlong()
         self._ck(self.L.eddy_last_timing(self.h, C.byref(a), C.byref(b), C.byref(c), C.byref(n)))
-        return dict(ms_kernels=a.value, ms_pairs=b.value, ms_units=c.value, launches=n.value)
+        st = (C.c_double * 4)()
+        self._ck(self.L.eddy_last_stage_timing(self.h, st))
+        return dict(ms_kernels=a.value, ms_pairs=b.value, ms_units=c.value, launches=n.value,
+                    ms_gemm=st[0], ms_decide=st[1], ms_networks=st[2], ms_js=st[3])

@@ -220,6 +220,13 @@ int eddy_device_info(int device, char *name, int name_len, int *sms, int *cc_maj
 int eddy_last_timing(const eddy_ctx *ctx, double *ms_kernels, double *ms_pairs, double *ms_units,
                      long long *launches);
 
+/* The same device time split by kernel, in milliseconds: ms4[0] the
+ * operand and contraction kernels (k_operands, k_pairs_mma; k_pairs on the
+ * popcount path), ms4[1] the general-path and exact decisions (k_general,
+ * k_exact), ms4[2] the network kernel (k_units), ms4[3] normalisation and
+ * JS (k_js).  ms4[0] + ms4[1] = ms_pairs, ms4[2] + ms4[3] = ms_units. */
+int eddy_last_stage_timing(const eddy_ctx *ctx, double *ms4);
+
 #ifdef __cplusplus
 }
 #endif

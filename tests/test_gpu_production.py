@@ -52,6 +52,11 @@ def test_config4_tuned_direct_and_graph_batches(eddy_lib, oracle_lib):
         j, u = ctx.run_permutations(sid, 1 + k * B, B)
         js.append(j)
         U.append(u)
+        # the per-kernel split of the device time adds up to the stage times
+        t = ctx.timing()
+        assert min(t["ms_gemm"], t["ms_decide"], t["ms_networks"], t["ms_js"]) >= 0
+        assert abs(t["ms_gemm"] + t["ms_decide"] - t["ms_pairs"]) <= 0.01 + 1e-3 * t["ms_pairs"]
+        assert abs(t["ms_networks"] + t["ms_js"] - t["ms_units"]) <= 0.01 + 1e-3 * t["ms_units"]
     js, U = np.concatenate(js), np.concatenate(U)
     labs = O.counter_labels(seed, sid, w.labels, B * calls + 1)
     pick = np.array([0, 1, 700, 1023, 1024, 1500, 2047, 2048, 2600, 3071, 3072, 3500, 3900,
