@@ -273,15 +273,19 @@ def run_multiset(args, rank, world, local):
     wall = time.perf_counter() - t0
     ms = e0.elapsed_time(e1)
     t = ctx.timing()
-    units = len(sids) * R
-    failed = sum(1 for s in sids if ctx.summary(s)["failed"])
-    # the same units set by set
+    # the units the run needed: iteration 0 of every set, and the
+    # permutations of the sets whose iteration-0 JS is finite (a set stops
+    # at a non-finite one, main.cu:1431-1435, as the reference's does)
+    iters = [ctx.summary(s)["iterations"] for s in sids]
+    units = int(sum(iters))
+    stop0 = sum(1 for s, it in zip(sids, iters) if it == 1 and R > 1)
+    # the same units set by set: one eddy_run_permutations call per set
     sids = add_all()
     torch.cuda.synchronize()
     f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     f0.record(stream)
-    for sid in sids:
-        ctx.run_permutations(sid, 0, R)
+    for sid, it in zip(sids, iters):
+        ctx.run_permutations(sid, 0, it)
     f1.record(stream)
     torch.cuda.synchronize()
     ms_per_set = f0.elapsed_time(f1)
@@ -290,10 +294,12 @@ def run_multiset(args, rank, world, local):
             "workload": f"config {args.workload}: {len(sids)} sets (sizes {min(sizes)}-"
                         f"{max(sizes)}, median {int(np.median(sizes))}) x {R} iterations "
                         f"(counter stream), {w.data.shape[0]} genes x {w.data.shape[1]} samples",
-            "wall_units_per_s": units / wall, "units": units, "launches": t["launches"],
+            "wall_units_per_s": units / wall, "units": units, "sets": len(sids),
+            "sets_per_s": len(sids) / (ms / 1e3), "ms": ms, "launches": t["launches"],
             "stage_ms": {"k_operands+k_pairs_mma": t["ms_gemm"], "k_general+k_exact": t["ms_decide"],
                          "k_units": t["ms_networks"], "k_js": t["ms_js"]},
-            "sets_failed_at_iteration0": failed,
+            "sets_stopped_at_iteration0": stop0,
+            "sets_with_all_iterations": sum(1 for it in iters if it == R),
             "per_set_value": units / (ms_per_set / 1e3),
             "batching_speedup": ms_per_set / ms}
     print(json.dumps(line), flush=True)

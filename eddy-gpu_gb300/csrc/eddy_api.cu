@@ -997,10 +997,11 @@ int run_jobs(eddy_ctx *ctx, std::vector<Job> &jobs) {
   int gmax = 0, cmax = 1, total = 0;
   size_t per_unit_max = 1;
   // kmax: changed-node records per network (records are written only for
-  // changed nodes, so room for more costs memory, not time: 64 covers every
-  // network of sets whose pair tests all sit near the threshold, measured
-  // at 200 genes; EDDY_KMAX lowers it, to test the re-run of the units that
-  // overflow it)
+  // changed nodes, so room for more costs memory, not time).  64 covers the
+  // networks of most sets; at 200 genes with ~3% of the pair tests within
+  // 20% of the threshold, about one unit in eight of a context's first
+  // batch needs more and is re-run, and the per-size hint gives later
+  // batches that room.  EDDY_KMAX lowers it, to test those re-runs.
   const char *ek = getenv("EDDY_KMAX");
   int kmax = 1;
   for (const Job &J : jobs) {
@@ -1372,16 +1373,20 @@ static int run_set(eddy_ctx *ctx, int set_id) {
   int rc = EDDY_OK;
   const int mpk0 = std::min(ctx->o.max_parents, std::max(g - 1, 1));
   if (ctx->o.rng == EDDY_RNG_COUNTER && n <= 4096) {
-    // counter stream: iteration 0 (the unpermuted labelling, kept) and the
-    // permutations in one pass, labellings generated on the device.  A
-    // non-finite JS at iteration 0 ends the set there (main.cu:1431-1435):
-    // the permutations' results are then discarded.
+    // counter stream, labellings generated on the device: iteration 0 (the
+    // unpermuted labelling, kept), then, unless its JS is not finite, which
+    // ends the set there (main.cu:1431-1435), the permutations in one pass
     std::vector<int32_t> perms(R);
     for (int i = 0; i < R; i++) perms[i] = i;
     KeepOut K;
-    rc = run_units(ctx, set_id, R, nullptr, perms.data(), S.js.data(), S.U.data(),
+    rc = run_units(ctx, set_id, 1, nullptr, perms.data(), S.js.data(), S.U.data(),
                    ctx->o.keep_networks ? &K : nullptr, mpk0, &S.exact, &S.tables);
     if (rc) return rc;
+    if (R > 1 && finite_js(S.js[0])) {
+      rc = run_units(ctx, set_id, R - 1, nullptr, perms.data() + 1, S.js.data() + 1,
+                     S.U.data() + 1, nullptr, 1, &S.exact, &S.tables);
+      if (rc) return rc;
+    }
     finish_counter_set(ctx, S, K, R);
     return EDDY_OK;
   } else {
@@ -1494,8 +1499,10 @@ static void finish_counter_set(eddy_ctx *ctx, SetHost &S, const KeepOut &K, int 
 
 // Sets that share a contingency-kernel choice (one tuning key) on the
 // counter stream, all in one run: their units go through batches that hold
-// several sets each (one set table per batch), iteration 0 of each set kept
-// for its output files.
+// several sets each (one set table per batch).  Iteration 0 of every set
+// runs first (kept for its output files); a set whose JS there is not
+// finite stops (main.cu:1431-1435), so only the other sets' permutations
+// are run, again batched across the sets.
 static int run_counter_sets(eddy_ctx *ctx, const std::vector<int> &ids) {
   const int R = ctx->o.permutations;
   std::vector<Job> jobs(ids.size());
@@ -1512,7 +1519,7 @@ static int run_counter_sets(eddy_ctx *ctx, const std::vector<int> &ids) {
     S.betafit_ok = 0;
     S.exact = S.tables = 0;
     jobs[j].set_id = ids[j];
-    jobs[j].n_units = R;
+    jobs[j].n_units = 1;
     jobs[j].perms = perms.data();
     jobs[j].js = S.js.data();
     jobs[j].U = S.U.data();
@@ -1521,12 +1528,33 @@ static int run_counter_sets(eddy_ctx *ctx, const std::vector<int> &ids) {
   }
   int rc = run_jobs(ctx, jobs);
   if (rc) return rc;
+  std::vector<Job> rest;
+  std::vector<size_t> of;
   for (size_t j = 0; j < ids.size(); j++) {
     SetHost &S = ctx->sets[ids[j]];
     S.exact = jobs[j].exact;
     S.tables = jobs[j].tables;
-    finish_counter_set(ctx, S, keeps[j], R);
+    if (R < 2 || !finite_js(S.js[0])) continue;
+    Job J;
+    J.set_id = ids[j];
+    J.n_units = R - 1;
+    J.perms = perms.data() + 1;
+    J.js = S.js.data() + 1;
+    J.U = S.U.data() + 1;
+    rest.push_back(J);
+    of.push_back(j);
   }
+  if (!rest.empty()) {
+    rc = run_jobs(ctx, rest);
+    if (rc) return rc;
+    for (size_t k = 0; k < rest.size(); k++) {
+      SetHost &S = ctx->sets[ids[of[k]]];
+      S.exact += rest[k].exact;
+      S.tables += rest[k].tables;
+    }
+  }
+  for (size_t j = 0; j < ids.size(); j++)
+    finish_counter_set(ctx, ctx->sets[ids[j]], keeps[j], R);
   return EDDY_OK;
 }
 
