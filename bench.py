@@ -527,8 +527,8 @@ def run_ours(args, rank, world, local):
                                          "and the sampled permutations whose Bonferroni-adjusted p is "
                                          "within +-20% of 0.05 (p_band), or whose chi-square is within "
                                          "+-20% of the critical chi-square (chi2_band)"},
-                       "l2": "per-step working set (decision masks + per-unit scratch) "
-                             f"~{(B * (c * 4 + 600e3)) / 1e9:.2f} GB > L2"},
+                       "l2": "per-launch working set (decision masks + per-unit scratch) "
+                             f"~{(Bl * (c * 4 + 1.3e6)) / 1e9:.2f} GB > L2"},
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h},
             "gpu_launches": acc["launches"],
