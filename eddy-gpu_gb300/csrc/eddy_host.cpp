@@ -56,6 +56,35 @@ static float round_up(double v) {
   return f;
 }
 
+// Bound on |p_ref - p_true| for chi-square values near chi.  AS 147
+// (kernel1.cu:10-74) sums the terms c_k = c_{k-1} x / (p + k) and stops at
+// the first c_k <= 1e-9 x (the running sum); the terms after it fall at
+// least geometrically from the ratio r = x / (p + k + 1) of the next one, so
+// the dropped tail is at most 1e-9 r / (1 - r) of the sum, and the sum times
+// its prefactor is P <= 1.  The ~k FP64 steps and the prefactor's log,
+// lgamma and exp add well under 1e-12.  The stop is replayed at chi and at
+// chi (1 +- 1e-3), which covers every chi-square of the guard band, with a
+// quarter added for a stop one term earlier or later; a ratio above 0.8
+// (far beyond any threshold below the underflow cliff) keeps 1e-8.
+static double as147_eps(double chi, int dof) {
+  const double p = 0.5 * dof;
+  double worst = 0;
+  for (const double f : {1 - 1e-3, 1.0, 1 + 1e-3}) {
+    const double x = 0.5 * chi * f;
+    double c = 1.0, v = 1.0, a = p;
+    for (int k = 0; k < 100000; k++) {
+      a += 1.0;
+      c = c * x / a;
+      v += c;
+      if (c <= 1e-9 * v) break;
+    }
+    const double r = x / (a + 1.0);
+    if (!(r < 0.8)) return 1e-8;
+    worst = std::max(worst, r / (1.0 - r));
+  }
+  return 1e-9 * (worst + 0.25) + 1e-12;
+}
+
 bool compute_thresholds(double alpha_edge, double alpha_edge_prior, int g, int bonferroni,
                         Thr out[2][kDofSlots]) {
   const double aeff[2] = {alpha_edge, std::max(alpha_edge, alpha_edge_prior)};
@@ -64,9 +93,6 @@ bool compute_thresholds(double alpha_edge, double alpha_edge_prior, int g, int b
     if (!(aeff[s] > 0.0) || !(aeff[s] <= 1.0)) exact_all = true;
   // Bonferroni factor as the reference computes it: int ((g-1)*g)/2
   const double C = bonferroni ? (double)(((g - 1) * g) / 2) : 1.0;
-  // |p_ref - p_true| < eps: AS 147 stops at a relative term of 1e-9 in a
-  // tail that decays at least geometrically, plus FP64 rounding.
-  const double eps = 1e-8;
   const double relf = 2e-5;  // FP32 chi-square relative error bound
   static const int dofs[kDofSlots] = {1, 2, 4};
   for (int s = 0; s < 2; s++) {
@@ -80,6 +106,8 @@ bool compute_thresholds(double alpha_edge, double alpha_edge_prior, int g, int b
         chiB = INFINITY;
       } else {
         const double t = aeff[s] / C;
+        // |p_ref - p_true| < eps at the chi-square where p_true = t
+        const double eps = chi2_sf(kc, dof) < t ? as147_eps(invert_sf(t, dof, kc), dof) : 1e-8;
         const double hiT = t * (1 + 1e-9) + eps;  // p above: surely no edge
         const double loT = t * (1 - 1e-9) - eps;  // p below: surely an edge
         if (chi2_sf(0.0, dof) < hiT) chiA = 0.0;
