@@ -82,6 +82,39 @@ def test_gammds_golden_and_scipy(oracle_lib):
     assert oracle_lib.gammds(0.0, 2.0) == 0.0 and oracle_lib.gammds(3.0, 0.0) == 0.0
 
 
+def test_gammds_truncation_within_guard_band(oracle_lib):
+    """The decision guard bands assume |p_ref - p_true| <= 1e-9 (r/(1-r) +
+    0.25) + 1e-12 near a threshold chi-square, r the ratio of the first term
+    AS 147 drops (kernel1.cu:56-68).  Checked around the thresholds of
+    alpha 0.05, the prior-pair alpha 0.328 and 1e-4, Bonferroni factors 1 to
+    130816 (512 genes), dof 1, 2 and 4."""
+    from scipy.stats import chi2
+
+    def bound(chi, dof):
+        worst = 0.0
+        for f in (1 - 1e-3, 1.0, 1 + 1e-3):
+            x, c, v, a = 0.5 * chi * f, 1.0, 1.0, 0.5 * dof
+            while True:
+                a += 1.0
+                c = c * x / a
+                v += c
+                if c <= 1e-9 * v:
+                    break
+            r = x / (a + 1.0)
+            assert r < 0.8
+            worst = max(worst, r / (1.0 - r))
+        return 1e-9 * (worst + 0.25) + 1e-12
+
+    for C in (1, 190, 19900, 130816):
+        for alpha in (0.05, 0.328, 1e-4):
+            for dof in (1, 2, 4):
+                ct = chi2.isf(alpha / C, dof)
+                e = bound(ct, dof)
+                for chi in np.linspace(ct * (1 - 1e-3), ct * (1 + 1e-3), 201):
+                    p_ref = 1.0 - oracle_lib.gammds(chi / 2.0, dof / 2.0)
+                    assert abs(p_ref - chi2.sf(chi, dof)) <= e, (C, alpha, dof, chi)
+
+
 def test_chisq_known_tables(oracle_lib):
     O = oracle_lib
     # balanced independent table: chi = 0, dof 4, no Yates (e = 10)
