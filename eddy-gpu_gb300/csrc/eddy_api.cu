@@ -91,6 +91,7 @@ struct SetHost {
   std::vector<uint8_t> labels; // external labellings R x n
   int R_ext = 0;
   bool done = false;
+  bool it0 = false;  // iteration 0 already run (JS, U, kept outputs), by the batched pass
   std::vector<double> js;
   std::vector<int32_t> U;
   int iterations = 0, failed = 0, betafit_ok = 0;
@@ -1350,12 +1351,14 @@ static int run_set(eddy_ctx *ctx, int set_id) {
   const int g = (int)S.genes.size();
   const int R = set_iterations(ctx, S);
   if (R < 1) return fail(ctx, EDDY_ERR_STATE, "set %d has no labellings", set_id);
-  S.js.assign(R, NAN);
-  S.U.assign(R, 0);
-  S.iterations = 0;
-  S.failed = 0;
-  S.betafit_ok = 0;
-  S.exact = S.tables = 0;
+  if (!S.it0) {
+    S.js.assign(R, NAN);
+    S.U.assign(R, 0);
+    S.iterations = 0;
+    S.failed = 0;
+    S.betafit_ok = 0;
+    S.exact = S.tables = 0;
+  }
   if (g < 2) {
     // no pair: every network is empty, U = 1, JS is NaN (main.cu:1431)
     S.js[0] = NAN;
@@ -1398,17 +1401,20 @@ static int run_set(eddy_ctx *ctx, int set_id) {
       glibc_permutation(ctx->rng, n, ctx->nA, false, lab.data(), ctx->seen, ctx->order);
     labels_to_mask(lab.data(), n, W, masks.data());
     // glibc stream: the permutations are drawn while the GPU runs
-    // iteration 0 and the earlier chunks
+    // iteration 0 and the earlier chunks (a set whose iteration 0 the
+    // batched pass ran draws them only if it goes on)
     std::unique_ptr<GlibcProducer> prod;
-    if (ctx->o.rng == EDDY_RNG_GLIBC && R > 1)
+    if (ctx->o.rng == EDDY_RNG_GLIBC && R > 1 && (!S.it0 || finite_js(S.js[0])))
       prod.reset(new GlibcProducer(ctx->rng, n, ctx->nA, W, R - 1, ctx->labels0.data()));
-    KeepOut K;
-    rc = run_units(ctx, set_id, 1, masks.data(), nullptr, S.js.data(), S.U.data(),
-                   ctx->o.keep_networks ? &K : nullptr, mpk0, &S.exact, &S.tables);
-    if (rc) return rc;
-    if (ctx->o.keep_networks) store_keep(ctx, S, K, g);
-    else S.U0 = S.U[0];
-    S.iterations = 1;
+    if (!S.it0) {
+      KeepOut K;
+      rc = run_units(ctx, set_id, 1, masks.data(), nullptr, S.js.data(), S.U.data(),
+                     ctx->o.keep_networks ? &K : nullptr, mpk0, &S.exact, &S.tables);
+      if (rc) return rc;
+      if (ctx->o.keep_networks) store_keep(ctx, S, K, g);
+      else S.U0 = S.U[0];
+      S.iterations = 1;
+    }
     if (!finite_js(S.js[0])) {
       // main.cu:1431-1435: break after iteration 0 (the stream goes on from
       // the state after its draws: the producer's are discarded)
@@ -1558,6 +1564,48 @@ static int run_counter_sets(eddy_ctx *ctx, const std::vector<int> &ids) {
   return EDDY_OK;
 }
 
+// Iteration 0 of sets on the glibc stream, in shared batches.  Iteration 0
+// labels the samples as given (its draws, main.cu:538-573, leave the labels
+// unchanged), so its networks and JS do not depend on the stream; the
+// stream itself is advanced set by set afterwards, in order (run_set), and
+// only the sets whose iteration-0 JS is finite draw permutations.
+static int run_iteration0_sets(eddy_ctx *ctx, const std::vector<int> &ids) {
+  const int W = ctx->W;
+  std::vector<uint64_t> mask0((size_t)W);
+  labels_to_mask(ctx->labels0.data(), ctx->samples, W, mask0.data());
+  std::vector<Job> jobs(ids.size());
+  std::vector<KeepOut> keeps(ids.size());
+  for (size_t j = 0; j < ids.size(); j++) {
+    SetHost &S = ctx->sets[ids[j]];
+    const int g = (int)S.genes.size(), R = set_iterations(ctx, S);
+    S.js.assign(R, NAN);
+    S.U.assign(R, 0);
+    S.iterations = 0;
+    S.failed = 0;
+    S.betafit_ok = 0;
+    S.exact = S.tables = 0;
+    jobs[j].set_id = ids[j];
+    jobs[j].n_units = 1;
+    jobs[j].masks_host = mask0.data();
+    jobs[j].js = S.js.data();
+    jobs[j].U = S.U.data();
+    jobs[j].keep = ctx->o.keep_networks ? &keeps[j] : nullptr;
+    jobs[j].mpk = std::min(ctx->o.max_parents, std::max(g - 1, 1));
+  }
+  int rc = run_jobs(ctx, jobs);
+  if (rc) return rc;
+  for (size_t j = 0; j < ids.size(); j++) {
+    SetHost &S = ctx->sets[ids[j]];
+    S.exact = jobs[j].exact;
+    S.tables = jobs[j].tables;
+    if (ctx->o.keep_networks) store_keep(ctx, S, keeps[j], (int)S.genes.size());
+    else S.U0 = S.U[0];
+    S.iterations = 1;
+    S.it0 = true;
+  }
+  return EDDY_OK;
+}
+
 int eddy_run(eddy_ctx *ctx) {
   if (!ctx) return EDDY_ERR_ARG;
   if (ctx->samples == 0) return fail(ctx, EDDY_ERR_STATE, "no matrix loaded");
@@ -1574,6 +1622,17 @@ int eddy_run(eddy_ctx *ctx) {
     }
     for (auto &gr : groups) {
       int rc = run_counter_sets(ctx, gr.second);
+      if (rc) return rc;
+    }
+  }
+  if (ctx->o.rng == EDDY_RNG_GLIBC) {
+    std::map<std::pair<int, int>, std::vector<int>> groups;
+    for (int s = 0; s < (int)ctx->sets.size(); s++) {
+      if (ctx->sets[s].done || ctx->sets[s].it0 || ctx->sets[s].genes.size() < 2) continue;
+      groups[tune_key(ctx->samples, shape_of(ctx, s))].push_back(s);
+    }
+    for (auto &gr : groups) {
+      int rc = run_iteration0_sets(ctx, gr.second);
       if (rc) return rc;
     }
   }
