@@ -536,11 +536,22 @@ __device__ __forceinline__ int bdeu_q(const uint16_t *cnt3, int np, int p0, int 
   }
   return q;
 }
+// Tasks of node t's score in one class: one per configuration of the
+// parents after the first (the first parent's states are summed within a
+// task), q / (the first parent's observed-state count), 0 when q is 0.
+__device__ __forceinline__ int bdeu_tasks(const uint16_t *cnt3, int np, int p0, int p1, int p2) {
+  const int q = bdeu_q(cnt3, np, p0, p1, p2);
+  if (q == 0) return 0;
+  const uint16_t *c = cnt3 + p0 * 3;
+  return q / ((c[0] > 0) + (c[1] > 0) + (c[2] > 0));
+}
 
-// One parent configuration j of node t's score over class mask m (the
-// terms of kernel5.cu:30-218 for that j): sum_k LG(q r)[N_jk] - LG(q)[N_j].
-// Summing the terms of all j gives the node's score (fixed point, exact).
-// dmap: the divisor map in shared memory.
+// The terms of kernel5.cu:30-218 for the parent configurations of task j
+// of node t's score over class mask m: configuration j of the parents after
+// the first, with every observed state of the first parent, i.e.
+//   sum over those configurations of  sum_k LG(q r)[N_jk] - LG(q)[N_j].
+// Summing the terms of all tasks gives the node's score (fixed point,
+// exact, in any order).  dmap: the divisor map in shared memory.
 static __device__ __noinline__ int64_t bdeu_config_term(const SetDev &sd, int t, int np, int p0,
                                                         int p1, int p2, const uint64_t *m,
                                                         const uint16_t *cnt3, int j,
@@ -560,31 +571,57 @@ static __device__ __noinline__ int64_t bdeu_config_term(const SetDev &sd, int t,
   const uint64_t *P = sd.planes;
   const int64_t *LGq = sd.lg + (size_t)dmap[q] * sd.lg_stride;
   const int64_t *LGqr = (r > 0) ? sd.lg + (size_t)dmap[q * r] * sd.lg_stride : LGq;
+  // plane rows as word offsets into the planes: the other parents' (the
+  // first parent's own row again when absent: ANDing it twice changes
+  // nothing), the first parent's observed states (repeated past its count;
+  // unused), the child's states
+  auto row_of = [&](int gene, int s) { return (gene * 3 + s) * W; };
   int rem = j;
-  const uint64_t *pp[3] = {P, P, P};
-  for (int k = 1; k <= np; k++) {
+  const int n1 = nstate[1];
+  const int oa0 = row_of(p0, st[1][0]);
+  const int oa1 = row_of(p0, st[1][n1 > 1 ? 1 : 0]);
+  const int oa2 = row_of(p0, st[1][n1 > 2 ? 2 : 0]);
+  int ob[2] = {-1, -1};
+  for (int k = 2; k <= np; k++) {
     const int s = st[k][rem % nstate[k]];
     rem /= nstate[k];
-    pp[k - 1] = P + ((size_t)idx[k] * 3 + s) * W;
+    ob[k - 2] = row_of(idx[k], s);
   }
-  const uint64_t *pt0 = P + ((size_t)t * 3 + (r > 0 ? st[0][0] : 0)) * W;
-  const uint64_t *pt1 = P + ((size_t)t * 3 + (r > 1 ? st[0][1] : 0)) * W;
-  const uint64_t *pt2 = P + ((size_t)t * 3 + (r > 2 ? st[0][2] : 0)) * W;
-  int c0 = 0, c1 = 0, c2 = 0;
+  const int ot0 = row_of(t, r > 0 ? st[0][0] : 0);
+  const int ot1 = row_of(t, r > 1 ? st[0][1] : 0);
+  const int ot2 = row_of(t, r > 2 ? st[0][2] : 0);
+  int c00 = 0, c01 = 0, c02 = 0, c10 = 0, c11 = 0, c12 = 0, c20 = 0, c21 = 0, c22 = 0;
+  const bool has2 = ob[0] >= 0, has3 = ob[1] >= 0;
+  const int ob0 = has2 ? ob[0] : 0, ob1 = has3 ? ob[1] : 0;
   for (int w = 0; w < W; w++) {
-    uint64_t pm = m[w] & pp[0][w];
-    if (np > 1) pm &= pp[1][w];
-    if (np > 2) pm &= pp[2][w];
-    c0 += __popcll(pm & pt0[w]);
-    c1 += __popcll(pm & pt1[w]);
-    c2 += __popcll(pm & pt2[w]);
+    uint64_t pm = m[w];
+    if (has2) pm &= P[ob0 + w];
+    if (has3) pm &= P[ob1 + w];
+    const uint64_t x0 = P[ot0 + w], x1 = P[ot1 + w], x2 = P[ot2 + w];
+    const uint64_t y0 = pm & P[oa0 + w], y1 = pm & P[oa1 + w], y2 = pm & P[oa2 + w];
+    c00 += __popcll(y0 & x0);
+    c01 += __popcll(y0 & x1);
+    c02 += __popcll(y0 & x2);
+    c10 += __popcll(y1 & x0);
+    c11 += __popcll(y1 & x1);
+    c12 += __popcll(y1 & x2);
+    c20 += __popcll(y2 & x0);
+    c21 += __popcll(y2 & x1);
+    c22 += __popcll(y2 & x2);
   }
-  int64_t term = 0;
-  int nij = 0;
-  if (r > 0) { nij += c0; term += LGqr[c0]; }
-  if (r > 1) { nij += c1; term += LGqr[c1]; }
-  if (r > 2) { nij += c2; term += LGqr[c2]; }
-  return term - LGq[nij];
+  // one configuration's terms: counts x0, x1, x2 of the child's states
+  auto conf = [&](int x0, int x1, int x2) -> int64_t {
+    int64_t v = 0;
+    int nij = 0;
+    if (r > 0) { nij += x0; v += LGqr[x0]; }
+    if (r > 1) { nij += x1; v += LGqr[x1]; }
+    if (r > 2) { nij += x2; v += LGqr[x2]; }
+    return v - LGq[nij];
+  };
+  int64_t term = conf(c00, c01, c02);
+  if (n1 > 1) term += conf(c10, c11, c12);
+  if (n1 > 2) term += conf(c20, c21, c22);
+  return term;
 }
 
 }  // namespace eddy

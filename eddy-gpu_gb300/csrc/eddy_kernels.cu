@@ -550,7 +550,7 @@ __device__ void bdeu_items(const SetDev &sd, const UnitPtrs &P, int *scan, int n
       const int p0 = (int)((key >> 16) & 0xFFFF), p1 = (int)((key >> 32) & 0xFFFF),
                 p2 = (int)((key >> 48) & 0xFFFF);
       for (int cls = 0; cls < 2; cls++) {
-        P.tq[2 * i + cls] = np ? bdeu_q(P.cnt3 + 3 * g * cls, np, p0, p1, p2) : 0;
+        P.tq[2 * i + cls] = np ? bdeu_tasks(P.cnt3 + 3 * g * cls, np, p0, p1, p2) : 0;
         P.acc[2 * i + cls] = 0;
       }
     }
@@ -1767,6 +1767,7 @@ constexpr int kJsWarps = 8;
 __global__ void __launch_bounds__(32 * kJsWarps) k_js(const __grid_constant__ BatchDev bd, int upw) {
   __shared__ int pre[kJsWarps][33];
   __shared__ double acc[kJsWarps][3][32];
+  __shared__ long long red[kJsWarps][6][32];  // per unit: min, max (class 1, 2), sums
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int u0 = (blockIdx.x * kJsWarps + warp) * upw, u = u0 + lane;
   const bool mine = lane < upw && u < bd.B;
@@ -1784,27 +1785,6 @@ __global__ void __launch_bounds__(32 * kJsWarps) k_js(const __grid_constant__ Ba
   auto dist_of = [&](int o) {
     return (long long *)__shfl_sync(0xffffffffu, dptr, o);
   };
-  long long l0 = LLONG_MAX, h0 = LLONG_MIN, l1 = LLONG_MAX, h1 = LLONG_MIN;
-  double m0 = 0.0, m1 = 0.0, sA = 0.0, sB = 0.0;
-  if (U > 0) {
-    const long long *d = (const long long *)dptr;
-    for (int uu = 0; uu < U; uu++) {
-      const long long a = d[uu], b = d[S + uu];
-      l0 = a < l0 ? a : l0;
-      h0 = a > h0 ? a : h0;
-      l1 = b < l1 ? b : l1;
-      h1 = b > h1 ? b : h1;
-    }
-    long long q0 = 0, q1 = 0;
-    for (int uu = 0; uu < U; uu++) {
-      q0 += d[uu] - l0;
-      q1 += d[S + uu] - l1;
-    }
-    m0 = (double)q0 / (double)U;
-    m1 = (double)q1 / (double)U;
-    sA = 10.0 / (double)(h0 - l0);
-    sB = 10.0 / (double)(h1 - l1);
-  }
   const int keep = (U > 0 && bd.keep_slot) ? bd.keep_slot[u] : -1;
   // the warp's units as prefix intervals of the flattened list
   int incl = U;
@@ -1816,6 +1796,9 @@ __global__ void __launch_bounds__(32 * kJsWarps) k_js(const __grid_constant__ Ba
   pre[warp][lane] = incl - U;
   if (lane == 31) pre[warp][32] = incl;
   acc[warp][0][lane] = acc[warp][1][lane] = acc[warp][2][lane] = 0.0;
+  red[warp][0][lane] = red[warp][2][lane] = LLONG_MAX;
+  red[warp][1][lane] = red[warp][3][lane] = LLONG_MIN;
+  red[warp][4][lane] = red[warp][5][lane] = 0;
   __syncwarp();
   const int total = pre[warp][32];
   // owner of network i: the last unit whose interval starts at or before i
@@ -1828,6 +1811,77 @@ __global__ void __launch_bounds__(32 * kJsWarps) k_js(const __grid_constant__ Ba
     }
     return lo;
   };
+  // the run's last live lane: the one after it has another owner or is dead
+  auto run_end = [&](int o, bool live) {
+    const int on = __shfl_down_sync(0xffffffffu, o, 1);
+    const bool nlive = __shfl_down_sync(0xffffffffu, live ? 1 : 0, 1) != 0;
+    return live && (lane == 31 || on != o || !nlive);
+  };
+  // v combined (op) over this lane's run of equal owners, ending at the
+  // run's last lane
+  auto seg_scan = [&](long long v, int o, auto op) {
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+      const long long y = __shfl_up_sync(0xffffffffu, v, d);
+      const int oy = __shfl_up_sync(0xffffffffu, o, d);
+      if (lane >= d && oy == o) v = op(v, y);
+    }
+    return v;
+  };
+  auto mn = [](long long a, long long b) { return a < b ? a : b; };
+  auto mx = [](long long a, long long b) { return a > b ? a : b; };
+  auto ad = [](long long a, long long b) { return a + b; };
+  // pass 0: each unit's smallest and largest score per class, then the sum
+  // of the scores less the smallest (exact integers), over the flattened list
+  for (int i0 = 0; i0 < total; i0 += 32) {
+    const int i = i0 + lane;
+    const bool live = i < total;
+    const int o = live ? owner(i) : 31;
+    const long long *d = dist_of(o);
+    long long a = LLONG_MAX, b = LLONG_MAX;
+    if (live) {
+      const int uu = i - pre[warp][o];
+      a = d[uu];
+      b = d[S + uu];
+    }
+    const long long a0 = seg_scan(a, o, mn), a1 = seg_scan(live ? a : LLONG_MIN, o, mx);
+    const long long b0 = seg_scan(b, o, mn), b1 = seg_scan(live ? b : LLONG_MIN, o, mx);
+    if (run_end(o, live)) {
+      red[warp][0][o] = mn(red[warp][0][o], a0);
+      red[warp][1][o] = mx(red[warp][1][o], a1);
+      red[warp][2][o] = mn(red[warp][2][o], b0);
+      red[warp][3][o] = mx(red[warp][3][o], b1);
+    }
+    __syncwarp();
+  }
+  const long long l0 = red[warp][0][lane], h0 = red[warp][1][lane];
+  const long long l1 = red[warp][2][lane], h1 = red[warp][3][lane];
+  for (int i0 = 0; i0 < total; i0 += 32) {
+    const int i = i0 + lane;
+    const bool live = i < total;
+    const int o = live ? owner(i) : 31;
+    const long long *d = dist_of(o);
+    const long long ol0 = __shfl_sync(0xffffffffu, l0, o), ol1 = __shfl_sync(0xffffffffu, l1, o);
+    long long a = 0, b = 0;
+    if (live) {
+      const int uu = i - pre[warp][o];
+      a = d[uu] - ol0;
+      b = d[S + uu] - ol1;
+    }
+    const long long qa = seg_scan(a, o, ad), qb = seg_scan(b, o, ad);
+    if (run_end(o, live)) {
+      red[warp][4][o] += qa;
+      red[warp][5][o] += qb;
+    }
+    __syncwarp();
+  }
+  double m0 = 0.0, m1 = 0.0, sA = 0.0, sB = 0.0;
+  if (U > 0) {
+    m0 = (double)red[warp][4][lane] / (double)U;
+    m1 = (double)red[warp][5][lane] / (double)U;
+    sA = 10.0 / (double)(h0 - l0);
+    sB = 10.0 / (double)(h1 - l1);
+  }
   // sum of v over this lane's run of equal owners, added to dst[owner] by
   // the run's last live lane
   auto seg_add = [&](double v, int o, bool live, double *dst) {
