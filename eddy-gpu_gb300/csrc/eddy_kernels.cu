@@ -404,6 +404,9 @@ struct UnitSmem {
 
 // BDeu work items (node scores) processed per round
 constexpr int kItems = 512;
+// the task prefix array (2 kItems + 1 ints) also holds the memo offsets of
+// the 2g rows of a unit, g <= 512 (the library's gene-set limit)
+static_assert(2 * 512 <= 2 * kItems + 1, "memo offsets do not fit the task prefix array");
 
 struct UnitPtrs {
   uint64_t *mA, *mB;      // [W]
@@ -1135,8 +1138,28 @@ __global__ void __launch_bounds__(256, 3) k_units(const __grid_constant__ BatchD
   // the capped list of each row with 1..kMemoE kept entries under every
   // non-empty subset of them (the entries a left-out sample triggers):
   // the record entry (t, first three parents) when it differs from the
-  // full network's list, and its hash; one thread per (row, subset)
+  // full network's list, and its hash; one thread per (row, subset).
+  // Packed by row: row i's 2^e - 1 lists from moff[i] on (the task prefix
+  // array is free from the signatures until the BDeu phase), so the lists
+  // the records read lie close together.
   unsigned long long *memo = (unsigned long long *)(scr + L.memo);
+  int *moff = P.tq;
+  {
+    int running = 0;
+    for (int i0 = 0; i0 < 2 * g; i0 += nt) {
+      const int i = i0 + tid;
+      int sz = 0;
+      if (i < 2 * g) {
+        const int e = P.phe[i] - P.phs[i];
+        sz = (e >= 1 && e <= kMemoE) ? (1 << e) - 1 : 0;
+      }
+      int total;
+      const int off = block_scan(sz, total, SM.scan);
+      if (i < 2 * g) moff[i] = running + off;
+      running += total;
+    }
+    __syncthreads();
+  }
   for (int task = tid; task < 2 * g * kMemoSub; task += nt) {
     const int i = task / kMemoSub, msub = task - i * kMemoSub + 1;
     const int e0 = P.phs[i], e1 = P.phe[i];
@@ -1165,7 +1188,7 @@ __global__ void __launch_bounds__(256, 3) k_units(const __grid_constant__ BatchD
     }
     // a shorter list than the full network's differs too
     if (cnt < sd.mp && Go.next() >= 0) diff = true;
-    unsigned long long *M = memo + ((size_t)i * kMemoSub + (msub - 1)) * 2;
+    unsigned long long *M = memo + ((size_t)moff[i] + (msub - 1)) * 2;
     M[0] = diff ? ((unsigned long long)t | ((unsigned long long)(cnt < 3 ? cnt : 3) << 14) |
                    ((unsigned long long)(ps[0] & 0xFFFF) << 16) |
                    ((unsigned long long)(ps[1] & 0xFFFF) << 32) |
@@ -1206,7 +1229,7 @@ __global__ void __launch_bounds__(256, 3) k_units(const __grid_constant__ BatchD
             if (sc <= 2 && (((phi[k][e0 + q] & 0x1FFu) >> (sr + sc)) & 1u)) msub |= 1 << q;
           }
           if (msub) {
-            const unsigned long long *M = memo + ((size_t)(k * g + t) * kMemoSub + (msub - 1)) * 2;
+            const unsigned long long *M = memo + ((size_t)moff[k * g + t] + (msub - 1)) * 2;
             if (M[0] != ~0ull) {
               changed = true;
               ent = M[0];
