@@ -395,6 +395,7 @@ struct UnitSmem {
   int firstE2;  // first class-2 network with an empty signature (S - 1: none)
   int ncand;    // candidates for unique networks
   int maxchg;   // most changed nodes of a network past kmax (0: none)
+  int nlg;      // keys of merged-row lists logged by the records
   int scan[32];
   unsigned status;
   int U;
@@ -1144,6 +1145,17 @@ __global__ void __launch_bounds__(256, 3) k_units(const __grid_constant__ BatchD
   // the records read lie close together.
   unsigned long long *memo = (unsigned long long *)(scr + L.memo);
   int *moff = P.tq;
+  uint32_t *used = (uint32_t *)P.fsc;
+  // a changed node's key (node, first three parents) unless it equals the
+  // full network's: the items scored in the BDeu phase
+  auto differs = [&](int k, unsigned long long e) -> bool {
+    const int t = (int)(e & 0x3FFF), np = (int)((e >> 14) & 3);
+    const int fnp = P.fcnt[k * g + t] < 3 ? P.fcnt[k * g + t] : 3;
+    if (np != fnp) return true;
+    for (int q = 0; q < np; q++)
+      if ((int)((e >> (16 + 16 * q)) & 0xFFFF) != (int)P.fps[(k * g + t) * 3 + q]) return true;
+    return false;
+  };
   {
     int running = 0;
     for (int i0 = 0; i0 < 2 * g; i0 += nt) {
@@ -1158,6 +1170,10 @@ __global__ void __launch_bounds__(256, 3) k_units(const __grid_constant__ BatchD
       if (i < 2 * g) moff[i] = running + off;
       running += total;
     }
+    // the lists the records use, one bit each (the base score array is
+    // free until the BDeu phase: 32 g bytes >= 2 g kMemoSub bits)
+    for (int w = tid; w < (running + 31) / 32; w += nt) used[w] = 0u;
+    if (tid == 0) SM.nlg = 0;
     __syncthreads();
   }
   for (int task = tid; task < 2 * g * kMemoSub; task += nt) {
@@ -1229,11 +1245,13 @@ __global__ void __launch_bounds__(256, 3) k_units(const __grid_constant__ BatchD
             if (sc <= 2 && (((phi[k][e0 + q] & 0x1FFu) >> (sr + sc)) & 1u)) msub |= 1 << q;
           }
           if (msub) {
-            const unsigned long long *M = memo + ((size_t)moff[k * g + t] + (msub - 1)) * 2;
+            const int mi = moff[k * g + t] + msub - 1;
+            const unsigned long long *M = memo + (size_t)mi * 2;
             if (M[0] != ~0ull) {
               changed = true;
               ent = M[0];
               hn = M[1];
+              if (!((used[mi >> 5] >> (mi & 31)) & 1u)) atomicOr(&used[mi >> 5], 1u << (mi & 31));
             }
           }
         } else {
@@ -1264,6 +1282,11 @@ __global__ void __launch_bounds__(256, 3) k_units(const __grid_constant__ BatchD
                 ((unsigned long long)(ps[0] & 0xFFFF) << 16) |
                 ((unsigned long long)(ps[1] & 0xFFFF) << 32) |
                 ((unsigned long long)(ps[2] & 0xFFFF) << 48);
+          if (differs(k, ent)) {
+            // logged in the signature table's keys (free from here on)
+            const int ix = atomicAdd(&SM.nlg, 1);
+            if (ix < HTs) hsk[ix] = ent;
+          }
         }
       }
       unsigned bal = __ballot_sync(0xffffffffu, changed);
@@ -1482,6 +1505,74 @@ __global__ void __launch_bounds__(256, 3) k_units(const __grid_constant__ BatchD
   if (bd.stats && tid == 0)
     atomicAdd(&bd.stats[4 * (size_t)bd.uslot[u] + 3], (unsigned long long)(S - U));
 
+  // ---- Keys of the changed nodes' lists.  The leave-one-out networks of a
+  // unit share most of their changed nodes' lists (one flip near a
+  // threshold changes the same node in every network whose left-out sample
+  // triggers it), so the items hold few distinct keys (node, first three
+  // parents): ~240 among ~24000 items per unit when nearly every pair sits
+  // near the threshold.  Each distinct key is scored once, in a
+  // shared-memory table of KT slots (in the flip-entry cache, which no phase
+  // reads from here on), and every item adds its key's score.  The keys are
+  // the memo lists the records used and the logged merged-row lists; when
+  // more were logged than the log holds, the items are walked instead.  A
+  // key that finds no slot within kKeyProbes probes: every item is scored
+  // on its own.
+  constexpr int kKeyProbes = 64;
+  const int KT = HT < kKeyT ? HT : kKeyT;  // slot-indexed scores fit ksc ([HT][2])
+  unsigned long long *kt = (unsigned long long *)P.ephi;
+  const unsigned kmask = (unsigned)KT - 1u;
+  if (compacted && bd.keep_slot && bd.keep_slot[u] >= 0) {
+    // the detailed outputs still read the flip entries: back to the
+    // unit's scratch, each class's (nent[k] <= c) to its own arrays, the
+    // class-2 row ranges shifted to start at 0
+    const int ne0 = SM.nent[0], ne = ne0 + SM.nent[1];
+    for (int k = 0; k < 2; k++) {
+      uint32_t *gphi = (uint32_t *)(scr + L.phi[k]);
+      uint16_t *gpcol = (uint16_t *)(scr + L.pcol[k]);
+      const int e0 = k ? ne0 : 0, e1 = k ? ne : ne0;
+      for (int i = e0 + tid; i < e1; i += nt) {
+        gphi[i - e0] = P.ephi[i];
+        gpcol[i - e0] = P.epcol[i];
+      }
+      phi[k] = gphi;
+      pcol[k] = gpcol;
+    }
+    for (int t = tid; t < g; t += nt)
+      if (P.phs[g + t] < P.phe[g + t]) {
+        P.phs[g + t] -= ne0;
+        P.phe[g + t] -= ne0;
+      }
+    __syncthreads();
+  }
+  for (int i = tid; i < KT; i += nt) kt[i] = ~0ull;
+  if (tid == 0) SM.tfull = 0;
+  __syncthreads();
+  auto insert_key = [&](unsigned long long rc) {
+    unsigned slot = (unsigned)(mix64(rc) & kmask);
+    for (int pr = 0; pr < kKeyProbes; pr++, slot = (slot + 1u) & kmask) {
+      // a slot only ever goes from empty to its final key: a read first,
+      // the atomic only on an empty slot
+      unsigned long long cur = kt[slot];
+      if (cur == ~0ull) cur = atomicCAS(&kt[slot], ~0ull, rc);
+      if (cur == ~0ull || cur == rc) return;
+    }
+    SM.tfull = 1;
+  };
+  const bool keys_logged = SM.nlg <= HTs;
+  if (keys_logged) {
+    for (int task = tid; task < 2 * g * kMemoSub; task += nt) {
+      const int i = task / kMemoSub, q = task - i * kMemoSub;
+      const int e = P.phe[i] - P.phs[i];
+      if (e < 1 || e > kMemoE || q >= (1 << e) - 1) continue;
+      const int mi = moff[i] + q;
+      if (!((used[mi >> 5] >> (mi & 31)) & 1u)) continue;
+      const unsigned long long ent = memo[(size_t)mi * 2];
+      if (differs(i / g, ent)) insert_key(ent);
+    }
+    for (int x = tid; x < SM.nlg; x += nt) insert_key(hsk[x]);
+  }
+  __syncthreads();
+
   // ---- P5: BDeu.  Base node scores of the two full networks: nodes
   // without parents from the state counts, the others as flat tasks; a
   // class-2 node whose capped parents equal the class-1 one copies its score.
@@ -1566,14 +1657,6 @@ __global__ void __launch_bounds__(256, 3) k_units(const __grid_constant__ BatchD
     net_of(s, sd, sig, k, sigma);
     rec = rec_of(s)[2 + (e - wl[uu])];
   };
-  auto differs = [&](int k, unsigned long long e) -> bool {
-    const int t = (int)(e & 0x3FFF), np = (int)((e >> 14) & 3);
-    const int fnp = P.fcnt[k * g + t] < 3 ? P.fcnt[k * g + t] : 3;
-    if (np != fnp) return true;
-    for (int q = 0; q < np; q++)
-      if ((int)((e >> (16 + 16 * q)) & 0xFFFF) != (int)P.fps[(k * g + t) * 3 + q]) return true;
-    return false;
-  };
   // the score delta of item e, given its key's scores in both classes
   auto add_delta = [&](int uu, int k, unsigned long long rec, long long s1, long long s2) {
     const int t = (int)(rec & 0x3FFF), np = (int)((rec >> 14) & 3);
@@ -1586,47 +1669,6 @@ __global__ void __launch_bounds__(256, 3) k_units(const __grid_constant__ BatchD
     atomicAdd((unsigned long long *)&dist[S + uu],
               (unsigned long long)(s2 - P.fsc[(k * 2 + 1) * g + t]));
   };
-  // The leave-one-out networks of a unit share most of their changed nodes'
-  // lists (one flip near a threshold changes the same node in every network
-  // whose left-out sample triggers it), so the items hold few distinct keys
-  // (node, first three parents): ~240 among ~19500 items per unit when
-  // nearly every pair sits near the threshold.  Each distinct key is scored
-  // once, in a shared-memory table of KT slots, and every item adds its
-  // key's score.  A key that finds no slot within kKeyProbes probes: every
-  // item is scored on its own.
-  constexpr int kKeyProbes = 64;
-  const int KT = HT < kKeyT ? HT : kKeyT;  // slot-indexed scores fit ksc ([HT][2])
-  unsigned long long *kt = (unsigned long long *)P.ephi;
-  int *kpos = htv;  // key list index -> slot
-  unsigned long long *klist = hsk;
-  long long *ksc = (long long *)(scr + L.ksc);
-  const unsigned kmask = (unsigned)KT - 1u;
-  if (compacted && bd.keep_slot && bd.keep_slot[u] >= 0) {
-    // the detailed outputs still read the flip entries: back to the
-    // unit's scratch, each class's (nent[k] <= c) to its own arrays, the
-    // class-2 row ranges shifted to start at 0
-    const int ne0 = SM.nent[0], ne = ne0 + SM.nent[1];
-    for (int k = 0; k < 2; k++) {
-      uint32_t *gphi = (uint32_t *)(scr + L.phi[k]);
-      uint16_t *gpcol = (uint16_t *)(scr + L.pcol[k]);
-      const int e0 = k ? ne0 : 0, e1 = k ? ne : ne0;
-      for (int i = e0 + tid; i < e1; i += nt) {
-        gphi[i - e0] = P.ephi[i];
-        gpcol[i - e0] = P.epcol[i];
-      }
-      phi[k] = gphi;
-      pcol[k] = gpcol;
-    }
-    for (int t = tid; t < g; t += nt)
-      if (P.phs[g + t] < P.phe[g + t]) {
-        P.phs[g + t] -= ne0;
-        P.phe[g + t] -= ne0;
-      }
-    __syncthreads();
-  }
-  for (int i = tid; i < KT; i += nt) kt[i] = ~0ull;
-  if (tid == 0) SM.tfull = 0;
-  __syncthreads();
   // the items of unique network uu whose list differs from the full
   // network's, in record order, read four records at a time
   auto for_items = [&](int uu, auto &&fn) {
@@ -1643,20 +1685,15 @@ __global__ void __launch_bounds__(256, 3) k_units(const __grid_constant__ BatchD
         if (rb[q] != ~0ull && differs(k, rb[q])) fn(k, rb[q]);
     }
   };
-  // a thread per unique network inserts its items' keys
-  for (int uu = tid; uu < U; uu += nt)
-    for_items(uu, [&](int, unsigned long long rc) {
-      unsigned slot = (unsigned)(mix64(rc) & kmask);
-      for (int pr = 0; pr < kKeyProbes; pr++, slot = (slot + 1u) & kmask) {
-        // a slot only ever goes from empty to its final key: a read first,
-        // the atomic only on an empty slot
-        unsigned long long cur = kt[slot];
-        if (cur == ~0ull) cur = atomicCAS(&kt[slot], ~0ull, rc);
-        if (cur == ~0ull || cur == rc) return;
-      }
-      SM.tfull = 1;
-    });
-  __syncthreads();
+  int *kpos = htv;  // key list index -> slot
+  unsigned long long *klist = hsk;
+  long long *ksc = (long long *)(scr + L.ksc);
+  if (!keys_logged) {
+    // a thread per unique network inserts its items' keys
+    for (int uu = tid; uu < U; uu += nt)
+      for_items(uu, [&](int, unsigned long long rc) { insert_key(rc); });
+    __syncthreads();
+  }
   if (!SM.tfull) {
     // the keys in slot order: key list and slot -> list index
     int nk = 0;
