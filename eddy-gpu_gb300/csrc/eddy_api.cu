@@ -744,6 +744,7 @@ int run_batch(eddy_ctx *ctx, std::vector<Job> &jobs, const std::vector<UnitRef> 
   bd.B = Bt;
   bd.nsets = ns;
   bd.kmax = kmax;
+  bd.key_walk = getenv("EDDY_KEY_WALK") ? 1 : 0;
   bd.sets = ctx->d_sets.as<BatchSet>();
   bd.uslot = ctx->d_uslot.as<int32_t>();
   bd.masks = ctx->d_masks.as<uint64_t>();
@@ -820,7 +821,7 @@ int run_batch(eddy_ctx *ctx, std::vector<Job> &jobs, const std::vector<UnitRef> 
                                   (uintptr_t)ctx->d_stats.p, (uintptr_t)ctx->d_afp8.p,
                                   (uintptr_t)ctx->d_Y.p, (uintptr_t)ctx->d_err.p,
                                   (uintptr_t)ctx->d_mask0.p, (uintptr_t)ctx->stream,
-                                  (uintptr_t)bp.sets[0].sd.exact_all};
+                                  (uintptr_t)bp.sets[0].sd.exact_all, (uintptr_t)bd.key_walk};
     for (int k = 0; k < ns; k++) {
       key.push_back((uintptr_t)ids[k]);
       key.push_back((uintptr_t)bp.sets[k].nb);

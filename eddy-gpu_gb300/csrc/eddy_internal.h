@@ -120,6 +120,8 @@ struct BatchDev {
   int B;                       // units in the batch
   int nsets;                   // sets in the batch
   int kmax;                    // changed-node records per network
+  int key_walk;                // 1: the key table from a walk over the unique
+                               // networks' records (EDDY_KEY_WALK, a test switch)
   const BatchSet *sets;        // [nsets]
   const int32_t *uslot;        // [B] set of each unit (index into sets)
   const uint64_t *masks;       // [B][W] class-1 sample mask per unit

@@ -1558,7 +1558,7 @@ __global__ void __launch_bounds__(256, 3) k_units(const __grid_constant__ BatchD
     }
     SM.tfull = 1;
   };
-  const bool keys_logged = SM.nlg <= HTs;
+  const bool keys_logged = !bd.key_walk && SM.nlg <= HTs;
   if (keys_logged) {
     for (int task = tid; task < 2 * g * kMemoSub; task += nt) {
       const int i = task / kMemoSub, q = task - i * kMemoSub;

@@ -161,3 +161,34 @@ def test_edge_list_matches_oracle(cfg, eddy_lib, oracle_lib):
     assert np.array_equal(el["epn"], epn)
     assert np.array_equal(el["edges"], pe)
     ctx.close()
+
+
+def test_key_table_paths_agree(eddy_lib, oracle_lib, monkeypatch):
+    """The unit kernel's table of distinct changed-node keys, built from the
+    memo lists the records mark and the merged-row keys they log, and built
+    by walking every unique network's records (EDDY_KEY_WALK=1, the path
+    taken when the log overflows), give the same JS and U at the
+    precision-stress shape, and agree with the oracle."""
+    from eddy_gpu import synth
+    O = oracle_lib
+    w = synth.make(4, seed=1)
+    genes = w.sets[0][1]
+    mp, pw = w.flags["mp"], w.flags["pw"]
+    out = []
+    for walk in (False, True):
+        if walk:
+            monkeypatch.setenv("EDDY_KEY_WALK", "1")
+        ctx = eddy_lib.Context(max_parents=mp, prior_weight=pw, permutations=65,
+                               rng=eddy_lib.RNG_COUNTER, seed=9, keep_networks=False)
+        ctx.load_matrix(w.data, w.labels)
+        sid = ctx.add_set(genes)
+        out.append(ctx.run_permutations(sid, 1, 64))
+        ctx.close()
+    monkeypatch.delenv("EDDY_KEY_WALK")
+    (js0, U0), (js1, U1) = out
+    assert np.array_equal(U0, U1)
+    assert np.array_equal(js0, js1, equal_nan=True)
+    labs = O.counter_labels(9, sid, w.labels, 65)
+    ojs, oU = O.units(w.data[genes], labs[[1, 64]], None, O.params(mp=mp, pw=pw))
+    assert np.array_equal(U0[[0, 63]], oU)
+    assert _close(js0[[0, 63]], ojs)
