@@ -1215,8 +1215,18 @@ __global__ void __launch_bounds__(256, 3) k_units(const __grid_constant__ BatchD
   __syncthreads();
 
   // one record per distinct signature: changed nodes (capped list differs
-  // from the full network's) with their lists, and the network hash
+  // from the full network's) with their lists, and the network hash.  A
+  // warp per network.  A first pass over the rows holding entries finds
+  // the rows whose entries the left-out sample triggers (shared memory
+  // only) and lists them (row | subset << 16, or a merged-row mark) in the
+  // warp's part of the BDeu item arrays, idle from the signatures until the
+  // dedup; a second pass looks up (or merges) the listed rows' lists 32 at
+  // a time, so a network's memo loads are in flight together.
+  constexpr int kMergedRow = 0x8000;  // a row with more than kMemoE entries
   int8_t *myst = P.stsig + (size_t)warp * st_stride(g);
+  uint32_t *lsts = reinterpret_cast<uint32_t *>(P.itk);  // P.acc follows P.itk
+  const int lcap = (int)((reinterpret_cast<uint32_t *>(P.acc + 2 * kItems) - lsts) / nw) & ~31;
+  uint32_t *lst = lsts + (size_t)warp * lcap;
   const int nwl = SM.nwl;
   for (int wi = warp; wi < nwl; wi += nw) {
     const int s = wl[wi];
@@ -1226,26 +1236,20 @@ __global__ void __launch_bounds__(256, 3) k_units(const __grid_constant__ BatchD
     const int nrk = SM.nrphi[k];
     load_stsig(sd, sigma, myst, lane);
     unsigned long long dh = 0;
-    int nchg = 0;
-    for (int t0 = 0; t0 < nrk; t0 += 32) {
-      const int t = (t0 + lane < nrk) ? (int)P.rphi[k * g + t0 + lane] : -1;
-      bool changed = false;
-      unsigned long long hn = 0, ent = 0;
-      int ps[3] = {0xFFFF, 0xFFFF, 0xFFFF};
-      int cnt = 0;
-      bool flips = false;
-      if (t >= 0 && myst[t] <= 2) {
-        // the entries of row t that sample sigma triggers
-        const int sr = myst[t] * 3;
-        const int e0 = P.phs[k * g + t], e1 = P.phe[k * g + t];
-        if (e1 - e0 <= kMemoE) {
-          int msub = 0;
-          for (int q = 0; q < e1 - e0; q++) {
-            const int sc = myst[pcol[k][e0 + q]];
-            if (sc <= 2 && (((phi[k][e0 + q] & 0x1FFu) >> (sr + sc)) & 1u)) msub |= 1 << q;
-          }
-          if (msub) {
-            const int mi = moff[k * g + t] + msub - 1;
+    int nchg = 0, nl = 0;
+    auto flush = [&]() {
+      __syncwarp();
+      for (int l0 = 0; l0 < nl; l0 += 32) {
+        const int l = l0 + lane;
+        bool changed = false;
+        unsigned long long hn = 0, ent = 0;
+        int t = 0;
+        if (l < nl) {
+          const uint32_t le = lst[l];
+          t = (int)(le & 0xFFFFu);
+          const int sub = (int)(le >> 16);
+          if (sub != kMergedRow) {
+            const int mi = moff[k * g + t] + sub - 1;
             const unsigned long long *M = memo + (size_t)mi * 2;
             if (M[0] != ~0ull) {
               changed = true;
@@ -1253,50 +1257,74 @@ __global__ void __launch_bounds__(256, 3) k_units(const __grid_constant__ BatchD
               hn = M[1];
               if (!((used[mi >> 5] >> (mi & 31)) & 1u)) atomicOr(&used[mi >> 5], 1u << (mi & 31));
             }
+          } else {
+            ListGen Gn, Go;
+            gen_for(Gn, sd, P, phi[k], pcol[k], k, t, myst);
+            gen_for(Go, sd, P, phi[k], pcol[k], k, t, nullptr);
+            uint64_t h = node_hash_init(sd.salt, t);
+            int cnt = 0, ps[3] = {0xFFFF, 0xFFFF, 0xFFFF};
+            bool diff = false;
+            for (int i = 0; i < sd.mp; i++) {
+              int x = Gn.next(), y = Go.next();
+              if (x != y) diff = true;
+              if (x < 0) break;
+              if (cnt < 3) ps[cnt] = x;
+              h = node_hash_step(h, x);
+              cnt++;
+            }
+            if (diff) {
+              changed = true;
+              hn = h;
+              ent = (unsigned long long)t | ((unsigned long long)(cnt < 3 ? cnt : 3) << 14) |
+                    ((unsigned long long)(ps[0] & 0xFFFF) << 16) |
+                    ((unsigned long long)(ps[1] & 0xFFFF) << 32) |
+                    ((unsigned long long)(ps[2] & 0xFFFF) << 48);
+              if (differs(k, ent)) {
+                // logged in the signature table's keys (free from here on)
+                const int ix = atomicAdd(&SM.nlg, 1);
+                if (ix < HTs) hsk[ix] = ent;
+              }
+            }
+          }
+        }
+        const unsigned bal = __ballot_sync(0xffffffffu, changed);
+        if (changed) {
+          const int pos = nchg + __popc(bal & ((1u << lane) - 1u));
+          dh += hn - P.fh[k * g + t];
+          if (pos < bd.kmax) R[2 + pos] = ent;
+        }
+        nchg += __popc(bal);
+      }
+      nl = 0;
+      __syncwarp();
+    };
+    for (int t0 = 0; t0 < nrk; t0 += 32) {
+      const int t = (t0 + lane < nrk) ? (int)P.rphi[k * g + t0 + lane] : -1;
+      int sub = 0;
+      if (t >= 0 && myst[t] <= 2) {
+        // the entries of row t that sample sigma triggers
+        const int sr = myst[t] * 3;
+        const int e0 = P.phs[k * g + t], e1 = P.phe[k * g + t];
+        if (e1 - e0 <= kMemoE) {
+          for (int q = 0; q < e1 - e0; q++) {
+            const int sc = myst[pcol[k][e0 + q]];
+            if (sc <= 2 && (((phi[k][e0 + q] & 0x1FFu) >> (sr + sc)) & 1u)) sub |= 1 << q;
           }
         } else {
+          bool flips = false;
           for (int i = e0; i < e1 && !flips; i++) {
             const int sc = myst[pcol[k][i]];
             flips = sc <= 2 && (((phi[k][i] & 0x1FFu) >> (sr + sc)) & 1u);
           }
+          if (flips) sub = kMergedRow;
         }
       }
-      if (flips) {
-        ListGen Gn, Go;
-        gen_for(Gn, sd, P, phi[k], pcol[k], k, t, myst);
-        gen_for(Go, sd, P, phi[k], pcol[k], k, t, nullptr);
-        uint64_t h = node_hash_init(sd.salt, t);
-        bool diff = false;
-        for (int i = 0; i < sd.mp; i++) {
-          int x = Gn.next(), y = Go.next();
-          if (x != y) diff = true;
-          if (x < 0) break;
-          if (cnt < 3) ps[cnt] = x;
-          h = node_hash_step(h, x);
-          cnt++;
-        }
-        if (diff) {
-          changed = true;
-          hn = h;
-          ent = (unsigned long long)t | ((unsigned long long)(cnt < 3 ? cnt : 3) << 14) |
-                ((unsigned long long)(ps[0] & 0xFFFF) << 16) |
-                ((unsigned long long)(ps[1] & 0xFFFF) << 32) |
-                ((unsigned long long)(ps[2] & 0xFFFF) << 48);
-          if (differs(k, ent)) {
-            // logged in the signature table's keys (free from here on)
-            const int ix = atomicAdd(&SM.nlg, 1);
-            if (ix < HTs) hsk[ix] = ent;
-          }
-        }
-      }
-      unsigned bal = __ballot_sync(0xffffffffu, changed);
-      if (changed) {
-        int pos = nchg + __popc(bal & ((1u << lane) - 1u));
-        dh += hn - P.fh[k * g + t];
-        if (pos < bd.kmax) R[2 + pos] = ent;
-      }
-      nchg += __popc(bal);
+      const unsigned bal = __ballot_sync(0xffffffffu, sub != 0);
+      if (sub) lst[nl + __popc(bal & ((1u << lane) - 1u))] = (uint32_t)t | ((uint32_t)sub << 16);
+      nl += __popc(bal);
+      if (nl > lcap - 32) flush();
     }
+    flush();
     for (int o = 16; o > 0; o >>= 1) dh += __shfl_down_sync(0xffffffffu, dh, o);
     if (lane == 0) {
       R[0] = SM.HF[k] + dh;
