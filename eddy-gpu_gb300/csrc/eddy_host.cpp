@@ -134,19 +134,23 @@ bool compute_thresholds(double alpha_edge, double alpha_edge_prior, int g, int b
 
 // ------------------------------------------------------------ glibc stream
 void GlibcRand::reseed(uint32_t seed) {
+  uint32_t st[31];
   int32_t w = (int32_t)(seed == 0 ? 1u : seed);
-  st_[0] = (uint32_t)w;
+  st[0] = (uint32_t)w;
   for (int i = 1; i < 31; i++) {
     // 16807 * w mod (2^31 - 1) by Schrage's method
     int32_t hi = w / 127773, lo = w % 127773;
     int32_t word = 16807 * lo - 2836 * hi;
     if (word < 0) word += 2147483647;
     w = word;
-    st_[i] = (uint32_t)w;
+    st[i] = (uint32_t)w;
   }
-  f_ = 3;
-  r_ = 0;
-  for (int k = 0; k < 310; k++) (void)next();
+  // glibc's first draw adds word 0 to word 3 (its front pointer starts 3
+  // words ahead of the rear one): in stream order the oldest word is st[3],
+  // then st[4..30], st[0..2]
+  for (int k = 0; k < 31; k++) buf_[k] = st[(k + 3) % 31];
+  fill();
+  skip(310);
 }
 
 void glibc_permutation(GlibcRand &rng, int n, int n_class1, bool relabel, uint8_t *labels,
@@ -155,17 +159,26 @@ void glibc_permutation(GlibcRand &rng, int n, int n_class1, bool relabel, uint8_
   // rand() % n without a division: Lemire, Kaser and Kurz, "Faster
   // remainder by direct computation" (2019), exact for 32-bit operands
   const uint64_t M = UINT64_C(0xFFFFFFFFFFFFFFFF) / un + 1;
-  for (int c = 0; c < n; c++) (void)rng.next();
+  rng.skip(n);
   seen.assign(n, 0);
   order.resize((size_t)n + 1);
   int cnt = 0;
+  uint8_t *sn = seen.data();
+  int *od = order.data();
   // the first n distinct values in draw order, branch-free: every draw is
-  // written at the end of the list, which grows only when it is new
+  // written at the end of the list, which grows only when it is new (a
+  // block of the stream's words at a time, its position in registers)
   while (cnt < n) {
-    const uint32_t r = (uint32_t)(((unsigned __int128)(M * rng.next()) * un) >> 64);
-    order[cnt] = (int)r;
-    cnt += !seen[r];
-    seen[r] = 1;
+    int avail;
+    const uint32_t *w = rng.peek(avail);
+    int k = 0;
+    for (; k < avail && cnt < n; k++) {
+      const uint32_t r = (uint32_t)(((unsigned __int128)(M * (w[k] >> 1)) * un) >> 64);
+      od[cnt] = (int)r;
+      cnt += !sn[r];
+      sn[r] = 1;
+    }
+    rng.advance(k);
   }
   if (relabel) {
     for (int k = 0; k < n_class1; k++) labels[order[k]] = 0;

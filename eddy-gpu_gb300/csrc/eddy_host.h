@@ -27,16 +27,52 @@ class GlibcRand {
   explicit GlibcRand(uint32_t seed = 1) { reseed(seed); }
   void reseed(uint32_t seed);
   inline uint32_t next() {
-    st_[f_] += st_[r_];
-    uint32_t res = st_[f_] >> 1;
-    if (++f_ == 31) f_ = 0;
-    if (++r_ == 31) r_ = 0;
-    return res;
+    if (pos_ == kEnd) refill();
+    return buf_[pos_++] >> 1;
+  }
+  // the raw words of the next *avail draws (at least one; output = word >> 1):
+  // a caller that uses k of them calls advance(k)
+  const uint32_t *peek(int &avail) {
+    if (pos_ == kEnd) refill();
+    avail = kEnd - pos_;
+    return buf_ + pos_;
+  }
+  void advance(int k) { pos_ += k; }
+  // n draws, discarded
+  void skip(int n) {
+    while (n > 0) {
+      if (pos_ == kEnd) refill();
+      const int take = n < kEnd - pos_ ? n : kEnd - pos_;
+      pos_ += take;
+      n -= take;
+    }
   }
 
  private:
-  uint32_t st_[31];
-  int f_ = 3, r_ = 0;
+  // The raw words r[i] = r[i-31] + r[i-3] (mod 2^32) in stream order, a
+  // block at a time: buf_[pos_-31 .. pos_) are the last 31 drawn (the
+  // generator's state), buf_[pos_ ..) the next ones, already computed.  A
+  // copy carries on exactly where the original would.
+  static constexpr int kBlock = 1024, kEnd = 31 + kBlock;
+  void fill() {
+    // the last three words in registers: each new word reads memory only
+    // 31 words back
+    uint32_t a = buf_[28], b = buf_[29], c = buf_[30];
+    for (int j = 31; j < kEnd; j++) {
+      const uint32_t v = buf_[j - 31] + a;
+      buf_[j] = v;
+      a = b;
+      b = c;
+      c = v;
+    }
+    pos_ = 31;
+  }
+  void refill() {
+    for (int j = 0; j < 31; j++) buf_[j] = buf_[kBlock + j];
+    fill();
+  }
+  uint32_t buf_[kEnd];
+  int pos_ = kEnd;
 };
 
 // One iteration of main.cu:541-570: n discarded draws, then the first n
