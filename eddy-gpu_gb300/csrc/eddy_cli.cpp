@@ -10,6 +10,7 @@
 // stream), --seed N (counter stream key), --device N.
 #include <errno.h>
 #include <math.h>
+#include <stdarg.h>
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
@@ -18,11 +19,22 @@
 #include <algorithm>
 #include <string>
 #include <thread>
+#include <unordered_map>
 #include <vector>
 
 #include "eddy_gpu.h"
 
 namespace {
+
+// printf into a string (a set's lines are printed when its turn comes)
+void appendf(std::string &out, const char *fmt, ...) {
+  char buf[4096];
+  va_list ap;
+  va_start(ap, fmt);
+  const int m = vsnprintf(buf, sizeof buf, fmt, ap);
+  va_end(ap);
+  if (m > 0) out.append(buf, (size_t)std::min(m, (int)sizeof buf - 1));
+}
 
 double now_ms() {
   struct timeval tv;
@@ -270,42 +282,58 @@ int main(int argc, char *argv[]) {
   }
 
   fprintf(fpResults, "Pathway\tJS\tPval\tnGenes\n");
+  // gene name -> its first row (main.cu:400-430 takes the first match)
+  std::unordered_map<std::string, int> rowOf;
+  rowOf.reserve((size_t)numGenes * 2);
+  for (int j = 0; j < numGenes; j++) rowOf.emplace(geneNames[j], j);
+  // Every set is read and added first (its lines of main.cu:359-503 kept
+  // for its turn in the output), then one eddy_run runs them all, batched
+  // across sets; the sets' lines, results and files then follow in order,
+  // as the reference prints them.
+  struct SetJob {
+    std::string name, lines;
+    std::vector<std::string> genes;
+    std::vector<uint8_t> prior;
+    bool havePrior = false;
+    int sid = -1;
+  };
+  std::vector<SetJob> jobs;
+  std::string addError, addLines;
   while (read_line(fpGeneSet, line)) {
     if (line[0] == '\n') continue;  // main.cu:361-363
-    const double t_set = now_ms();
+    SetJob J;
     std::vector<std::string> lt = tokens(line, "\n");
     std::vector<std::string> tk = lt.empty() ? std::vector<std::string>() : tokens(lt[0], "\t");
-    std::string pathwayName = tk.empty() ? std::string() : tk[0];
+    J.name = tk.empty() ? std::string() : tk[0];
     std::vector<std::string> setGenes(tk.size() > 2 ? tk.begin() + 2 : tk.end(), tk.end());
-    printf("%s\n", pathwayName.c_str());
-    printf("%d genes in geneset\n", (int)setGenes.size());
+    appendf(J.lines, "%s\n", J.name.c_str());
+    appendf(J.lines, "%d genes in geneset\n", (int)setGenes.size());
     // main.cu:400-430: first matching row, missing genes dropped
-    std::vector<std::string> genesetGenes;
     std::vector<int32_t> gidx;
-    for (auto &s : setGenes)
-      for (int j = 0; j < numGenes; j++)
-        if (geneNames[j] == s) {
-          genesetGenes.push_back(geneNames[j]);
-          gidx.push_back(j);
-          break;
-        }
+    for (auto &gs : setGenes) {
+      auto it = rowOf.find(gs);
+      if (it != rowOf.end()) {
+        J.genes.push_back(geneNames[it->second]);
+        gidx.push_back(it->second);
+      }
+    }
     const int g = (int)gidx.size();
-    printf("Adjusted genes : %d\n", g);
+    appendf(J.lines, "Adjusted genes : %d\n", g);
     // main.cu:432-503 prior file
-    std::string dir = "PRIORS/" + pathwayName + ".prior";
-    if (dir.find('\r') != std::string::npos) printf("File problem! Uses window endings!\n");
+    std::string dir = "PRIORS/" + J.name + ".prior";
+    if (dir.find('\r') != std::string::npos) appendf(J.lines, "File problem! Uses window endings!\n");
     FILE *pf = fopen(dir.c_str(), "r");
-    printf("file : %s\n", dir.c_str());
-    std::vector<uint8_t> prior((size_t)g * g, 0);
-    bool havePrior = pf != nullptr;
-    if (!pf) printf("No prior file exists. Computing without prior knowledge\n");
+    appendf(J.lines, "file : %s\n", dir.c_str());
+    J.prior.assign((size_t)g * g, 0);
+    J.havePrior = pf != nullptr;
+    if (!pf) appendf(J.lines, "No prior file exists. Computing without prior knowledge\n");
     char pbuf[100];
     while (pf && fgets(pbuf, sizeof pbuf, pf)) {
       char *tok = strtok(pbuf, "\t");
       if (!tok) continue;
       int row = -1, col = -1;
       for (int k = 0; k < g; k++)
-        if (genesetGenes[k] == tok) { row = k; break; }
+        if (J.genes[k] == tok) { row = k; break; }
       if (row < 0) continue;
       tok = strtok(nullptr, "\t");
       if (!tok || strcmp(tok, "neighbor-of") == 0) continue;
@@ -314,27 +342,35 @@ int main(int argc, char *argv[]) {
       size_t L = strlen(tok);
       if (L > 0) tok[L - 1] = '\0';
       for (int k = 0; k < g; k++)
-        if (genesetGenes[k] == tok) { col = k; break; }
+        if (J.genes[k] == tok) { col = k; break; }
       if (col < 0) continue;
-      prior[(size_t)row * g + col] = prior[(size_t)col * g + row] = 1;
+      J.prior[(size_t)row * g + col] = J.prior[(size_t)col * g + row] = 1;
     }
     if (pf) fclose(pf);
-    printf("Permutations begin:\n");
-    int sid = -1;
-    if (eddy_add_set(ctx, gidx.data(), g, havePrior ? prior.data() : nullptr, &sid) != EDDY_OK ||
-        eddy_run(ctx) != EDDY_OK) {
-      fprintf(stderr, "eddy: %s\n", eddy_last_error(ctx));
-      exit(EXIT_FAILURE);
+    appendf(J.lines, "Permutations begin:\n");
+    if (eddy_add_set(ctx, gidx.data(), g, J.havePrior ? J.prior.data() : nullptr, &J.sid) != EDDY_OK) {
+      // the sets before it are still run and printed, then its lines
+      addLines = J.lines;
+      addError = eddy_last_error(ctx);
+      break;
     }
+    jobs.push_back(std::move(J));
+  }
+  std::string runError;
+  if (!jobs.empty() && eddy_run(ctx) != EDDY_OK) runError = eddy_last_error(ctx);
+  for (SetJob &J : jobs) {
+    const double t_set = now_ms();
     eddy_set_summary sm;
-    eddy_get_set_summary(ctx, sid, &sm);
+    if (eddy_get_set_summary(ctx, J.sid, &sm) != EDDY_OK) break;  // not run: the run failed
+    const int g = (int)J.genes.size();
+    fputs(J.lines.c_str(), stdout);
     printf("Original Number of unique Networks : %d\n", sm.unique0);
     if (isnan(sm.js0)) printf("jsVal[0] NAN--Breaking permutation loop\n");
     for (int p = 100; p < sm.iterations; p += 100) printf("  Permutation %d finished\n", p);
     printf("permutation loop (%d) finished\n", perms);
     if (sm.failed) {
       fprintf(fpResults, "%s failed with %d genes- one of the js scores was nan\n",
-              pathwayName.c_str(), g);
+              J.name.c_str(), g);
       printf("nan value- quiting!\n\n\n");
       continue;
     }
@@ -342,46 +378,51 @@ int main(int argc, char *argv[]) {
     printf("alpha : %f beta : %f\n", sm.alpha, sm.beta);
     if (!sm.betafit_ok)
       fprintf(stderr, "eddy: beta fit of set %s has alpha/beta outside (0, inf); pDDN "
-                      "undefined\n", pathwayName.c_str());
+                      "undefined\n", J.name.c_str());
     printf("pDDN = %f\n", sm.pddn);
-    fprintf(fpResults, "%s\t%f\t%f\t%d\n", pathwayName.c_str(), sm.js0, sm.pddn, g);
+    fprintf(fpResults, "%s\t%f\t%f\t%d\n", J.name.c_str(), sm.js0, sm.pddn, g);
     fflush(fpResults);
     if (sm.pddn < alphaDDN) {
       int U = 0, E = 0;
-      eddy_get_networks(ctx, sid, &U, &E, nullptr, nullptr, nullptr, nullptr, nullptr);
+      eddy_get_networks(ctx, J.sid, &U, &E, nullptr, nullptr, nullptr, nullptr, nullptr);
       std::vector<int32_t> ids(U), nodes((size_t)U * g), epn(U + 1), edges(E > 0 ? E : 1);
       std::vector<double> lval(2 * (size_t)U);
-      eddy_get_networks(ctx, sid, &U, &E, ids.data(), nodes.data(), epn.data(), edges.data(),
+      eddy_get_networks(ctx, J.sid, &U, &E, ids.data(), nodes.data(), epn.data(), edges.data(),
                         lval.data());
       std::vector<const char *> gn(g);
-      for (int k = 0; k < g; k++) gn[k] = genesetGenes[k].c_str();
-      std::string pn = pathwayName + "_Networks.txt", pb = pathwayName + "_BDEU_SCORES.txt",
-                  pe = pathwayName + "_EdgeList.txt";
-      if (eddy_write_networks(pn.c_str(), inputFile, classFile, pathwayName.c_str(), U, epn.data(),
+      for (int k = 0; k < g; k++) gn[k] = J.genes[k].c_str();
+      std::string pn = J.name + "_Networks.txt", pb = J.name + "_BDEU_SCORES.txt",
+                  pe = J.name + "_EdgeList.txt";
+      if (eddy_write_networks(pn.c_str(), inputFile, classFile, J.name.c_str(), U, epn.data(),
                               gn.data(), g, nodes.data(), edges.data(), epn[U], ids.data()) != EDDY_OK) {
         printf("output when accessing networkOutput.txt is NULL. Error code : %s. Exiting...\n",
                strerror(errno));
         exit(EXIT_FAILURE);
       }
       printf("Finished writing %s\n", pn.c_str());
-      if (eddy_write_bdeu(pb.c_str(), inputFile, classFile, pathwayName.c_str(), class1.c_str(),
+      if (eddy_write_bdeu(pb.c_str(), inputFile, classFile, J.name.c_str(), class1.c_str(),
                           class2.c_str(), U, lval.data()) != EDDY_OK) {
         printf("scoreFile is NULL. Error code : %s. Exiting...\n", strerror(errno));
         exit(EXIT_FAILURE);
       }
       printf("Finished bdeu file %s\n", pb.c_str());
       int EL = 0;
-      eddy_get_edge_list(ctx, sid, &EL, nullptr, nullptr, nullptr);
+      eddy_get_edge_list(ctx, J.sid, &EL, nullptr, nullptr, nullptr);
       std::vector<int32_t> eln(2 * (size_t)g), elp(3), ele(EL > 0 ? EL : 1);
-      eddy_get_edge_list(ctx, sid, &EL, eln.data(), elp.data(), ele.data());
+      eddy_get_edge_list(ctx, J.sid, &EL, eln.data(), elp.data(), ele.data());
       eddy_write_edge_list(pe.c_str(), gn.data(), g, eln.data(), ele.data(), elp.data(),
-                           havePrior ? prior.data() : nullptr, class1.c_str(), class2.c_str());
+                           J.havePrior ? J.prior.data() : nullptr, class1.c_str(), class2.c_str());
       printf("Finished writing edgelist file %s\n", pe.c_str());
       printf("Total run time : %f\n", now_ms() - t_set);
     }
     printf("\nPathway finished.\n\n");
     int msec = (int)(now_ms() - t_set);
     printf("Time taken %d seconds %d milliseconds\n\n\n", msec / 1000, msec % 1000);
+  }
+  if (runError.empty() && !addError.empty()) fputs(addLines.c_str(), stdout);
+  if (!runError.empty() || !addError.empty()) {
+    fprintf(stderr, "eddy: %s\n", (!runError.empty() ? runError : addError).c_str());
+    exit(EXIT_FAILURE);
   }
   fclose(fpGeneSet);
   fclose(fpResults);
